@@ -1,0 +1,137 @@
+"""Pin the CPU oracle against the reference's own known answers (tests/golden/reference_kats.json).
+
+Every value here is evaluated from the reference's test files (test/test_mesh.jl,
+test/test_ScalarFuncSp.jl, test/test_FunctionSpace.jl, test/test_quadrature.jl,
+test/test_basis.jl, examples/poisson2D_HDG.jl); the oracle must reproduce them before any GPU
+result is compared with it.
+"""
+import math
+
+import numpy as np
+import pytest
+
+
+def test_mesh_figure21(oracle, kats, figure_root):
+    m = oracle.parse_mesh_triangle(figure_root)
+    assert m.ncells == 4 and m.nnodes == 5
+    assert m.cells.tolist() == kats["figure2_1_cells"]
+    assert m.xy.tolist() == kats["figure2_1_vertices"]
+    assert m.cell_faces[0].tolist() == kats["figure2_1_cell1_faces"]
+    assert [m.orientation(0, f) for f in range(3)] == kats["figure2_1_cell1_orientation"]
+    assert m.faceset("boundary").tolist() == kats["figure2_1_boundary"]
+    # cell_diameter(mesh,1): longest face of cell 1, src/mesh.jl:126-134
+    d = max(np.linalg.norm(m.xy[m.faces[f - 1, 1] - 1] - m.xy[m.faces[f - 1, 0] - 1]) for f in m.cell_faces[0])
+    assert d == kats["figure2_1_cell1_diameter"]
+    for c in range(4):
+        detJ = m.cell_geometry(c)[0]
+        assert detJ / 2 == pytest.approx(kats["figure2_1_cell_volume"])
+
+
+def test_mesh_rect2x2(oracle, kats):
+    m = oracle.rectangle_mesh(2, 2)
+    assert m.ncells == 8 and m.nnodes == 9 and m.nfaces == 16
+    assert m.cells.tolist() == kats["rect2x2_cells"]
+    assert m.xy.tolist() == kats["rect2x2_vertices"]
+    assert m.cell_faces[0].tolist() == kats["rect2x2_cell1_faces"]
+    assert [m.orientation(0, f) for f in range(3)] == kats["rect2x2_cell1_orientation"]
+    assert m.faceset("boundary").tolist() == kats["rect2x2_boundary"]
+    d = max(np.linalg.norm(m.xy[m.faces[f - 1, 1] - 1] - m.xy[m.faces[f - 1, 0] - 1]) for f in m.cell_faces[0])
+    assert d == kats["rect2x2_cell1_diameter"]
+    for c in range(8):
+        assert m.cell_geometry(c)[0] / 2 == pytest.approx(kats["rect2x2_cell_volume"])
+
+
+def test_geometry_figure21(oracle, kats, figure_root):
+    m = oracle.parse_mesh_triangle(figure_root)
+    for c in range(4):
+        detJ, Jinv, detJf, nrm = m.cell_geometry(c)
+        assert detJ == pytest.approx(kats["figure2_1_detJ"])
+        np.testing.assert_allclose(Jinv, kats["figure2_1_Jinv"][c], rtol=1e-14, atol=1e-14)
+        np.testing.assert_allclose(detJf, kats["figure2_1_detJf"][c], rtol=1e-14)
+        if c == 0:
+            np.testing.assert_allclose(nrm, kats["figure2_1_cell1_normals"], rtol=1e-14, atol=1e-15)
+    # getfacedetJdS(Mh, f, 1) after the loop = detJf of the last cell times the first GL weight
+    t = oracle.tables(1)
+    detJf = m.cell_geometry(3)[2]
+    np.testing.assert_allclose(detJf * t["fw"][0], kats["figure2_1_facedetJdS_last_cell"], rtol=1e-14)
+
+
+def test_golden_element_blocks(oracle, kats, figure_root):
+    m = oracle.parse_mesh_triangle(figure_root)
+    nw, nt = 3, 2
+    assert [2 * nw, nw, 3 * nt] == kats["figure2_1_local_dofs"]
+    for c in range(4):
+        b = oracle.element_blocks(m, c, 1, f=oracle.MANUFACTURED_F)
+        np.testing.assert_allclose(b["A"], kats["figure2_1_Ae_scale"] * np.eye(6), atol=1e-14)
+        np.testing.assert_allclose(b["B"], kats["figure2_1_Be"][c], atol=1e-13)
+        np.testing.assert_allclose(b["C"], kats["figure2_1_Ce"][c], atol=1e-13)
+        np.testing.assert_allclose(b["E"], kats["figure2_1_Ee"][c], atol=1e-13)
+        np.testing.assert_allclose(b["H"], kats["figure2_1_He"][c], atol=1e-14)
+
+
+def test_errornorm_bounds(oracle, kats, figure_root):
+    m = oracle.parse_mesh_triangle(figure_root)
+    r = oracle.solve_poisson(m, 1)
+    e = oracle.errornorm(m, 1, r["u"], oracle.MANUFACTURED_U)
+    assert 0 < e <= kats["figure2_1_errornorm_sq_max"]
+    m = oracle.rectangle_mesh(10, 10)
+    r = oracle.solve_poisson(m, 1)
+    e = oracle.errornorm(m, 1, r["u"], oracle.MANUFACTURED_U)
+    assert 0 < e <= kats["rect10_errornorm_sq_max"]
+
+
+def test_quadrature(oracle, kats):
+    x, y, w = oracle.rule(1, 0)  # Grundmann–Möller s=0
+    np.testing.assert_allclose(w, [0.5])
+    np.testing.assert_allclose([x[0], y[0]], kats["gm0_points"][0])
+    x, y, w = oracle.rule(1, 1)
+    pts = sorted(zip(x.round(12), y.round(12), w))
+    ref = sorted(zip(np.round([p[0] for p in kats["gm1_points"]], 12), np.round([p[1] for p in kats["gm1_points"]], 12),
+                     kats["gm1_weights"]))
+    for a, b in zip(pts, ref):
+        np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-12)
+    for s in range(6):
+        assert oracle.rule(1, s)[2].sum() == pytest.approx(0.5)
+    for o in range(1, 6):
+        assert oracle.rule(0, o)[2].sum() == pytest.approx(0.5)
+    # Gauss-Legendre on (0,1): two points 1/2 -+ 1/(2 sqrt 3), weights 1/2
+    x, _, w = oracle.rule(2, 2)
+    np.testing.assert_allclose(x, [0.5 - 0.5 / math.sqrt(3), 0.5 + 0.5 / math.sqrt(3)], rtol=1e-15)
+    np.testing.assert_allclose(w, [0.5, 0.5], rtol=1e-15)
+
+
+def test_bases(oracle):
+    # test/test_basis.jl:34-39: closed forms equal the generic Jacobi form (values and gradients)
+    x, y, w = oracle.rule(0, 5)
+    for j in range(1, 16):
+        d0 = d1 = 0.0
+        for xi, yi, wi in zip(x, y, w):
+            a, ga = oracle.dubiner(j, xi, yi)
+            b, gb = oracle.dubiner(j, xi, yi, generic=True)
+            d0 += (a - b) ** 2 * wi
+            d1 += ((ga - gb) ** 2).sum() * wi
+        assert d0 < 2.2e-16 and d1 < 2.2e-16
+    # test/test_basis.jl:90-120: orthonormal Legendre on [0,1]
+    ref = [lambda s: 1.0, lambda s: math.sqrt(3) * (2 * s - 1), lambda s: math.sqrt(5) * (6 * s * s - 6 * s + 1),
+           lambda s: math.sqrt(7) * (2 * s - 1) * (10 * s * s - 10 * s + 1)]
+    for k in range(4):
+        for s in (0.1, 0.37, 0.8):
+            assert oracle.lib().hr_legendre(k + 1, s) == pytest.approx(ref[k](s), rel=1e-14, abs=1e-14)
+    # Dubiner basis is orthonormal on the reference triangle (exact rule)
+    t = oracle.tables(4, 9)
+    M = np.einsum("iq,jq,q->ij", t["N"], t["N"], t["vw"])
+    np.testing.assert_allclose(M, np.eye(15), atol=1e-12)
+
+
+def test_trace_system_structure(oracle):
+    # The condensed trace matrix is symmetric and negative definite on the free dofs
+    # (the reason the GPU CG runs on -K restricted to free dofs).
+    m = oracle.rectangle_mesh(4, 4)
+    S = oracle.System(m, 2, f=oracle.MANUFACTURED_F)
+    K, b = S.csc()
+    A = K.toarray()
+    assert np.abs(A - A.T).max() < 1e-12 * np.abs(A).max()
+    dofs, vals = S.dirichlet()
+    free = np.setdiff1d(np.arange(S.ndofs), dofs - 1)
+    ev = np.linalg.eigvalsh(A[np.ix_(free, free)])
+    assert ev.max() < 0
