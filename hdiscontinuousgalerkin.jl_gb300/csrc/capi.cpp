@@ -1,0 +1,671 @@
+// C ABI of libhdg (include/hdg.h): argument checking, object lifetimes, error reporting.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <functional>
+
+#include "hdg_internal.h"
+
+namespace {
+
+thread_local std::string g_err;  // for failures before a context exists
+
+int guard(hdg_ctx* ctx, const std::function<int()>& fn) {
+  try {
+    int rc = fn();
+    return rc;
+  } catch (const HdgError& e) {
+    if (ctx) ctx->err = e.msg;
+    g_err = e.msg;
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    if (ctx) ctx->err = "host allocation failed";
+    g_err = "host allocation failed";
+    return HDG_ERR_OOM;
+  } catch (const std::exception& e) {
+    if (ctx) ctx->err = e.what();
+    g_err = e.what();
+    return HDG_ERR_ARG;
+  }
+}
+
+int fail(hdg_ctx* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  g_err = msg;
+  return code;
+}
+
+void set_device(hdg_ctx* ctx) { HDG_CUDA(cudaSetDevice(ctx->device)); }
+
+}  // namespace
+
+hdg_system::~hdg_system() {
+  if (cg) destroy_cg(cg);
+}
+
+extern "C" {
+
+int hdg_ctx_create(int device, hdg_ctx** out) {
+  if (!out) return HDG_ERR_ARG;
+  return guard(nullptr, [&]() -> int {
+    int n = 0;
+    HDG_CUDA(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return fail(nullptr, HDG_ERR_ARG, "no such CUDA device");
+    hdg_ctx* c = new hdg_ctx();
+    c->device = device;
+    HDG_CUDA(cudaSetDevice(device));
+    HDG_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    c->own_stream = true;
+    *out = c;
+    return HDG_OK;
+  });
+}
+
+int hdg_ctx_destroy(hdg_ctx* ctx) {
+  if (!ctx) return HDG_OK;
+  cudaSetDevice(ctx->device);
+  if (ctx->own_stream && ctx->stream) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+  }
+  delete ctx;
+  return HDG_OK;
+}
+
+const char* hdg_last_error(const hdg_ctx* ctx) { return ctx ? ctx->err.c_str() : g_err.c_str(); }
+
+int hdg_ctx_set_stream(hdg_ctx* ctx, void* stream) {
+  if (!ctx) return HDG_ERR_ARG;
+  return guard(ctx, [&]() -> int {
+    set_device(ctx);
+    if (ctx->own_stream && ctx->stream) {
+      HDG_CUDA(cudaStreamSynchronize(ctx->stream));
+      HDG_CUDA(cudaStreamDestroy(ctx->stream));
+    }
+    if (stream) {
+      ctx->stream = (cudaStream_t)stream;
+      ctx->own_stream = false;
+    } else {
+      HDG_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+      ctx->own_stream = true;
+    }
+    return HDG_OK;
+  });
+}
+
+int64_t hdg_ctx_launch_count(const hdg_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int hdg_ctx_set_profiling(hdg_ctx* ctx, int on) {
+  if (!ctx) return HDG_ERR_ARG;
+  ctx->profiling = on != 0;
+  return HDG_OK;
+}
+
+// ---------------------------------------------------------------- mesh
+// A NULL context builds a host-only mesh (topology queries only; no space can be built on it).
+int hdg_mesh_rectangle(hdg_ctx* ctx, int nx, int ny, const double LL[2], const double UR[2], hdg_mesh** out) {
+  if (!out || nx < 1 || ny < 1 || !LL || !UR) return fail(ctx, HDG_ERR_ARG, "hdg_mesh_rectangle: bad arguments");
+  if ((double)nx * ny * 3.0 + nx + ny > 2.0e9) return fail(ctx, HDG_ERR_ARG, "mesh too large for 32-bit face ids");
+  return guard(ctx, [&]() -> int {
+    if (ctx) set_device(ctx);
+    hdg_mesh* m = new hdg_mesh();
+    m->ctx = ctx;
+    try {
+      mesh_build_rectangle(m, nx, ny, LL, UR);
+      if (ctx) m->upload();
+    } catch (...) {
+      delete m;
+      throw;
+    }
+    *out = m;
+    return HDG_OK;
+  });
+}
+
+int hdg_mesh_from_cells(hdg_ctx* ctx, int nnodes, const double* xy, int ncells, const int32_t* cell_nodes, int nedges,
+                        const int32_t* edges, hdg_mesh** out) {
+  if (!out || nnodes < 3 || ncells < 1 || !xy || !cell_nodes || (nedges > 0 && !edges))
+    return fail(ctx, HDG_ERR_ARG, "hdg_mesh_from_cells: bad arguments");
+  return guard(ctx, [&]() -> int {
+    if (ctx) set_device(ctx);
+    hdg_mesh* m = new hdg_mesh();
+    m->ctx = ctx;
+    int rc = mesh_build_from_cells(m, nnodes, xy, ncells, cell_nodes, nedges, edges);
+    if (rc != HDG_OK) {
+      delete m;
+      return fail(ctx, rc, "hdg_mesh_from_cells: node id out of range");
+    }
+    try {
+      if (ctx) m->upload();
+    } catch (...) {
+      delete m;
+      throw;
+    }
+    *out = m;
+    return HDG_OK;
+  });
+}
+
+int hdg_mesh_set_coordinates(hdg_mesh* m, const double* xy) {
+  if (!m || !xy) return HDG_ERR_ARG;
+  return guard(m->ctx, [&]() -> int {
+    std::memcpy(m->xy.data(), xy, m->xy.size() * sizeof(double));
+    if (!m->ctx) return HDG_OK;
+    set_device(m->ctx);
+    m->upload_coordinates();
+    return HDG_OK;
+  });
+}
+
+int hdg_mesh_jitter(hdg_mesh* m, double a, uint64_t seed) {
+  if (!m || !m->structured || !(a >= 0.0) || a >= 0.35)
+    return fail(m ? m->ctx : nullptr, HDG_ERR_ARG, "hdg_mesh_jitter: needs a rectangle mesh and 0 <= a < 0.35");
+  return guard(m->ctx, [&]() -> int {
+    const double hx = (m->UR[0] - m->LL[0]) / m->nx, hy = (m->UR[1] - m->LL[1]) / m->ny;
+    uint64_t st = seed ^ 0x9E3779B97F4A7C15ull;
+    auto next = [&]() {  // splitmix64 -> uniform in [-1, 1)
+      uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+      z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+      z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+      z ^= z >> 31;
+      return (double)(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+    };
+    const int NX = m->nx + 1;
+    for (int j = 1; j < m->ny; ++j)
+      for (int i = 1; i < m->nx; ++i) {
+        double* p = &m->xy[2 * ((size_t)j * NX + i)];
+        p[0] += a * hx * next();
+        p[1] += a * hy * next();
+      }
+    if (!m->ctx) return HDG_OK;
+    set_device(m->ctx);
+    m->upload_coordinates();
+    HDG_CUDA(cudaStreamSynchronize(m->ctx->stream));
+    return HDG_OK;
+  });
+}
+
+int hdg_mesh_sizes(const hdg_mesh* m, int* nn, int* nc, int* nf) {
+  if (!m) return HDG_ERR_ARG;
+  if (nn) *nn = m->nn;
+  if (nc) *nc = m->nc;
+  if (nf) *nf = m->nf;
+  return HDG_OK;
+}
+
+int hdg_mesh_get_topology(const hdg_mesh* m, double* xy, int32_t* cell_nodes, int32_t* cell_faces, int32_t* faces) {
+  if (!m) return HDG_ERR_ARG;
+  if (xy) std::memcpy(xy, m->xy.data(), m->xy.size() * sizeof(double));
+  if (cell_nodes)
+    for (size_t i = 0; i < m->cells.size(); ++i) cell_nodes[i] = m->cells[i] + 1;
+  if (cell_faces)
+    for (size_t i = 0; i < m->cfaces.size(); ++i) cell_faces[i] = m->cfaces[i] + 1;
+  if (faces)
+    for (size_t i = 0; i < m->faces.size(); ++i) faces[i] = m->faces[i] + 1;  // c2 = -1 -> 0
+  return HDG_OK;
+}
+
+int hdg_mesh_faceset(const hdg_mesh* m, const char* name, int32_t* out, int* count) {
+  if (!m || !name || !count) return HDG_ERR_ARG;
+  auto it = m->facesets.find(name);
+  if (it == m->facesets.end()) return fail(m->ctx, HDG_ERR_UNKNOWN_SET, std::string("no face set ") + name);
+  *count = (int)it->second.size();
+  if (out)
+    for (size_t i = 0; i < it->second.size(); ++i) out[i] = it->second[i] + 1;
+  return HDG_OK;
+}
+
+int hdg_mesh_destroy(hdg_mesh* m) {
+  if (m) {
+    if (m->ctx) {
+      cudaSetDevice(m->ctx->device);
+      cudaStreamSynchronize(m->ctx->stream);
+    }
+    delete m;
+  }
+  return HDG_OK;
+}
+
+// ---------------------------------------------------------------- spaces
+int hdg_space_create(hdg_mesh* mesh, int p, int qd, hdg_space** out) {
+  if (!mesh || !out) return HDG_ERR_ARG;
+  hdg_ctx* ctx = mesh->ctx;
+  if (!ctx) return fail(nullptr, HDG_ERR_ARG, "the mesh was built without a device context");
+  if (p < 1 || p > HDG_MAX_P) return fail(ctx, HDG_ERR_ARG, "degree must be 1..4");
+  if (qd <= 0) qd = p + 1;
+  return guard(ctx, [&]() -> int {
+    set_device(ctx);
+    hdg_space* s = new hdg_space();
+    s->mesh = mesh;
+    if (!build_ref_tables(p, qd, &s->t)) {
+      delete s;
+      return fail(ctx, HDG_ERR_BAD_ORDER, "Quadrature rule of order " + std::to_string(qd) + " not available");
+    }
+    s->d_ref.upload(s->t.packed.data(), s->t.packed.size(), ctx->stream);
+    std::vector<float> pf(s->t.packed.begin(), s->t.packed.end());
+    s->d_reff.upload(pf.data(), pf.size(), ctx->stream);
+    HDG_CUDA(cudaStreamSynchronize(ctx->stream));
+    *out = s;
+    return HDG_OK;
+  });
+}
+
+int hdg_space_info(const hdg_space* s, int* nw, int* nv, int* nt, int* nq, int* nfq) {
+  if (!s) return HDG_ERR_ARG;
+  if (nw) *nw = s->t.nw;
+  if (nv) *nv = 2 * s->t.nw;
+  if (nt) *nt = s->t.nt;
+  if (nq) *nq = s->t.nq;
+  if (nfq) *nfq = s->t.nfq;
+  return HDG_OK;
+}
+
+int hdg_space_tables(const hdg_space* s, double* pts, double* w, double* N, double* dN, double* fpts, double* fw,
+                     double* E, double* T) {
+  if (!s) return HDG_ERR_ARG;
+  const RefTables& t = s->t;
+  if (pts)
+    for (int q = 0; q < t.nq; ++q) { pts[2 * q] = t.qx[q]; pts[2 * q + 1] = t.qy[q]; }
+  if (w) std::memcpy(w, t.qw.data(), t.nq * sizeof(double));
+  if (N) std::memcpy(N, t.N.data(), t.N.size() * sizeof(double));
+  if (dN) std::memcpy(dN, t.dN.data(), t.dN.size() * sizeof(double));
+  if (fpts) std::memcpy(fpts, t.fx.data(), t.nfq * sizeof(double));
+  if (fw) std::memcpy(fw, t.fw.data(), t.nfq * sizeof(double));
+  if (E) std::memcpy(E, t.E.data(), t.E.size() * sizeof(double));
+  if (T) std::memcpy(T, t.T.data(), t.T.size() * sizeof(double));
+  return HDG_OK;
+}
+
+int hdg_space_cell_geometry(const hdg_space* s, int cell, double* detJ, double* Jinv, double* detJf, double* nrm) {
+  if (!s || cell < 1 || cell > s->mesh->nc) return fail(s ? s->mesh->ctx : nullptr, HDG_ERR_ARG, "bad cell");
+  const hdg_mesh* m = s->mesh;
+  const int c = cell - 1;
+  const double* X[3] = {&m->xy[2 * m->cells[3 * c]], &m->xy[2 * m->cells[3 * c + 1]], &m->xy[2 * m->cells[3 * c + 2]]};
+  const double J00 = X[1][0] - X[0][0], J01 = X[2][0] - X[0][0], J10 = X[1][1] - X[0][1], J11 = X[2][1] - X[0][1];
+  const double d = J00 * J11 - J01 * J10;
+  if (!(d > 0.0)) return fail(m->ctx, HDG_ERR_NEG_DETJ, "det(J) is not positive: det(J) = " + std::to_string(d));
+  if (detJ) *detJ = d;
+  if (Jinv) { Jinv[0] = J11 / d; Jinv[1] = -J01 / d; Jinv[2] = -J10 / d; Jinv[3] = J00 / d; }
+  const double wn[3][2] = {{-(J10 - J11), J00 - J01}, {-J11, J01}, {J10, -J00}};
+  for (int f = 0; f < 3; ++f) {
+    const double l = std::sqrt(wn[f][0] * wn[f][0] + wn[f][1] * wn[f][1]);
+    if (detJf) detJf[f] = l;
+    if (nrm) { nrm[2 * f] = wn[f][0] / l; nrm[2 * f + 1] = wn[f][1] / l; }
+  }
+  return HDG_OK;
+}
+
+int hdg_space_destroy(hdg_space* s) {
+  delete s;
+  return HDG_OK;
+}
+
+// ---------------------------------------------------------------- assembly
+static void set_coefficients(hdg_system* s, double tau, const hdg_field* f, const hdg_field* kappa,
+                             const double* kappa_cell) {
+  cudaStream_t st = s->ctx->stream;
+  s->tau = tau;
+  s->f = field_from(f, 0.0);
+  s->d_fprm.upload(s->f.prm.data(), s->f.prm.size(), st);
+  s->kappa_field = kappa != nullptr;
+  s->kappa = field_from(kappa, 1.0);
+  s->d_kprm.upload(s->kappa.prm.data(), s->kappa.prm.size(), st);
+  s->kappa_cells = kappa_cell != nullptr;
+  if (kappa_cell) {
+    for (int c = 0; c < s->nc; ++c)
+      if (!(kappa_cell[c] > 0.0)) throw HdgError{HDG_ERR_ARG, "kappa must be positive"};
+    s->d_kappa.upload(kappa_cell, (size_t)s->nc, st);
+  }
+}
+
+static void assemble_now(hdg_system* s) {
+  cudaStream_t st = s->ctx->stream;
+  const bool prof = s->ctx->profiling;
+  HDG_CUDA(cudaMemsetAsync(s->d_scal.p, 0, 4 * sizeof(double), st));
+  if (prof) s->ev_element.start(st);
+  launch_element_condense(s, st);
+  if (prof) {
+    s->ev_element.stop(st);
+    s->ev_gather.start(st);
+  }
+  launch_gather(s, st);
+  if (prof) s->ev_gather.stop(st);
+  double sc[2];
+  HDG_CUDA(cudaMemcpyAsync(sc, s->d_scal.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  HDG_CUDA(cudaStreamSynchronize(st));
+  int err = 0;
+  std::memcpy(&err, &sc[1], sizeof(int));
+  if (err & 1) throw HdgError{HDG_ERR_NEG_DETJ, "det(J) is not positive on some cell"};
+  if (err & 2) throw HdgError{HDG_ERR_SINGULAR, "a local system has a zero pivot (singular)"};
+  s->applied = false;
+  s->have_solution = false;
+  s->have_recovery = false;
+}
+
+int hdg_assemble_condense(hdg_space* space, double tau, const hdg_field* f, const hdg_field* kappa,
+                          const double* kappa_cell, int precision, hdg_system** out) {
+  if (!space || !out) return HDG_ERR_ARG;
+  hdg_ctx* ctx = space->mesh->ctx;
+  if (!(tau > 0.0)) return fail(ctx, HDG_ERR_ARG, "tau must be positive");
+  if (precision != HDG_PREC_FP64 && precision != HDG_PREC_MIXED) return fail(ctx, HDG_ERR_ARG, "bad precision");
+  return guard(ctx, [&]() -> int {
+    set_device(ctx);
+    hdg_system* s = new hdg_system();
+    try {
+      s->space = space;
+      s->ctx = ctx;
+      s->precision = precision;
+      const RefTables& t = space->t;
+      s->nw = t.nw;
+      s->nt = t.nt;
+      s->n = 3 * t.nw;
+      s->m = 3 * t.nt;
+      s->nc = space->mesh->nc;
+      s->nf = space->mesh->nf;
+      s->ndofs = s->nf * s->nt;
+      set_coefficients(s, tau, f, kappa, kappa_cell);
+      s->d_AB.alloc((size_t)s->nc * s->m * (s->m + 1));
+      s->d_KB.alloc((size_t)s->nc * s->n * (s->m + 1));
+      s->d_scal.alloc(4);
+      build_block_structure(s);
+      s->d_val.alloc((size_t)s->nnz);
+      s->d_b.alloc((size_t)s->ndofs);
+      assemble_now(s);
+    } catch (...) {
+      delete s;
+      throw;
+    }
+    *out = s;
+    return HDG_OK;
+  });
+}
+
+int hdg_system_reassemble(hdg_system* s, double tau, const hdg_field* f, const hdg_field* kappa,
+                          const double* kappa_cell) {
+  if (!s) return HDG_ERR_ARG;
+  if (!(tau > 0.0)) return fail(s->ctx, HDG_ERR_ARG, "tau must be positive");
+  return guard(s->ctx, [&]() -> int {
+    set_device(s->ctx);
+    set_coefficients(s, tau, f, kappa, kappa_cell);
+    assemble_now(s);
+    return HDG_OK;
+  });
+}
+
+int hdg_system_sizes(const hdg_system* s, int* ndofs, int64_t* nnz, int* n, int* m) {
+  if (!s) return HDG_ERR_ARG;
+  if (ndofs) *ndofs = s->ndofs;
+  if (nnz) *nnz = s->nnz;
+  if (n) *n = s->n;
+  if (m) *m = s->m;
+  return HDG_OK;
+}
+
+int hdg_system_get_csc(const hdg_system* s, int base, int64_t* colptr, int64_t* rowval, double* nzval, double* rhs) {
+  if (!s || (base != 0 && base != 1)) return HDG_ERR_ARG;
+  return guard(s->ctx, [&]() -> int {
+    set_device(s->ctx);
+    cudaStream_t st = s->ctx->stream;
+    const int nt = s->nt, nf = s->nf;
+    std::vector<double> val;
+    if (nzval) {
+      val.resize((size_t)s->nnz);
+      s->d_val.download(val.data(), val.size(), st);
+    }
+    std::vector<double> b;
+    if (rhs) {
+      b.resize(s->ndofs);
+      s->d_b.download(b.data(), b.size(), st);
+    }
+    std::vector<uint8_t> pres;
+    if (s->applied) {
+      pres.resize(s->ndofs);
+      s->d_pres.download(pres.data(), pres.size(), st);
+    }
+    HDG_CUDA(cudaStreamSynchronize(st));
+    auto sign = [&](int row) { return (s->applied && !pres[row]) ? -1.0 : 1.0; };
+    // the block pattern is symmetric: column g*nt+j of K holds K[f*nt+i, g*nt+j] for the
+    // blocks (f,g) with f in block row g's neighbour list, rows ascending
+    int64_t pos = 0;
+    if (colptr) colptr[0] = base;
+    for (int g = 0; g < nf; ++g) {
+      const int k0 = s->h_browptr[g], k1 = s->h_browptr[g + 1];
+      for (int j = 0; j < nt; ++j) {
+        for (int k = k0; k < k1; ++k) {
+          const int f = s->h_bcol[k];
+          // partner block (f, g)
+          int kp = -1;
+          for (int q = s->h_browptr[f]; q < s->h_browptr[f + 1]; ++q)
+            if (s->h_bcol[q] == g) { kp = q; break; }
+          for (int i = 0; i < nt; ++i) {
+            const int row = f * nt + i;
+            if (rowval) rowval[pos] = row + base;
+            if (nzval) nzval[pos] = sign(row) * val[(size_t)kp * nt * nt + i * nt + j];
+            ++pos;
+          }
+        }
+        if (colptr) colptr[g * nt + j + 1] = pos + base;
+      }
+    }
+    if (rhs)
+      for (int r = 0; r < s->ndofs; ++r) rhs[r] = sign(r) * b[r];
+    return HDG_OK;
+  });
+}
+
+int hdg_system_get_element_blocks(const hdg_system* s, double* Ate, double* bte, double* Ke, double* be) {
+  if (!s) return HDG_ERR_ARG;
+  return guard(s->ctx, [&]() -> int {
+    set_device(s->ctx);
+    cudaStream_t st = s->ctx->stream;
+    const int n = s->n, m = s->m, nc = s->nc;
+    std::vector<double> AB((size_t)nc * m * (m + 1)), KB((size_t)nc * n * (m + 1));
+    if (Ate || bte) s->d_AB.download(AB.data(), AB.size(), st);
+    if (Ke || be) s->d_KB.download(KB.data(), KB.size(), st);
+    HDG_CUDA(cudaStreamSynchronize(st));
+    for (int c = 0; c < nc; ++c) {
+      for (int i = 0; i < m; ++i) {
+        const double* r = &AB[((size_t)c * m + i) * (m + 1)];
+        if (Ate) std::memcpy(Ate + ((size_t)c * m + i) * m, r, m * sizeof(double));
+        if (bte) bte[(size_t)c * m + i] = r[m];
+      }
+      for (int i = 0; i < n; ++i) {
+        const double* r = &KB[((size_t)c * n + i) * (m + 1)];
+        if (Ke) std::memcpy(Ke + ((size_t)c * n + i) * m, r, m * sizeof(double));
+        if (be) be[(size_t)c * n + i] = r[m];
+      }
+    }
+    return HDG_OK;
+  });
+}
+
+// ---------------------------------------------------------------- Dirichlet
+int hdg_dirichlet(const hdg_space* sp, const char* faceset, const hdg_field* g, int32_t* dofs, double* vals,
+                  int* count) {
+  if (!sp || !faceset || !count) return HDG_ERR_ARG;
+  const hdg_mesh* m = sp->mesh;
+  auto it = m->facesets.find(faceset);
+  if (it == m->facesets.end()) return fail(m->ctx, HDG_ERR_UNKNOWN_SET, std::string("no face set ") + faceset);
+  const RefTables& t = sp->t;
+  const int nt = t.nt, nfq = t.nfq;
+  *count = (int)it->second.size() * nt;
+  if (!dofs && !vals) return HDG_OK;
+  FieldSpec gs = field_from(g, 0.0);
+  static const double EDGE[3][4] = {{1, 0, 0, 1}, {0, 1, 0, 0}, {0, 0, 1, 0}};
+  static const int EN[3][2] = {{1, 2}, {2, 0}, {0, 1}};
+  int k = 0;
+  // faces in increasing id (the reference loops 1:getnfaces and tests membership)
+  for (int32_t f : it->second) {
+    if (m->faces[4 * f + 3] >= 0) return fail(m->ctx, HDG_ERR_NOT_BOUNDARY, "Face " + std::to_string(f + 1) + " is not in boundary");
+    const int c = m->faces[4 * f + 2];
+    int fl = 0;
+    while (m->cfaces[3 * c + fl] != f) ++fl;
+    const bool o = m->cells[3 * c + EN[fl][1]] > m->cells[3 * c + EN[fl][0]];
+    // the reference's projection (src/boundary.jl:232-242): the accumulator N runs across the
+    // basis functions of a face, the weights are the parent's volume weights, no |e|
+    double acc = 0.0;
+    for (int i = 0; i < nt; ++i) {
+      for (int q = 0; q < nfq; ++q) {
+        const int oq = o ? q : nfq - 1 - q;
+        const double s = t.fx[oq];
+        const double ex = (1.0 - s) * EDGE[fl][0] + s * EDGE[fl][2], ey = (1.0 - s) * EDGE[fl][1] + s * EDGE[fl][3];
+        const double L[3] = {1.0 - ex - ey, ex, ey};
+        double xq = 0, yq = 0;
+        for (int a = 0; a < 3; ++a) {
+          xq += L[a] * m->xy[2 * m->cells[3 * c + a]];
+          yq += L[a] * m->xy[2 * m->cells[3 * c + a] + 1];
+        }
+        acc += t.qw[q] * eval_field_host(gs, xq, yq) * t.T[i * nfq + q];
+      }
+      if (vals) vals[k] = acc;
+      if (dofs) dofs[k] = f * nt + i + 1;
+      ++k;
+    }
+  }
+  return HDG_OK;
+}
+
+int hdg_apply_dirichlet(hdg_system* s, const int32_t* dofs, const double* vals, int n) {
+  if (!s || n < 0 || (n > 0 && (!dofs || !vals))) return HDG_ERR_ARG;
+  if (s->applied) return fail(s->ctx, HDG_ERR_ARG, "apply! was already called on this system");
+  return guard(s->ctx, [&]() -> int {
+    set_device(s->ctx);
+    std::vector<int32_t> d0(n);
+    std::vector<double> v(vals, vals + n);
+    for (int k = 0; k < n; ++k) {
+      if (dofs[k] < 1 || dofs[k] > s->ndofs) return fail(s->ctx, HDG_ERR_ARG, "prescribed dof out of range");
+      d0[k] = dofs[k] - 1;
+    }
+    if (s->ctx->profiling) s->ev_apply.start(s->ctx->stream);
+    launch_apply_dirichlet(s, d0, v, s->ctx->stream);
+    if (s->ctx->profiling) s->ev_apply.stop(s->ctx->stream);
+    s->applied = true;
+    return HDG_OK;
+  });
+}
+
+// ---------------------------------------------------------------- solve / recover
+static hdg_solver solver_defaults(const hdg_solver* o) {
+  hdg_solver d{1e-12, 100000, HDG_PREC_FP64, 32, 1e-5};
+  if (!o) return d;
+  hdg_solver r = *o;
+  if (!(r.tol > 0)) r.tol = d.tol;
+  if (r.maxit <= 0) r.maxit = d.maxit;
+  if (r.chunk <= 0) r.chunk = d.chunk;
+  if (!(r.inner_tol > 0)) r.inner_tol = d.inner_tol;
+  return r;
+}
+
+int hdg_solve(hdg_system* s, const hdg_solver* opts, double* uhat, hdg_stats* stats) {
+  if (!s) return HDG_ERR_ARG;
+  if (!s->applied) return fail(s->ctx, HDG_ERR_ARG, "apply the Dirichlet conditions (hdg_apply_dirichlet) first");
+  return guard(s->ctx, [&]() -> int {
+    set_device(s->ctx);
+    hdg_solver o = solver_defaults(opts);
+    int rc = run_solve(s, o, stats);
+    s->have_solution = (rc == HDG_OK || rc == HDG_ERR_NO_CONVERGENCE);
+    if (uhat && s->have_solution) {
+      s->d_x.download(uhat, (size_t)s->ndofs, s->ctx->stream);
+      HDG_CUDA(cudaStreamSynchronize(s->ctx->stream));
+    }
+    if (rc == HDG_ERR_NO_CONVERGENCE) return fail(s->ctx, rc, "CG did not reach the tolerance within maxit");
+    if (rc == HDG_ERR_BREAKDOWN) return fail(s->ctx, rc, "CG breakdown: the trace system is not definite");
+    return rc;
+  });
+}
+
+int hdg_recover(hdg_system* s, double* q, double* u, double* uhat_cell) {
+  if (!s) return HDG_ERR_ARG;
+  if (!s->have_solution) return fail(s->ctx, HDG_ERR_ARG, "solve first");
+  return guard(s->ctx, [&]() -> int {
+    set_device(s->ctx);
+    cudaStream_t st = s->ctx->stream;
+    if (s->ctx->profiling) s->ev_recover.start(st);
+    launch_recover(s, st);
+    if (s->ctx->profiling) s->ev_recover.stop(st);
+    s->have_recovery = true;
+    const int n = s->n, nv = 2 * s->nw, nw = s->nw, nt = s->nt, nc = s->nc;
+    if (q || u) {
+      std::vector<double> qu((size_t)nc * n);
+      s->d_qu.download(qu.data(), qu.size(), st);
+      HDG_CUDA(cudaStreamSynchronize(st));
+      for (int c = 0; c < nc; ++c) {
+        if (q) std::memcpy(q + (size_t)c * nv, &qu[(size_t)c * n], nv * sizeof(double));
+        if (u) std::memcpy(u + (size_t)c * nw, &qu[(size_t)c * n + nv], nw * sizeof(double));
+      }
+    }
+    if (uhat_cell) {
+      std::vector<double> x(s->ndofs);
+      s->d_x.download(x.data(), x.size(), st);
+      HDG_CUDA(cudaStreamSynchronize(st));
+      const hdg_mesh* m = s->space->mesh;
+      for (int c = 0; c < nc; ++c)
+        for (int f = 0; f < 3; ++f)
+          for (int j = 0; j < nt; ++j) uhat_cell[((size_t)c * 3 + f) * nt + j] = x[(size_t)m->cfaces[3 * c + f] * nt + j];
+    }
+    return HDG_OK;
+  });
+}
+
+int hdg_errornorm_l2sq(hdg_system* s, const hdg_field* uex, double* out) {
+  if (!s || !uex || !out) return HDG_ERR_ARG;
+  if (!s->have_recovery) return fail(s->ctx, HDG_ERR_ARG, "recover first");
+  return guard(s->ctx, [&]() -> int {
+    set_device(s->ctx);
+    *out = run_errornorm(s, field_from(uex, 0.0), s->ctx->stream);
+    return HDG_OK;
+  });
+}
+
+int hdg_system_timings(hdg_system* s, hdg_timings* out) {
+  if (!s || !out) return HDG_ERR_ARG;
+  return guard(s->ctx, [&]() -> int {
+    set_device(s->ctx);
+    std::memset(out, 0, sizeof(*out));
+    out->element_ms = s->ev_element.ms();
+    out->gather_ms = s->ev_gather.ms();
+    out->apply_ms = s->ev_apply.ms();
+    out->cg_ms = s->ev_cg.ms();
+    out->recover_ms = s->ev_recover.ms();
+    double ta = 0, tb = 0;
+    for (auto* e : s->ev_cg_a) ta += e->ms();
+    for (auto* e : s->ev_cg_b) tb += e->ms();
+    out->cg_samples = (int)s->ev_cg_a.size();
+    if (out->cg_samples) {
+      out->cg_a_ms = ta / out->cg_samples;
+      out->cg_b_ms = tb / out->cg_samples;
+    }
+    out->cg_iterations = s->cg_iterations;
+    return HDG_OK;
+  });
+}
+
+int hdg_system_destroy(hdg_system* s) {
+  if (s) {
+    cudaSetDevice(s->ctx->device);
+    cudaStreamSynchronize(s->ctx->stream);
+    delete s;
+  }
+  return HDG_OK;
+}
+
+int hdg_solve_poisson(hdg_space* space, double tau, const hdg_field* f, const hdg_field* kappa,
+                      const double* kappa_cell, const char* faceset, const hdg_field* g, const hdg_solver* opts,
+                      double* uhat, double* q, double* u, hdg_stats* stats) {
+  hdg_system* s = nullptr;
+  int prec = opts ? opts->precision : HDG_PREC_FP64;
+  int rc = hdg_assemble_condense(space, tau, f, kappa, kappa_cell, prec, &s);
+  if (rc != HDG_OK) return rc;
+  int cnt = 0;
+  rc = hdg_dirichlet(space, faceset ? faceset : "boundary", g, nullptr, nullptr, &cnt);
+  std::vector<int32_t> dofs(cnt);
+  std::vector<double> vals(cnt);
+  if (rc == HDG_OK) rc = hdg_dirichlet(space, faceset ? faceset : "boundary", g, dofs.data(), vals.data(), &cnt);
+  if (rc == HDG_OK) rc = hdg_apply_dirichlet(s, dofs.data(), vals.data(), cnt);
+  if (rc == HDG_OK) rc = hdg_solve(s, opts, uhat, stats);
+  if (rc == HDG_OK) rc = hdg_recover(s, q, u, nullptr);
+  hdg_system_destroy(s);
+  return rc;
+}
+
+}  // extern "C"

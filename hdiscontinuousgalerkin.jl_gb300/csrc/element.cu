@@ -1,0 +1,289 @@
+// Element assembly + static condensation (the body of doassemble,
+// examples/poisson2D_HDG.jl:77-174), one warp per cell.
+//
+// Per cell the warp
+//   1. gathers the three vertices and forms J, det J, adj(J) = det J * J^-1, the weighted
+//      outward normals wn_f (|wn_f| = |e_f|) and the orientation bits (src/mesh.jl:51-54);
+//   2. writes the augmented local system [Me | EF | Bte] of size n x (n+m+1) into shared memory,
+//      Me = [Ae -Be; Be' Ce], EF = [-Ee; Fe], Bte = [0; be], every block being a combination
+//      of the packed reference matrices of tables.cpp (no per-point basis loops);
+//   3. eliminates with partial pivoting (the LU of `factorize`, :160) and back-substitutes all
+//      m+1 right-hand sides: X = [K_e | b_e] (:171,:173);
+//   4. forms [Ate | bte] = [Ee;Fe]' X - [He | 0] through the factorised form of Ee and Fe
+//      (Ee = wn_f (x) F_{f,o}, Fe = tau |e_f| F_{f,o}), with bte = -[Ee;Fe]' b_e (:172,:174).
+// Outputs per cell: AB = [Ate | bte] (m x (m+1)) and KB = [K_e | b_e] (n x (m+1)), row-major.
+#include "hdg_device.cuh"
+
+namespace {
+
+struct ElemArgs {
+  const double* xy;
+  const int32_t* cells;
+  const uint8_t* orient;
+  const double* ref;
+  int ref_len, nq;
+  int nc;
+  double tau;
+  FieldDev f;
+  FieldDev kf;
+  int kappa_mode;  // 0: kappa = 1, 1: per-cell array, 2: field
+  const double* kcell;
+  double* AB;
+  double* KB;
+  int* err;
+};
+
+constexpr int EWARPS = 4;
+
+template <int P> __global__ void __launch_bounds__(EWARPS * 32) k_element_condense(ElemArgs a) {
+  using D = Dims<P>;
+  constexpr int NW = D::NW, NT = D::NT, NV = D::NV, N = D::N, M = D::M, NC = D::NC, LD = D::LD;
+  extern __shared__ double smem[];
+  double* ref = smem;
+  const int ref_len = a.ref_len;
+  for (int i = threadIdx.x; i < ref_len; i += blockDim.x) ref[i] = a.ref[i];
+  const int nq = a.nq;
+  const RefLayout L = [&] {
+    RefLayout l;
+    int o = 0;
+    l.M = o; o += NW * NW;
+    l.D0 = o; o += NW * NW;
+    l.D1 = o; o += NW * NW;
+    l.C = o; o += 3 * NW * NW;
+    l.F = o; o += 6 * NW * NT;
+    l.H = o; o += NT * NT;
+    l.NW = o; o += NW * nq;
+    l.N = o; o += NW * nq;
+    l.Q = o; o += 2 * nq;
+    l.total = o;
+    return l;
+  }();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wstride = N * LD + 2 * nq + NW + 2;
+  double* W = smem + ((ref_len + 1) & ~1) + warp * wstride;
+  double* sq = W + N * LD;  // per-warp scratch: f (or kappa^-1) at the quadrature points, be
+  __syncthreads();
+
+  for (int e = blockIdx.x * EWARPS + warp; e < a.nc; e += gridDim.x * EWARPS) {
+    // ---- geometry (reinit!, src/ScalarFunctionSpaces.jl:251-282) -------------------------
+    int nid = (lane < 3) ? a.cells[3 * e + lane] : 0;
+    double px = 0.0, py = 0.0;
+    if (lane < 3) {
+      px = a.xy[2 * nid];
+      py = a.xy[2 * nid + 1];
+    }
+    const double x1 = __shfl_sync(0xffffffffu, px, 0), y1 = __shfl_sync(0xffffffffu, py, 0);
+    const double x2 = __shfl_sync(0xffffffffu, px, 1), y2 = __shfl_sync(0xffffffffu, py, 1);
+    const double x3 = __shfl_sync(0xffffffffu, px, 2), y3 = __shfl_sync(0xffffffffu, py, 2);
+    const double J00 = x2 - x1, J01 = x3 - x1, J10 = y2 - y1, J11 = y3 - y1;
+    const double detJ = J00 * J11 - J01 * J10;
+    if (!(detJ > 0.0) && lane == 0) atomicOr(a.err, 1);
+    // adj(J) = detJ * J^-1 ; Be[(c,a),j] = sum_l adj[l][c] D_l[a][j]
+    const double ad00 = J11, ad01 = -J01, ad10 = -J10, ad11 = J00;
+    // weighted normals (src/shapes.jl:80-87)
+    double wn[3][2] = {{-(J10 - J11), J00 - J01}, {-J11, J01}, {J10, -J00}};
+    double el[3];
+#pragma unroll
+    for (int f = 0; f < 3; ++f) el[f] = sqrt(wn[f][0] * wn[f][0] + wn[f][1] * wn[f][1]);
+    const unsigned ob = a.orient[e];
+    const double tau = a.tau;
+    double kinv = 1.0;
+    if (a.kappa_mode == 1) kinv = 1.0 / a.kcell[e];
+    const double smass = kinv * detJ;
+    // ---- source (and kappa field) at the volume points -----------------------------------
+    for (int q = lane; q < nq; q += 32) {
+      double xi = ref[L.Q + 2 * q], eta = ref[L.Q + 2 * q + 1];
+      double xq = (1.0 - xi - eta) * x1 + xi * x2 + eta * x3;
+      double yq = (1.0 - xi - eta) * y1 + xi * y2 + eta * y3;
+      sq[q] = eval_field_dev(a.f, xq, yq);
+      if (a.kappa_mode == 2) sq[nq + q] = 1.0 / eval_field_dev(a.kf, xq, yq);
+    }
+    __syncwarp();
+    double* be = sq + 2 * nq;
+    for (int i = lane; i < NW; i += 32) {
+      double s = 0.0;
+      for (int q = 0; q < nq; ++q) s += ref[L.NW + i * nq + q] * sq[q];
+      be[i] = s * detJ;
+    }
+    __syncwarp();
+    // ---- augmented local system ----------------------------------------------------------
+    for (int idx = lane; idx < N * NC; idx += 32) {
+      const int r = idx / NC, col = idx - (idx / NC) * NC;
+      double v;
+      if (r < NV) {
+        const int c = r / NW, ia = r - c * NW;
+        const double adl0 = c ? ad01 : ad00, adl1 = c ? ad11 : ad10;
+        if (col < NV) {
+          const int c2 = col / NW, ib = col - c2 * NW;
+          if (c2 != c) {
+            v = 0.0;
+          } else if (a.kappa_mode == 2) {
+            double s = 0.0;
+            for (int q = 0; q < nq; ++q) s += ref[L.NW + ia * nq + q] * sq[nq + q] * ref[L.N + ib * nq + q];
+            v = s * detJ;
+          } else {
+            v = smass * ref[L.M + ia * NW + ib];
+          }
+        } else if (col < N) {
+          const int j = col - NV;
+          v = -(adl0 * ref[L.D0 + ia * NW + j] + adl1 * ref[L.D1 + ia * NW + j]);
+        } else if (col < N + M) {
+          const int f = (col - N) / NT, j = (col - N) - f * NT;
+          const int o = (ob >> f) & 1;
+          v = -wn[f][c] * ref[L.F + ((f * 2 + o) * NW + ia) * NT + j];
+        } else {
+          v = 0.0;
+        }
+      } else {
+        const int ia = r - NV;
+        if (col < NV) {
+          const int c2 = col / NW, ib = col - c2 * NW;
+          const double adl0 = c2 ? ad01 : ad00, adl1 = c2 ? ad11 : ad10;
+          v = adl0 * ref[L.D0 + ib * NW + ia] + adl1 * ref[L.D1 + ib * NW + ia];
+        } else if (col < N) {
+          const int ib = col - NV;
+          v = tau * (el[0] * ref[L.C + (0 * NW + ia) * NW + ib] + el[1] * ref[L.C + (1 * NW + ia) * NW + ib] +
+                     el[2] * ref[L.C + (2 * NW + ia) * NW + ib]);
+        } else if (col < N + M) {
+          const int f = (col - N) / NT, j = (col - N) - f * NT;
+          const int o = (ob >> f) & 1;
+          v = tau * el[f] * ref[L.F + ((f * 2 + o) * NW + ia) * NT + j];
+        } else {
+          v = be[ia];
+        }
+      }
+      W[r * LD + col] = v;
+    }
+    __syncwarp();
+    // ---- Gaussian elimination with partial pivoting --------------------------------------
+    for (int k = 0; k < N; ++k) {
+      double best = -1.0;
+      int bi = k;
+      for (int i = k + lane; i < N; i += 32) {
+        double v = fabs(W[i * LD + k]);
+        if (v > best) { best = v; bi = i; }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        double ov = __shfl_xor_sync(0xffffffffu, best, o);
+        int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+      }
+      if (best == 0.0 && lane == 0) atomicOr(a.err, 2);
+      if (bi != k) {
+        for (int j = k + lane; j < NC; j += 32) {
+          double t = W[k * LD + j];
+          W[k * LD + j] = W[bi * LD + j];
+          W[bi * LD + j] = t;
+        }
+        __syncwarp();
+      }
+      const double pinv = 1.0 / W[k * LD + k];
+      for (int i = k + 1 + lane; i < N; i += 32) W[i * LD + k] *= pinv;
+      __syncwarp();
+      const int cols = NC - k - 1, rows = N - k - 1;
+      for (int t = lane; t < rows * cols; t += 32) {
+        const int i = k + 1 + t / cols, j = k + 1 + (t - (t / cols) * cols);
+        W[i * LD + j] -= W[i * LD + k] * W[k * LD + j];
+      }
+      __syncwarp();
+    }
+    // ---- back substitution on the m+1 right-hand sides -----------------------------------
+    for (int k = N - 1; k >= 0; --k) {
+      const double dinv = 1.0 / W[k * LD + k];
+      for (int j = lane; j <= M; j += 32) W[k * LD + N + j] *= dinv;
+      __syncwarp();
+      for (int t = lane; t < k * (M + 1); t += 32) {
+        const int i = t / (M + 1), j = t - (t / (M + 1)) * (M + 1);
+        W[i * LD + N + j] -= W[i * LD + k] * W[k * LD + N + j];
+      }
+      __syncwarp();
+    }
+    // ---- K_e, b_e out; Y_f = wn_f,x X_qx + wn_f,y X_qy + tau |e_f| X_u into the free columns --
+    double* KB = a.KB + (size_t)e * N * (M + 1);
+    for (int t = lane; t < N * (M + 1); t += 32) {
+      const int r = t / (M + 1), j = t - (t / (M + 1)) * (M + 1);
+      KB[t] = W[r * LD + N + j];
+    }
+    for (int t = lane; t < 3 * NW * (M + 1); t += 32) {
+      const int fa = t / (M + 1), j = t - (t / (M + 1)) * (M + 1);
+      const int f = fa / NW, ia = fa - f * NW;
+      W[fa * LD + j] = wn[f][0] * W[ia * LD + N + j] + wn[f][1] * W[(NW + ia) * LD + N + j] +
+                       tau * el[f] * W[(NV + ia) * LD + N + j];
+    }
+    __syncwarp();
+    // ---- [Ate | bte] ----------------------------------------------------------------------
+    double* AB = a.AB + (size_t)e * M * (M + 1);
+    for (int t = lane; t < M * (M + 1); t += 32) {
+      const int row = t / (M + 1), col = t - (t / (M + 1)) * (M + 1);
+      const int f = row / NT, i = row - f * NT;
+      const int o = (ob >> f) & 1;
+      const double* F = ref + L.F + (f * 2 + o) * NW * NT;
+      double s = 0.0;
+#pragma unroll
+      for (int ia = 0; ia < NW; ++ia) s += F[ia * NT + i] * W[(f * NW + ia) * LD + col];
+      double v;
+      if (col < M) {
+        const int g = col / NT, j = col - g * NT;
+        v = (g == f) ? s - el[f] * ref[L.H + i * NT + j] : s;
+      } else {
+        v = -s;
+      }
+      AB[t] = v;
+    }
+    __syncwarp();
+  }
+}
+
+template <int P> void launch_p(hdg_system* s, cudaStream_t st, const ElemArgs& a) {
+  using D = Dims<P>;
+  const int nq = a.nq;
+  const int wstride = D::N * D::LD + 2 * nq + D::NW + 2;
+  size_t smem = (size_t)(((a.ref_len + 1) & ~1) + EWARPS * wstride) * sizeof(double);
+  static bool attr_set = false;
+  if (!attr_set) {
+    HDG_CUDA(cudaFuncSetAttribute(k_element_condense<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr_set = true;
+  }
+  int dev_sms = 152;
+  cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, s->ctx->device);
+  int blocks_per_sm = 0;
+  HDG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_element_condense<P>, EWARPS * 32, smem));
+  if (blocks_per_sm < 1) blocks_per_sm = 1;
+  long need = (a.nc + EWARPS - 1) / EWARPS;
+  long grid = std::min<long>(need, (long)dev_sms * blocks_per_sm * 4);
+  if (grid < 1) grid = 1;
+  k_element_condense<P><<<(unsigned)grid, EWARPS * 32, smem, st>>>(a);
+  HDG_CUDA(cudaGetLastError());
+  s->ctx->launches++;
+}
+
+}  // namespace
+
+void launch_element_condense(hdg_system* s, cudaStream_t st) {
+  hdg_space* sp = s->space;
+  hdg_mesh* m = sp->mesh;
+  ElemArgs a;
+  a.xy = m->d_xy.p;
+  a.cells = m->d_cells.p;
+  a.orient = m->d_orient.p;
+  a.ref = sp->d_ref.p;
+  a.ref_len = (int)sp->t.packed.size();
+  a.nq = sp->t.nq;
+  a.nc = m->nc;
+  a.tau = s->tau;
+  a.f = FieldDev{s->f.kind, (int)s->f.prm.size(), s->d_fprm.p};
+  a.kf = FieldDev{s->kappa.kind, (int)s->kappa.prm.size(), s->d_kprm.p};
+  a.kappa_mode = s->kappa_cells ? 1 : (s->kappa_field ? 2 : 0);
+  a.kcell = s->d_kappa.p;
+  a.AB = s->d_AB.p;
+  a.KB = s->d_KB.p;
+  a.err = reinterpret_cast<int*>(s->d_scal.p + 1);
+  switch (sp->t.p) {
+    case 1: launch_p<1>(s, st, a); break;
+    case 2: launch_p<2>(s, st, a); break;
+    case 3: launch_p<3>(s, st, a); break;
+    case 4: launch_p<4>(s, st, a); break;
+    default: throw HdgError{HDG_ERR_ARG, "degree not supported"};
+  }
+}

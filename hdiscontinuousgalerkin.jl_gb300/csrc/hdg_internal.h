@@ -1,0 +1,222 @@
+// Internal declarations of libhdg (not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/hdg.h"
+
+#define HDG_MAX_P 4
+
+// ------------------------------------------------------------------ errors
+struct HdgError {
+  int code;
+  std::string msg;
+};
+#define HDG_CUDA(call)                                                                          \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess)                                                                      \
+      throw HdgError{e_ == cudaErrorMemoryAllocation ? HDG_ERR_OOM : HDG_ERR_CUDA,              \
+                     std::string(#call) + ": " + cudaGetErrorString(e_)};                       \
+  } while (0)
+
+// ------------------------------------------------------------------ device buffers
+template <class T> struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void alloc(size_t count) {
+    if (count == n && p) return;
+    release();
+    if (count == 0) return;
+    HDG_CUDA(cudaMalloc(&p, count * sizeof(T)));
+    n = count;
+  }
+  void upload(const T* h, size_t count, cudaStream_t s) {
+    alloc(count);
+    if (count) HDG_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+  void download(T* h, size_t count, cudaStream_t s) const {
+    if (count) HDG_CUDA(cudaMemcpyAsync(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, s));
+  }
+};
+
+// ------------------------------------------------------------------ fields
+struct FieldSpec {
+  int kind = HDG_FIELD_CONST;
+  std::vector<double> prm{0.0};
+};
+FieldSpec field_from(const hdg_field* f, double default_const);
+double eval_field_host(const FieldSpec& f, double x, double y);
+
+// POD view passed to kernels: parameters live in device memory
+struct FieldDev {
+  int kind;
+  int np;
+  const double* prm;
+};
+
+// ------------------------------------------------------------------ objects
+struct hdg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  int64_t launches = 0;
+  bool profiling = false;
+};
+
+// A pair of CUDA events bracketing work on one stream (used only while profiling).
+struct EventPair {
+  cudaEvent_t a = nullptr, b = nullptr;
+  bool armed = false;
+  void start(cudaStream_t s) {
+    if (!a) {
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+    }
+    cudaEventRecord(a, s);
+    armed = false;
+  }
+  void stop(cudaStream_t s) {
+    cudaEventRecord(b, s);
+    armed = true;
+  }
+  double ms() {
+    if (!armed) return 0.0;
+    float t = 0.f;
+    cudaEventSynchronize(b);
+    cudaEventElapsedTime(&t, a, b);
+    return t;
+  }
+  ~EventPair() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+};
+
+struct hdg_mesh {
+  hdg_ctx* ctx = nullptr;
+  int nn = 0, nc = 0, nf = 0;
+  std::vector<double> xy;       // [nn][2]
+  std::vector<int32_t> cells;   // [nc][3] 0-based
+  std::vector<int32_t> cfaces;  // [nc][3] 0-based
+  std::vector<int32_t> faces;   // [nf][4] v1 v2 c1 c2, 0-based, c2 = -1 on the boundary
+  std::map<std::string, std::vector<int32_t>> facesets;  // 0-based, sorted
+  bool structured = false;
+  int nx = 0, ny = 0;
+  double LL[2] = {0, 0}, UR[2] = {1, 1};
+  // device copies
+  DevBuf<double> d_xy;
+  DevBuf<int32_t> d_cells, d_cfaces;
+  DevBuf<uint8_t> d_orient;   // bit f = face_orientation(cell, f)
+  DevBuf<int32_t> d_fcell;    // [nf][2] cells of a face (second -1 on the boundary)
+  DevBuf<int8_t> d_flf;       // [nf][2] local face index in those cells
+  void upload();
+  void upload_coordinates();
+};
+
+// Reference-element tables of one (p, quad_degree) pair.
+struct RefTables {
+  int p, qd, nw, nt, nq, nfq;
+  std::vector<double> qx, qy, qw;  // volume rule
+  std::vector<double> fx, fw;      // face rule on (0,1)
+  std::vector<double> N, dN;       // [nw][nq], [nw][nq][2]
+  std::vector<double> E;           // [nw][nfq][3]
+  std::vector<double> T;           // [nt][nfq]
+  // packed device tables (see tables.cpp: ref_layout)
+  std::vector<double> packed;
+};
+bool build_ref_tables(int p, int qd, RefTables* t);
+
+// Offsets of the packed table, in doubles.
+struct RefLayout {
+  int M, D0, D1, C, F, H, NW, N, Q, total;
+};
+RefLayout ref_layout(int nw, int nt, int nq);
+
+struct hdg_space {
+  hdg_mesh* mesh = nullptr;
+  RefTables t;
+  DevBuf<double> d_ref;
+  DevBuf<float> d_reff;
+};
+
+struct CgState;  // cg.cu
+
+struct hdg_system {
+  hdg_space* space = nullptr;
+  hdg_ctx* ctx = nullptr;
+  int precision = HDG_PREC_FP64;
+  int nw, nt, n, m, nc, nf, ndofs;
+  int64_t nblocks, nnz;
+  double tau = 1.0;
+  // per-cell condensed blocks: AB = [Ate | bte] (m x (m+1)), KB = [K_e | b_e] (n x (m+1))
+  DevBuf<double> d_AB, d_KB;
+  DevBuf<float> d_ABf, d_KBf;
+  DevBuf<double> d_kappa;  // per-cell kappa (optional)
+  DevBuf<double> d_fprm, d_kprm;
+  FieldSpec f, kappa;
+  bool kappa_field = false, kappa_cells = false;
+  // block-sparse trace matrix, nt x nt blocks, one block row per face
+  std::vector<int32_t> h_browptr, h_bcol;
+  std::vector<int32_t> h_bsrc;  // [nblocks][2] source (cell*9 + lf*3 + lg) or -1
+  DevBuf<int32_t> d_browptr, d_bcol, d_bsrc, d_dof_prob;
+  DevBuf<double> d_val;   // K values [nblocks][nt][nt]
+  DevBuf<float> d_valf;   // FP32 copy for the mixed solve
+  DevBuf<double> d_b;     // rhs
+  // Dirichlet state
+  bool applied = false;   // apply! done: d_val/d_b are in solver form (free rows negated)
+  DevBuf<uint8_t> d_pres;
+  DevBuf<double> d_gv;    // prescribed values scattered to dofs
+  DevBuf<int32_t> d_dofs; // prescribed dofs (0-based)
+  DevBuf<double> d_dvals;
+  DevBuf<double> d_part;  // reduction partials
+  DevBuf<unsigned> d_cnt; // reduction tickets
+  DevBuf<double> d_scal;  // device scalars: [0] = meandiag, [1] = error flags, [2],[3] = residual norms
+  // profiling
+  EventPair ev_element, ev_gather, ev_apply, ev_cg, ev_recover;
+  std::vector<EventPair*> ev_cg_a, ev_cg_b;
+  int cg_iterations = 0;
+  double mdiag = 0.0;
+  // solution and recovery
+  DevBuf<double> d_x;
+  DevBuf<double> d_qu;  // [nc][n] recovered (q; u)
+  bool have_solution = false, have_recovery = false;
+  CgState* cg = nullptr;
+  ~hdg_system();
+  void ensure_reduction_buffers() {
+    if (!d_part.p) d_part.alloc(2048);
+    if (!d_cnt.p) {
+      d_cnt.alloc(8);
+      HDG_CUDA(cudaMemsetAsync(d_cnt.p, 0, 8 * sizeof(unsigned), ctx->stream));
+    }
+  }
+};
+
+// ------------------------------------------------------------------ kernel launchers
+void launch_element_condense(hdg_system* s, cudaStream_t st);
+void launch_gather(hdg_system* s, cudaStream_t st);
+void launch_apply_dirichlet(hdg_system* s, const std::vector<int32_t>& dofs0, const std::vector<double>& vals,
+                            cudaStream_t st);
+int run_solve(hdg_system* s, const hdg_solver& o, hdg_stats* st);
+void launch_recover(hdg_system* s, cudaStream_t st);
+double run_errornorm(hdg_system* s, const FieldSpec& uex, cudaStream_t st);
+void destroy_cg(CgState* c);
+
+void mesh_build_rectangle(hdg_mesh* m, int nx, int ny, const double LL[2], const double UR[2]);
+int mesh_build_from_cells(hdg_mesh* m, int nnodes, const double* xy, int ncells, const int32_t* cells1, int nedges,
+                          const int32_t* edges1);
+void build_block_structure(hdg_system* s);

@@ -1,0 +1,128 @@
+// Local recovery of (q, u) from the trace solution (get_uσ!, examples/poisson2D_HDG.jl:197-212)
+// and the squared L2 error (errornorm, src/DiscreteFunctions.jl:97-120).
+#include "hdg_device.cuh"
+
+namespace {
+
+// [q; u]_c = K_e u_hat_e + b_e, with u_hat_e gathered face by face, slice (f-1)nt+1 : f nt.
+template <int P>
+__global__ void k_recover(const int nc, const int32_t* __restrict__ cfaces, const double* __restrict__ KB,
+                          const double* __restrict__ x, double* __restrict__ qu) {
+  using D = Dims<P>;
+  constexpr int N = D::N, M = D::M, NT = D::NT;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)nc * N) return;
+  const int c = (int)(t / N), i = (int)(t - (int64_t)c * N);
+  const double* row = KB + ((int64_t)c * N + i) * (M + 1);
+  double s = row[M];
+#pragma unroll
+  for (int f = 0; f < 3; ++f) {
+    const int g = cfaces[3 * c + f];
+#pragma unroll
+    for (int j = 0; j < NT; ++j) s += row[f * NT + j] * x[g * NT + j];
+  }
+  qu[t] = s;
+}
+
+template <int P>
+__global__ void k_errornorm(const int nc, const int32_t* __restrict__ cells, const double* __restrict__ xy,
+                            const double* __restrict__ ref, int nq, int offN, int offQ, const double* __restrict__ qw,
+                            const double* __restrict__ qu, FieldDev uex, double* partial, unsigned* counter,
+                            double* out) {
+  using D = Dims<P>;
+  constexpr int NW = D::NW, N = D::N, NV = D::NV;
+  __shared__ double sh[32];
+  __shared__ bool last;
+  double acc = 0.0;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    const int n0 = cells[3 * c], n1 = cells[3 * c + 1], n2 = cells[3 * c + 2];
+    const double x1 = xy[2 * n0], y1 = xy[2 * n0 + 1], x2 = xy[2 * n1], y2 = xy[2 * n1 + 1];
+    const double x3 = xy[2 * n2], y3 = xy[2 * n2 + 1];
+    const double detJ = (x2 - x1) * (y3 - y1) - (x3 - x1) * (y2 - y1);
+    double el = 0.0;
+    for (int q = 0; q < nq; ++q) {
+      double uh = 0.0;
+#pragma unroll
+      for (int a = 0; a < NW; ++a) uh += qu[(int64_t)c * N + NV + a] * ref[offN + a * nq + q];
+      const double xi = ref[offQ + 2 * q], eta = ref[offQ + 2 * q + 1];
+      const double xq = (1.0 - xi - eta) * x1 + xi * x2 + eta * x3;
+      const double yq = (1.0 - xi - eta) * y1 + xi * y2 + eta * y3;
+      const double d = uh - eval_field_dev(uex, xq, yq);
+      el += d * d * detJ * qw[q];
+    }
+    acc += el;
+  }
+  acc = block_sum<256>(acc, sh);
+  if (threadIdx.x == 0) {
+    partial[blockIdx.x] = acc;
+    __threadfence();
+    last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    double s = 0.0;
+    for (int k = threadIdx.x; k < gridDim.x; k += blockDim.x) s += ((volatile double*)partial)[k];
+    s = block_sum<256>(s, sh);
+    if (threadIdx.x == 0) {
+      out[0] = s;
+      *counter = 0;
+    }
+  }
+}
+
+template <int P> void recover_p(hdg_system* s, cudaStream_t st) {
+  using D = Dims<P>;
+  hdg_mesh* m = s->space->mesh;
+  const int64_t tot = (int64_t)m->nc * D::N;
+  s->d_qu.alloc((size_t)tot);
+  k_recover<P><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(m->nc, m->d_cfaces.p, s->d_KB.p, s->d_x.p, s->d_qu.p);
+  HDG_CUDA(cudaGetLastError());
+  s->ctx->launches++;
+}
+
+template <int P> double errornorm_p(hdg_system* s, const FieldSpec& uex, cudaStream_t st) {
+  hdg_space* sp = s->space;
+  hdg_mesh* m = sp->mesh;
+  const RefTables& t = sp->t;
+  RefLayout L = ref_layout(t.nw, t.nt, t.nq);
+  DevBuf<double> prm, qw, partial, out;
+  prm.upload(uex.prm.data(), uex.prm.size(), st);
+  qw.upload(t.qw.data(), t.qw.size(), st);
+  const int blocks = std::min(1024, (m->nc + 255) / 256);
+  partial.alloc(blocks);
+  out.alloc(1);
+  DevBuf<unsigned> counter;
+  counter.alloc(1);
+  HDG_CUDA(cudaMemsetAsync(counter.p, 0, sizeof(unsigned), st));
+  FieldDev fd{uex.kind, (int)uex.prm.size(), prm.p};
+  k_errornorm<P><<<blocks, 256, 0, st>>>(m->nc, m->d_cells.p, m->d_xy.p, sp->d_ref.p, t.nq, L.N, L.Q, qw.p, s->d_qu.p,
+                                         fd, partial.p, counter.p, out.p);
+  HDG_CUDA(cudaGetLastError());
+  s->ctx->launches++;
+  double h = 0;
+  out.download(&h, 1, st);
+  HDG_CUDA(cudaStreamSynchronize(st));
+  return h;
+}
+
+}  // namespace
+
+void launch_recover(hdg_system* s, cudaStream_t st) {
+  switch (s->space->t.p) {
+    case 1: recover_p<1>(s, st); break;
+    case 2: recover_p<2>(s, st); break;
+    case 3: recover_p<3>(s, st); break;
+    case 4: recover_p<4>(s, st); break;
+  }
+}
+
+double run_errornorm(hdg_system* s, const FieldSpec& uex, cudaStream_t st) {
+  switch (s->space->t.p) {
+    case 1: return errornorm_p<1>(s, uex, st);
+    case 2: return errornorm_p<2>(s, uex, st);
+    case 3: return errornorm_p<3>(s, uex, st);
+    case 4: return errornorm_p<4>(s, uex, st);
+  }
+  return -1.0;
+}

@@ -1,0 +1,217 @@
+/*
+ * hdg.h — C ABI of libhdg, the GB300 (sm_103a) implementation of the 2D HDG Poisson path of
+ * HDiscontinuousGalerkin.jl: per-element assembly over the Dubiner scalar/vector and Legendre
+ * trace spaces, static condensation onto the edge traces, assembly of the global trace system,
+ * its solve, and local recovery of u and q.
+ *
+ * Conventions
+ *   - Every function returns an int status: HDG_OK (0) or a negative HDG_ERR_* code; the
+ *     message of the last failure on a context is hdg_last_error().
+ *   - Ids crossing this boundary are 1-based, as in the reference's Julia data structures
+ *     (cells, faces, nodes, dofs); arrays are caller-owned host memory that the library copies.
+ *   - Matrices are row-major unless stated.  The library owns all device memory behind opaque
+ *     handles.  A context is bound to one device and one CUDA stream and is not thread-safe.
+ *   - The reference has no FFI; each entry point names the Julia function it stands in for.
+ */
+#ifndef HDG_H
+#define HDG_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  HDG_OK = 0,
+  HDG_ERR_ARG = -1,            /* invalid argument / size */
+  HDG_ERR_NEG_DETJ = -2,       /* ArgumentError("det(J) is not positive"), src/ScalarFunctionSpaces.jl:260 */
+  HDG_ERR_BAD_ORDER = -3,      /* ArgumentError("Quadrature rule of order … not available"), src/quadrature.jl:24 */
+  HDG_ERR_NOT_BOUNDARY = -4,   /* "Face … is not in boundary", src/boundary.jl:227 / generate_mesh.jl:80 */
+  HDG_ERR_NO_CONVERGENCE = -5, /* CG reached maxit (no reference counterpart: the reference solves directly) */
+  HDG_ERR_OOM = -6,            /* device allocation failed */
+  HDG_ERR_CUDA = -7,           /* CUDA runtime error */
+  HDG_ERR_SINGULAR = -8,       /* a local system had a zero pivot (LAPACK SingularException) */
+  HDG_ERR_BREAKDOWN = -9,      /* CG breakdown: p'Ap <= 0 (trace system not definite) */
+  HDG_ERR_UNKNOWN_SET = -10,   /* KeyError on a face set name, src/mesh.jl:259 */
+  HDG_ERR_TIMEOUT = -11,       /* a bounded device wait gave up */
+  HDG_ERR_CAPACITY = -12       /* a request exceeds a fixed capacity (admission budget, scratch size) */
+};
+
+/* Scalar fields for the source f, the coefficient kappa, the boundary data g and the exact
+ * solution u_ex.  The reference passes Julia closures; across a C ABI a field is a kind plus
+ * parameters, evaluated on the device.
+ *   HDG_FIELD_CONST       c                                   params = {c}
+ *   HDG_FIELD_SINSIN      a sin(kx pi x) sin(ky pi y)         params = {a, kx, ky}
+ *   HDG_FIELD_BUMPS       sum_k a_k exp(-|x-c_k|^2/(2 s_k^2)) params = {K, (cx, cy, s, a) x K}
+ *   HDG_FIELD_FOURIER     g = g0 + sum_k a_k cos(2 pi (kx x + ky y) + phi_k)
+ *                                                             params = {K, g0, (kx, ky, phi, a) x K}
+ *   HDG_FIELD_EXP_FOURIER exp(g) with g as above                                              */
+enum { HDG_FIELD_CONST = 0, HDG_FIELD_SINSIN = 1, HDG_FIELD_BUMPS = 2, HDG_FIELD_FOURIER = 3, HDG_FIELD_EXP_FOURIER = 4 };
+typedef struct {
+  int kind;
+  int nparams;
+  const double* params;
+} hdg_field;
+
+/* Arithmetic of the element kernels and of the trace solve. */
+enum {
+  HDG_PREC_FP64 = 0,  /* FP64 throughout (the plain path) */
+  HDG_PREC_MIXED = 1  /* FP32 quadrature/condensation + one FP64 refinement step per local solve;
+                         FP32 inner CG inside an FP64 iterative-refinement loop */
+};
+
+typedef struct hdg_ctx hdg_ctx;
+typedef struct hdg_mesh hdg_mesh;
+typedef struct hdg_space hdg_space;
+typedef struct hdg_system hdg_system;
+typedef struct hdg_assembler hdg_assembler;
+
+/* ---- context ------------------------------------------------------------------------- */
+int hdg_ctx_create(int device, hdg_ctx** out);
+int hdg_ctx_destroy(hdg_ctx* ctx);
+const char* hdg_last_error(const hdg_ctx* ctx);
+/* Use a caller-owned cudaStream_t for all work of this context (NULL = the library's own). */
+int hdg_ctx_set_stream(hdg_ctx* ctx, void* cuda_stream);
+/* Number of kernels this context has launched so far (for launch accounting). */
+int64_t hdg_ctx_launch_count(const hdg_ctx* ctx);
+/* Profiling: when on, the library times its own launches with CUDA events on its stream
+ * (element, gather, apply, recover, the CG loop, and a sample of un-graphed CG iterations);
+ * read them with hdg_system_timings.  No reference counterpart (the reference only has @time). */
+int hdg_ctx_set_profiling(hdg_ctx* ctx, int on);
+
+/* ---- mesh ---------------------------------------------------------------------------- */
+/* rectangle_mesh(TriangleCell, (nx,ny), LL, UR): src/generate_mesh.jl:101-143.
+ * With ctx == NULL (here and in hdg_mesh_from_cells) the mesh is host-only: its topology can be
+ * queried, but no space can be built on it. */
+int hdg_mesh_rectangle(hdg_ctx* ctx, int nx, int ny, const double LL[2], const double UR[2], hdg_mesh** out);
+/* Triangle-format mesh from already-parsed arrays: parse_cells! face construction,
+ * src/triangle_mesh.jl:94-154.  cell_nodes: ncells x 3 (1-based); edges: nedges x 3
+ * (v1, v2, boundary marker) as in the .edge file. */
+int hdg_mesh_from_cells(hdg_ctx* ctx, int nnodes, const double* xy, int ncells, const int32_t* cell_nodes,
+                        int nedges, const int32_t* edges, hdg_mesh** out);
+/* Replace all node coordinates (nnodes x 2).  Topology and face sets are kept. */
+int hdg_mesh_set_coordinates(hdg_mesh* mesh, const double* xy);
+/* Move interior nodes of a rectangle mesh by U(-a,a)*h per coordinate (seeded; h = cell size). */
+int hdg_mesh_jitter(hdg_mesh* mesh, double a, uint64_t seed);
+int hdg_mesh_sizes(const hdg_mesh* mesh, int* nnodes, int* ncells, int* nfaces);
+/* Node coordinates (nnodes x 2), cell nodes and faces (ncells x 3, 1-based), and the face
+ * table rows [v1 v2 cell1 cell2] (nfaces x 4, cell2 = 0 on the boundary), src/mesh.jl:227-233.
+ * Any pointer may be NULL. */
+int hdg_mesh_get_topology(const hdg_mesh* mesh, double* xy, int32_t* cell_nodes, int32_t* cell_faces,
+                          int32_t* faces);
+/* getfaceset(mesh, name), sorted ascending, 1-based: src/mesh.jl:259.  out may be NULL. */
+int hdg_mesh_faceset(const hdg_mesh* mesh, const char* name, int32_t* out, int* count);
+int hdg_mesh_destroy(hdg_mesh* mesh);
+
+/* ---- function spaces ----------------------------------------------------------------- */
+/* The triple (ScalarFunctionSpace, VectorFunctionSpace, ScalarTraceFunctionSpace) of
+ * examples/poisson2D_HDG.jl:41-44 over one mesh: Dubiner degree p for u and q (component-major
+ * vector dofs), Legendre degree p on the edges.  quad_degree <= 0 selects the reference default
+ * p+1 (src/ScalarFunctionSpaces.jl:174-179). */
+int hdg_space_create(hdg_mesh* mesh, int p, int quad_degree, hdg_space** out);
+/* getnbasefunctions of W, V and M; getnquadpoints; getnfacequadpoints. */
+int hdg_space_info(const hdg_space* space, int* nw, int* nv, int* nt, int* nq, int* nfq);
+/* Reference tables: volume points (nq x 2), weights (nq), N (nw x nq), dN/dxi (nw x nq x 2),
+ * face points (nfq), face weights (nfq), E (nw x nfq x 3), trace T (nt x nfq).  NULL skips. */
+int hdg_space_tables(const hdg_space* space, double* pts, double* w, double* N, double* dN, double* fpts,
+                     double* fw, double* E, double* T);
+/* reinit!(fs, cell) geometry on the host: detJ, Jinv (2x2), detJf (3), unit normals (3x2).
+ * src/ScalarFunctionSpaces.jl:251-282.  cell is 1-based. */
+int hdg_space_cell_geometry(const hdg_space* space, int cell, double* detJ, double* Jinv, double* detJf,
+                            double* normals);
+int hdg_space_destroy(hdg_space* space);
+
+/* ---- assembly and condensation ------------------------------------------------------- */
+/* doassemble(Vh, Wh, Mh, tau), examples/poisson2D_HDG.jl:58-186, on the device: element
+ * integrals, dense LU condensation, and the deterministic gather into the global trace system
+ * (end_assemble's CSC with duplicates summed, src/assembler.jl:47-49; rhs scatter-add :55-60).
+ * kappa (NULL = 1) scales the (q,v) term as (kappa^-1 q, v); kappa_cell (host, ncells, NULL =
+ * unused) is a piecewise-constant alternative.  precision: HDG_PREC_*. */
+int hdg_assemble_condense(hdg_space* space, double tau, const hdg_field* f, const hdg_field* kappa,
+                          const double* kappa_cell, int precision, hdg_system** out);
+/* Recompute with a new source and/or coefficient on the same mesh and space, reusing every
+ * topology buffer (no reallocation). */
+int hdg_system_reassemble(hdg_system* sys, double tau, const hdg_field* f, const hdg_field* kappa,
+                          const double* kappa_cell);
+/* Trace dofs, stored entries of K, local system size n = 3 nw, trace dofs per cell m = 3 nt. */
+int hdg_system_sizes(const hdg_system* sys, int* ndofs, int64_t* nnz, int* n, int* m);
+/* K and b as the reference holds them (sign included) in CSC; base 0 or 1 (Julia). */
+int hdg_system_get_csc(const hdg_system* sys, int base, int64_t* colptr, int64_t* rowval, double* nzval,
+                       double* rhs);
+/* Per-cell condensed blocks: Ate (ncells x m x m), bte (ncells x m), K_e (ncells x n x m),
+ * b_e (ncells x n); K_element / b_element of examples/poisson2D_HDG.jl:171-174.  NULL skips. */
+int hdg_system_get_element_blocks(const hdg_system* sys, double* Ate, double* bte, double* Ke, double* be);
+
+/* ---- boundary conditions ------------------------------------------------------------- */
+/* Dirichlet(u_hat, mesh, faceset, g), src/boundary.jl:212-247: prescribed trace dofs (1-based)
+ * and values.  The values follow the reference's projection exactly (its accumulator is not
+ * reset between basis functions); they are all 0 for g = 0, the case every example uses.
+ * dofs/vals may be NULL to query count. */
+int hdg_dirichlet(const hdg_space* space, const char* faceset, const hdg_field* g, int32_t* dofs, double* vals,
+                  int* count);
+/* apply!(K, b, dbc), src/boundary.jl:326-363 (APPLY_TRANSPOSE): b -= v K[:,d]; zero rows and
+ * columns of the prescribed dofs; K[d,d] = mean|diag K|; b[d] = v * mean|diag K|. */
+int hdg_apply_dirichlet(hdg_system* sys, const int32_t* dofs, const double* vals, int n);
+
+/* ---- solve --------------------------------------------------------------------------- */
+typedef struct {
+  double tol;         /* relative residual |r|/|b| to reach (default 1e-12) */
+  int maxit;          /* iteration cap (default 100000) */
+  int precision;      /* HDG_PREC_FP64: Jacobi-PCG in FP64; HDG_PREC_MIXED: FP32 inner PCG + FP64 refinement */
+  int chunk;          /* CG iterations per CUDA-graph launch between convergence checks (default 32) */
+  double inner_tol;   /* mixed only: relative reduction per inner solve (default 1e-5) */
+} hdg_solver;
+typedef struct {
+  int iterations;     /* inner CG iterations in total */
+  int outer;          /* outer refinement steps (1 for FP64) */
+  double rel_residual;/* final |b - K u|/|b| measured in FP64 */
+  int converged;
+} hdg_stats;
+/* u_hat = K \ b (examples/poisson2D_HDG.jl:195) by Jacobi-preconditioned CG on the free
+ * trace dofs.  uhat (host, ndofs) may be NULL to keep the result on the device only. */
+int hdg_solve(hdg_system* sys, const hdg_solver* opts, double* uhat, hdg_stats* stats);
+
+/* ---- recovery and errors ------------------------------------------------------------- */
+/* get_uσ!, examples/poisson2D_HDG.jl:197-212 (trace slice for any nt): q (ncells x nv),
+ * u (ncells x nw), uhat per cell (ncells x 3 x nt).  Host outputs; NULL skips a copy. */
+int hdg_recover(hdg_system* sys, double* q, double* u, double* uhat_cell);
+/* errornorm(u_h, u_ex), src/DiscreteFunctions.jl:97-120: the SQUARED L2 error of the last
+ * recovery. */
+int hdg_errornorm_l2sq(hdg_system* sys, const hdg_field* u_exact, double* out);
+int hdg_system_destroy(hdg_system* sys);
+
+typedef struct {
+  double element_ms;   /* element assemble+condense kernel of the last (re)assembly */
+  double gather_ms;    /* matrix + rhs gather of the last (re)assembly */
+  double apply_ms;     /* apply! (meandiag, lift, zeroing) */
+  double cg_ms;        /* whole CG loop of the last solve */
+  double cg_a_ms;      /* mean duration of the CG product kernel (q = A z + beta q), sampled */
+  double cg_b_ms;      /* mean duration of the CG update kernel (x, r, z), sampled */
+  int cg_samples;      /* number of sampled iterations */
+  int cg_iterations;   /* iterations of the last solve */
+  double recover_ms;   /* last recovery */
+} hdg_timings;
+/* Per-phase device times recorded while profiling was on (0 where nothing was recorded). */
+int hdg_system_timings(hdg_system* sys, hdg_timings* out);
+
+/* ---- whole flow ---------------------------------------------------------------------- */
+/* The poisson2D_HDG flow in one call: assemble+condense, Dirichlet on `faceset` with g,
+ * apply!, solve, recover.  Outputs are host arrays (any may be NULL). */
+int hdg_solve_poisson(hdg_space* space, double tau, const hdg_field* f, const hdg_field* kappa,
+                      const double* kappa_cell, const char* faceset, const hdg_field* g, const hdg_solver* opts,
+                      double* uhat, double* q, double* u, hdg_stats* stats);
+
+/* ---- triplet assembler (host) -------------------------------------------------------- */
+/* start_assemble(N) / assemble!(a, edof, Ke) / end_assemble(a), src/assembler.jl:1-60.
+ * Ke is ndofs x ndofs column-major (Julia order); edof is 1-based. */
+int hdg_assembler_create(int64_t sizehint, hdg_assembler** out);
+int hdg_assembler_add(hdg_assembler* a, int ndofs, const int64_t* edof, const double* Ke);
+/* end_assemble -> CSC with duplicates summed; sizes first (colptr may be NULL), then values. */
+int hdg_assembler_finish(hdg_assembler* a, int64_t* nrows, int64_t* ncols, int64_t* nnz);
+int hdg_assembler_get_csc(const hdg_assembler* a, int base, int64_t* colptr, int64_t* rowval, double* nzval);
+int hdg_assembler_destroy(hdg_assembler* a);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HDG_H */

@@ -289,10 +289,12 @@ class System:
         lib().hr_apply(self.h, len(dofs), _ip(dofs), _dp(vals))
 
     def solve(self):
-        """û = K \\ b with SuperLU (examples/poisson2D_HDG.jl:195)."""
+        """û = K \\ b with SuperLU (examples/poisson2D_HDG.jl:195).  The column ordering is minimum
+        degree on A'+A, the analogue of UMFPACK's symmetric strategy for a matrix with a symmetric
+        pattern (Julia's `\\` on a non-Hermitian SparseMatrixCSC calls UMFPACK)."""
         import scipy.sparse.linalg as spla
         K, b = self.csc()
-        return spla.splu(K.tocsc()).solve(b)
+        return spla.splu(K.tocsc(), permc_spec="MMD_AT_PLUS_A").solve(b)
 
     def recover(self, uhat):
         nc = self.mesh.ncells

@@ -1,0 +1,179 @@
+"""GPU parity: libhdg (CUDA, sm_103a) against the CPU oracle on the same inputs.
+
+Tolerances (FP64 path): element blocks and global matrix entries within 1e-12 relative to the
+largest entry; sparsity pattern and dof numbering bit-exact; trace solution within a tolerance
+derived from the CG stopping criterion (relative residual 1e-13 here)."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RTOL_BLOCK = 1e-12
+
+
+@pytest.fixture(scope="module")
+def H():
+    import __graft_entry__ as g
+    g.build()
+    return g.import_package()
+
+
+def spaces(H, mesh, p, qd=None):
+    fe = H.GenericFiniteElement(H.Dubiner(2, H.RefTetrahedron, p))
+    Wh = H.ScalarFunctionSpace(mesh, fe, quad_degree=qd)
+    Vh = H.VectorFunctionSpace(mesh, fe, quad_degree=qd)
+    Mh = H.ScalarTraceFunctionSpace(Wh, H.GenericFiniteElement(H.Legendre(1, H.RefTetrahedron, p)))
+    return Vh, Wh, Mh
+
+
+def rel(a, b):
+    return np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(np.asarray(b)).max(), 1e-300)
+
+
+def compare_system(H, oracle, mesh, omesh, p, qd=None, f=None, kappa=None, kappa_cell=None, tau=1.0, apply=True):
+    f = f or H.MANUFACTURED_F
+    Vh, Wh, Mh = spaces(H, mesh, p, qd)
+    K, b, K_e, b_e = H.doassemble(Vh, Wh, Mh, tau, f, kappa=kappa, kappa_cell=kappa_cell)
+    S = oracle.System(omesh, p, qd, tau, f.as_oracle(), kappa.as_oracle() if kappa is not None else None, kappa_cell)
+    Ate, bte, Ke, be = K.element_blocks()
+    oKe, obe = S.local()
+    assert rel(Ke, oKe) < RTOL_BLOCK
+    assert rel(be, obe) < RTOL_BLOCK
+    if apply:
+        dbc = H.Dirichlet(H.TrialFunction(Mh), mesh, "boundary")
+        od, ov = S.dirichlet()
+        np.testing.assert_array_equal(dbc.prescribed_dofs, od)
+        np.testing.assert_allclose(dbc.values, ov, atol=1e-15)
+        H.apply_(K, b, dbc)
+        S.apply(od, ov)
+    colptr, rowval, nzval, rhs = K.csc(0)
+    oK, ob = S.csc()
+    np.testing.assert_array_equal(colptr, oK.indptr)
+    np.testing.assert_array_equal(rowval, oK.indices)
+    assert rel(nzval, oK.data) < RTOL_BLOCK
+    assert rel(rhs, ob) < RTOL_BLOCK
+    return K, S, (Vh, Wh, Mh)
+
+
+def test_golden_figure21(H, oracle, kats, figure_root):
+    """figure2.1, p=1, tau=1 (test/test_FunctionSpace.jl): blocks, matrix, solution, error bound."""
+    mesh = H.parse_mesh_triangle(figure_root)
+    omesh = oracle.parse_mesh_triangle(figure_root)
+    K, S, (Vh, Wh, Mh) = compare_system(H, oracle, mesh, omesh, 1)
+    uhat = H.solve(K, None, tol=1e-14)
+    ref = S.solve()
+    assert rel(uhat, ref) < 1e-12
+    sigma_h, u_h, uhat_h = H.TrialFunction(Vh), H.TrialFunction(Wh), H.TrialFunction(Mh)
+    K_e = H.system._LocalView(K, "K")
+    H.get_usigma_(sigma_h, u_h, uhat_h, uhat, K_e, None, mesh)
+    oq, ou, ouc = S.recover(ref)
+    assert rel(u_h.m_values, ou) < 1e-11
+    assert rel(sigma_h.m_values, oq) < 1e-11
+    e = H.errornorm(u_h, H.MANUFACTURED_U)
+    assert e == pytest.approx(oracle.errornorm(omesh, 1, ou, oracle.MANUFACTURED_U), rel=1e-10)
+    assert e <= kats["figure2_1_errornorm_sq_max"]
+
+
+def test_rect10_example_bound(H, oracle, kats):
+    """examples/poisson2D_HDG.jl: 10x10, p=1, errornorm <= 6e-5."""
+    mesh = H.rectangle_mesh(H.TriangleCell, (10, 10), (0.0, 0.0), (1.0, 1.0))
+    uhat, q, u, st = H.solve_poisson(mesh, 1, H.MANUFACTURED_F, tol=1e-13)
+    r = oracle.solve_poisson(oracle.rectangle_mesh(10, 10), 1)
+    assert rel(uhat, r["uhat"]) < 1e-11
+    assert rel(u, r["u"]) < 1e-11
+    e = oracle.errornorm(oracle.rectangle_mesh(10, 10), 1, u, oracle.MANUFACTURED_U)
+    assert e <= kats["rect10_errornorm_sq_max"]
+
+
+@pytest.mark.parametrize("n,p,qd", [(2, 1, None), (4, 2, None), (8, 2, None), (5, 3, 6), (4, 4, 9), (32, 1, None),
+                                    (16, 2, None)])
+def test_rectangle_parity(H, oracle, n, p, qd):
+    mesh = H.rectangle_mesh(H.TriangleCell, (n, n), (0.0, 0.0), (1.0, 1.0))
+    omesh = oracle.rectangle_mesh(n, n)
+    K, S, _ = compare_system(H, oracle, mesh, omesh, p, qd)
+    uhat = H.solve(K, None, tol=1e-14)
+    # the recursive CG residual reaches 1e-14; the true FP64 residual plateaus near 1e-13..1e-12
+    assert K.stats.converged and K.stats.rel_residual < 1e-11
+    assert rel(uhat, S.solve()) < 1e-11
+
+
+def test_non_square_box(H, oracle):
+    mesh = H.rectangle_mesh(H.TriangleCell, (6, 3), (-1.0, 0.5), (2.0, 2.0))
+    omesh = oracle.rectangle_mesh(6, 3, (-1.0, 0.5), (2.0, 2.0))
+    compare_system(H, oracle, mesh, omesh, 2, f=H.Field.const(1.0))
+
+
+def test_jitter_kappa_bumps(H, oracle):
+    """The extensions of the precision/batching workloads: jittered nodes, kappa per cell or as
+    exp(Fourier) field, Gaussian-bump source — against the oracle with the same inputs."""
+    rng = np.random.default_rng(3)
+    mesh = H.rectangle_mesh(H.TriangleCell, (8, 8), (0.0, 0.0), (1.0, 1.0))
+    mesh.jitter(0.2, 11)
+    omesh = oracle.rectangle_mesh(8, 8)
+    omesh.set_xy(H.get_vertices_matrix(mesh))
+    f = H.Field.bumps(rng.random((8, 2)), 0.05 + 0.1 * rng.random(8), rng.standard_normal(8))
+    kc = np.exp(rng.uniform(np.log(1e-2), np.log(1e2), mesh.ncells))
+    compare_system(H, oracle, mesh, omesh, 2, f=f, kappa_cell=kc)
+    modes = np.column_stack([rng.integers(-3, 4, 16), rng.integers(-3, 4, 16), rng.uniform(0, 6.28, 16),
+                             rng.standard_normal(16) / 4])
+    kap = H.Field.fourier(0.0, modes, exponential=True)
+    compare_system(H, oracle, mesh, omesh, 3, qd=6, f=f, kappa=kap)
+
+
+def test_convergence_rates(H):
+    """L2 error of u against sin(pi x) sin(pi y): rate ~ p+1 (exact-enough quadrature for p >= 3)."""
+    for p, qd in ((1, None), (2, None), (3, 6)):
+        errs = []
+        for n in (8, 16):
+            mesh = H.rectangle_mesh(H.TriangleCell, (n, n), (0.0, 0.0), (1.0, 1.0))
+            Vh, Wh, Mh = spaces(H, mesh, p, qd)
+            K, b, K_e, b_e = H.doassemble(Vh, Wh, Mh, 1.0, H.MANUFACTURED_F)
+            H.apply_(K, b, H.Dirichlet(H.TrialFunction(Mh), mesh, "boundary"))
+            H.solve(K, b, tol=1e-13)
+            K.recover()
+            errs.append(math.sqrt(K.errornorm(H.MANUFACTURED_U)))
+        rate = math.log2(errs[0] / errs[1])
+        assert rate > p + 0.7, (p, errs, rate)
+
+
+def test_deterministic(H):
+    mesh = H.rectangle_mesh(H.TriangleCell, (16, 16), (0.0, 0.0), (1.0, 1.0))
+    outs = []
+    for _ in range(2):
+        uhat, q, u, st = H.solve_poisson(mesh, 2, H.MANUFACTURED_F, tol=1e-12)
+        outs.append((uhat, u))
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
+def test_reassemble_new_rhs(H, oracle):
+    mesh = H.rectangle_mesh(H.TriangleCell, (6, 6), (0.0, 0.0), (1.0, 1.0))
+    Vh, Wh, Mh = spaces(H, mesh, 2)
+    K, b, _, _ = H.doassemble(Vh, Wh, Mh, 1.0, H.MANUFACTURED_F)
+    K.reassemble(1.0, H.Field.const(3.0))
+    S = oracle.System(oracle.rectangle_mesh(6, 6), 2, None, 1.0, (0, [3.0]))
+    assert rel(K.csc()[3], S.csc()[1]) < RTOL_BLOCK
+
+
+def test_error_paths(H):
+    mesh = H.rectangle_mesh(H.TriangleCell, (4, 4), (0.0, 0.0), (1.0, 1.0))
+    with pytest.raises(H.HDGError) as e:
+        spaces(H, mesh, 4, 8)  # Strang/GM: an even order > 6 is not available (src/quadrature.jl:24)
+    assert e.value.code == -3
+    Vh, Wh, Mh = spaces(H, mesh, 1)
+    with pytest.raises(H.HDGError) as e:
+        H.Dirichlet(H.TrialFunction(Mh), mesh, "nowhere")
+    assert e.value.code == -10
+    K, b, _, _ = H.doassemble(Vh, Wh, Mh, 1.0, H.MANUFACTURED_F)
+    H.apply_(K, b, H.Dirichlet(H.TrialFunction(Mh), mesh, "boundary"))
+    with pytest.raises(H.HDGError) as e:
+        H.solve(K, b, maxit=2, chunk=1)
+    assert e.value.code == -5
+    # a flipped cell: det(J) <= 0 (src/ScalarFunctionSpaces.jl:260)
+    xy = H.get_vertices_matrix(mesh)
+    xy[6] = xy[6] + np.array([0.6, 0.6])
+    mesh.set_coordinates(xy)
+    with pytest.raises(H.HDGError) as e:
+        H.doassemble(Vh, Wh, Mh, 1.0, H.MANUFACTURED_F)
+    assert e.value.code == -2
