@@ -38,13 +38,305 @@ WORKLOADS = {
 }
 
 
+def c4_problems(H, count=256, seed=20240611):
+    """The batching workload: `count` problems, n log-uniform in [8, 128], p uniform in {1,2,3,4},
+    interior nodes jittered by U(-0.2h, 0.2h), per-cell kappa log-uniform in [1e-2, 1e2], f = 8
+    Gaussian bumps (centres uniform in the square, widths 0.03-0.15, amplitudes N(0, 10^2))."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    probs = []
+    for k in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(8), math.log(128)))))
+        p = int(rng.integers(1, 5))
+        f = H.Field.bumps(rng.random((8, 2)), 0.03 + 0.12 * rng.random(8), 10.0 * rng.standard_normal(8))
+        kc = np.exp(rng.uniform(math.log(1e-2), math.log(1e2), 2 * n * n))
+        probs.append(H.Problem(n=n, p=p, f=f, kappa_cell=kc, jitter=0.2, seed=seed + k))
+    return probs
+
+
+def rel_l2(a, b):
+    import numpy as np
+    nb = float(np.linalg.norm(b))
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b))) / (nb if nb > 0 else 1.0)
+
+
+def run_c4(args, ws, rank, local):
+    """Batched workload: the degree-binned batch (one launch sequence for all problems of a
+    degree, interleaved CG) against the plain FP64 path that solves the problems one at a time."""
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as g
+    g.build()
+    H = g.import_package()
+    torch.cuda.set_device(local)
+    ctx = H.Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    probs = c4_problems(H)
+    prec = H.PREC_FP64 if args.precision == "fp64" else H.PREC_MIXED
+    tol = args.tol if args.tol != 1e-12 else 1e-9
+    ncells = sum(2 * pr.n * pr.n for pr in probs)
+
+    # plain FP64 path: one resident system per problem, solved one after another
+    plain = []
+    for pr in probs:
+        m = H.batch.host_mesh(pr)
+        dm = H.rectangle_mesh(H.TriangleCell, (pr.n, pr.n), pr.LL, pr.UR, ctx=ctx)
+        dm.set_coordinates(m._topology()[0])
+        fe = H.GenericFiniteElement(H.Dubiner(2, H.RefTetrahedron, pr.p))
+        Wh = H.ScalarFunctionSpace(dm, fe, quad_degree=pr.qd())
+        Vh = H.VectorFunctionSpace(dm, fe, quad_degree=pr.qd())
+        Mh = H.ScalarTraceFunctionSpace(Wh, H.GenericFiniteElement(H.Legendre(1, H.RefTetrahedron, pr.p)))
+        K, b, _, _ = H.doassemble(Vh, Wh, Mh, pr.tau, pr.f, kappa_cell=pr.kappa_cell)
+        dbc = H.Dirichlet(H.TrialFunction(Mh), dm, "boundary")
+        plain.append((dm, K, dbc, pr))
+
+    def plain_step(keep=False):
+        out = []
+        for dm, K, dbc, pr in plain:
+            K.reassemble(pr.tau, pr.f, kappa_cell=pr.kappa_cell)
+            K.apply_dirichlet(dbc.prescribed_dofs, dbc.values)
+            uh = K.solve(tol=tol, precision=H.PREC_FP64, to_host=keep)
+            r = K.recover(to_host=keep)
+            if keep:
+                out.append((uh, r[0], r[1]))
+        return out
+
+    B = H.Batch(ctx, probs, precision=prec)
+
+    for _ in range(max(args.warmup, 3)):
+        B.solve(tol=tol)
+    plain_step()
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = ctx.launches()
+    barrier(ws)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    steps_ms = []
+    e0.record(stream)
+    for _ in range(args.steps):
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        B.solve(tol=tol)
+        s1.record(stream)
+        s1.synchronize()
+        steps_ms.append(s0.elapsed_time(s1))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = ctx.launches() - launches0
+    clk = clocks.stop()
+    batch_ms = max_over_ranks(e0.elapsed_time(e1), ws) / args.steps
+    value = ws * len(probs) / (batch_ms / 1e3)
+    iters = [s.iterations for s in B.stats]
+
+    # plain path, one timed pass over the batch
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    plain_step()
+    p1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = p0.elapsed_time(p1)
+
+    # accuracy of the batched solutions against the plain FP64 path at tolerance 1e-12
+    ref = []
+    for dm, K, dbc, pr in plain:
+        K.reassemble(pr.tau, pr.f, kappa_cell=pr.kappa_cell)
+        K.apply_dirichlet(dbc.prescribed_dofs, dbc.values)
+        uh = K.solve(tol=1e-12, precision=H.PREC_FP64)
+        q, u, _ = K.recover()
+        ref.append((uh, q, u))
+    sols = B.solutions()
+    err = max(max(rel_l2(a[0], b[0]), rel_l2(a[1], b[1]), rel_l2(a[2], b[2])) for a, b in zip(sols, ref))
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": batch_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64" if prec == H.PREC_MIXED else "f64", "data": "synthetic",
+        "config": {"workload": "c4: 256 independent Poisson problems, n log-uniform [8,128], p uniform {1..4}, "
+                               "jitter 0.2h, per-cell kappa log-uniform [1e-2,1e2], 8 Gaussian bumps; "
+                               f"degree-binned batch, {args.precision}, CG tol {tol:g}",
+                   "problems": len(probs), "cells": ncells, "tol": tol,
+                   "quadrature": "Strang(p+1) for p<=2, Strang(6) for p=3, Grundmann-Moeller(9) for p=4",
+                   "l2": "inputs larger than L2 (per-step condensed blocks of 1.5M cells)"},
+        "plain_fp64_solves_per_s": len(probs) / (plain_ms / 1e3),
+        "speedup_vs_plain": (len(probs) / (batch_ms / 1e3)) / (len(probs) / (plain_ms / 1e3)),
+        "max_rel_l2_err_vs_fp64": err,
+        "converged_fraction": float(np.mean([s.converged for s in B.stats])),
+        "max_rel_residual": float(max(s.rel_residual for s in B.stats)),
+        "cg_iterations_max": max(iters), "cg_iterations_mean": float(np.mean(iters)),
+        "p50_ms": statistics.median(steps_ms), "p99_ms": max(steps_ms),
+        "gpu_launches": launches, "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def draw_shape(rng):
+    n = int(round(math.exp(rng.uniform(math.log(8), math.log(128)))))
+    return n, int(rng.integers(1, 5))
+
+
+def draw_coefficients(H, rng, n):
+    import numpy as np
+    f = H.Field.bumps(rng.random((8, 2)), 0.03 + 0.12 * rng.random(8), 10.0 * rng.standard_normal(8))
+    kc = np.exp(rng.uniform(math.log(1e-2), math.log(1e2), 2 * n * n))
+    return f, kc
+
+
+def run_c5(args, ws, rank, local):
+    """Serving workload: a Poisson stream of solve requests (2000 req/s, seeded); each request is
+    drawn like the batching workload; 70 % reuse one of 32 resident meshes with a new source and
+    coefficient, 30 % come with a new mesh.  The engine admits by HBM budget, runs flights on
+    separate streams and completes requests as their flights converge."""
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as g
+    g.build()
+    H = g.import_package()
+    torch.cuda.set_device(local)
+    ctx = H.Context(local)
+    tol = args.tol if args.tol != 1e-12 else 1e-9
+    nreq = args.requests
+    rate = 2000.0
+    rng = np.random.default_rng(777 + rank)
+    resident = []
+    for k in range(32):
+        n, p = draw_shape(rng)
+        resident.append(H.Problem(n=n, p=p, f=H.Field.const(1.0), jitter=0.2, seed=9000 + k))
+    reqs = []
+    t = 0.0
+    for k in range(nreq):
+        t += rng.exponential(1.0 / rate)
+        if rng.random() < 0.7:
+            mid = int(rng.integers(0, 32))
+            pr = resident[mid]
+            f, kc = draw_coefficients(H, rng, pr.n)
+            reqs.append(dict(t=t, mid=mid, n=pr.n, p=pr.p, f=f, kc=kc, mesh=None, seed=pr.seed))
+        else:
+            n, p = draw_shape(rng)
+            f, kc = draw_coefficients(H, rng, n)
+            sd = 50000 + k
+            reqs.append(dict(t=t, mid=-1, n=n, p=p, f=f, kc=kc, seed=sd,
+                             mesh=H.batch.host_mesh(H.Problem(n=n, p=p, f=f, jitter=0.2, seed=sd))))
+
+    eng = H.Engine(ctx, hbm_budget_gb=args.hbm_budget_gb, max_batch=args.max_batch, max_flights=args.max_flights,
+                   tol=tol, precision=H.PREC_MIXED if args.precision == "mixed" else H.PREC_FP64, keep_results=True)
+    host_res = [H.batch.host_mesh(pr) for pr in resident]
+    mids = [eng.add_resident(hm, pr.p) for hm, pr in zip(host_res, resident)]
+
+    def submit(r):
+        if r["mid"] >= 0:
+            return eng.submit(r["p"], r["f"], r["kc"], mesh_id=mids[r["mid"]])
+        return eng.submit(r["p"], r["f"], r["kc"], mesh=r["mesh"])
+
+    # warm-up: a short burst through the engine (compiles graphs, fills the memory pool)
+    for w in range(max(args.warmup, 3)):
+        for r in reqs[w * 16:(w + 1) * 16]:
+            submit(r)
+        for d in eng.run_until_idle():
+            eng.result(d["id"])
+    torch.cuda.synchronize()
+
+    sample = set(range(0, nreq, max(1, nreq // 12)))
+    id2k, kept = {}, {}
+    lat, its, res, conv = [], [], [], []
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = ctx.launches()
+    t0 = time.perf_counter()
+    i = ndone = 0
+    t_last = 0.0
+    while ndone < nreq:
+        now = time.perf_counter() - t0
+        while i < nreq and reqs[i]["t"] <= now:
+            id2k[submit(reqs[i])] = i
+            i += 1
+        if i < nreq and eng.inflight == 0 and eng.pending == 0 and ndone == i:
+            time.sleep(max(0.0, min(reqs[i]["t"] - now, 0.001)))
+            continue
+        eng.step()
+        for d in eng.poll():
+            k = id2k[d["id"]]
+            uh, q, u = eng.result(d["id"])
+            if k in sample:
+                kept[k] = (uh, q, u)
+            lat.append(d["latency"])
+            its.append(d["iterations"])
+            res.append(d["rel_residual"])
+            conv.append(d["converged"])
+            ndone += 1
+            t_last = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    launches = ctx.launches() - launches0
+    first = reqs[0]["t"]
+    served = nreq / (t_last - first)
+    lat_ms = sorted(1e3 * x for x in lat)
+
+    # plain FP64 path on a sample of the same requests, one at a time, and the accuracy check
+    def plain_solve(r, tol_):
+        pr = H.Problem(n=r["n"], p=r["p"], f=r["f"], kappa_cell=r["kc"], jitter=0.2, seed=r["seed"])
+        hm = H.batch.host_mesh(pr)
+        dm = H.rectangle_mesh(H.TriangleCell, (pr.n, pr.n), ctx=ctx)
+        dm.set_coordinates(hm._topology()[0])
+        fe = H.GenericFiniteElement(H.Dubiner(2, H.RefTetrahedron, pr.p))
+        Wh = H.ScalarFunctionSpace(dm, fe, quad_degree=pr.qd())
+        Vh = H.VectorFunctionSpace(dm, fe, quad_degree=pr.qd())
+        Mh = H.ScalarTraceFunctionSpace(Wh, H.GenericFiniteElement(H.Legendre(1, H.RefTetrahedron, pr.p)))
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        K, b, _, _ = H.doassemble(Vh, Wh, Mh, 1.0, pr.f, kappa_cell=pr.kappa_cell)
+        H.apply_(K, b, H.Dirichlet(H.TrialFunction(Mh), dm, "boundary"))
+        uh = H.solve(K, b, tol=tol_, precision=H.PREC_FP64)
+        q, u, _ = K.recover()
+        t2 = time.perf_counter()
+        return t2 - t1, (uh, q, u)
+
+    errs = []
+    for k, got in kept.items():
+        _, ref = plain_solve(reqs[k], 1e-12)
+        errs.append(max(rel_l2(got[0], ref[0]), rel_l2(got[1].ravel(), ref[1].ravel()),
+                        rel_l2(got[2].ravel(), ref[2].ravel())))
+    plain_t = [plain_solve(reqs[k], tol)[0] for k in range(0, min(nreq, 48))]
+    plain_rate = len(plain_t) / sum(plain_t)
+    line = {
+        "metric": METRIC, "value": served, "unit": "solves/s", "n_gpus": ws, "steps": nreq,
+        "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * (t_last - first) / nreq, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64",
+        "data": "synthetic",
+        "config": {"workload": "c5: Poisson request stream at 2000 req/s (seeded), each drawn like the batching "
+                               "workload; 70% on one of 32 resident meshes with a new source and kappa, 30% new meshes;"
+                               f" continuous batching, {args.precision}, CG tol {tol:g}",
+                   "requests": nreq, "hbm_budget_gb": args.hbm_budget_gb, "max_batch": args.max_batch,
+                   "max_flights": args.max_flights, "step": "one request solved"},
+        "p50_ms": lat_ms[len(lat_ms) // 2], "p99_ms": lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))],
+        "plain_fp64_solves_per_s": plain_rate,
+        "plain_fp64_p50_ms": 1e3 * statistics.median(plain_t),
+        "speedup_vs_plain": served / plain_rate,
+        "max_rel_l2_err_vs_fp64": max(errs) if errs else None, "accuracy_sample": len(errs),
+        "all_converged": bool(all(conv)), "cg_iterations_mean": float(np.mean(its)), "wall_s": wall,
+        "gpu_launches": launches, "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c4", "c5"])
+    ap.add_argument("--requests", type=int, default=2000)
+    ap.add_argument("--hbm-budget-gb", type=float, default=64.0)
+    ap.add_argument("--max-batch", type=int, default=64)
+    ap.add_argument("--max-flights", type=int, default=8)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--tol", type=float, default=1e-12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -355,7 +647,12 @@ def main():
     if args.impl == "reference":
         run_reference(args, ws, rank)
         return
-    run_ours(args, ws, rank, local)
+    if args.workload == "c4":
+        run_c4(args, ws, rank, local)
+    elif args.workload == "c5":
+        run_c5(args, ws, rank, local)
+    else:
+        run_ours(args, ws, rank, local)
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

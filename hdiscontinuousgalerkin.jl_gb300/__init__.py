@@ -7,6 +7,8 @@ CellIterator, start_assemble / assemble_ / end_assemble, doassemble, apply_, sol
 get_usigma_, errornorm.  Everything numerical runs in libhdg.so (CUDA, built in-tree)."""
 from . import _lib
 from ._lib import HDGError, PREC_FP64, PREC_MIXED
+from .batch import Batch, Problem, concat_meshes, problem_offsets
+from .serve import Engine
 from .assembler import Assembler, SparseMatrixCSC, assemble_, end_assemble, start_assemble
 from .context import Context, default_context
 from .fields import MANUFACTURED_F, MANUFACTURED_U, Field

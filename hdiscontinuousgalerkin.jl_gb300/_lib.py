@@ -91,6 +91,20 @@ SIGNATURES = {
     "hdg_system_destroy": ([vp], ip),
     "hdg_solve_poisson": ([vp, C.c_double, C.POINTER(hdg_field), C.POINTER(hdg_field), dp, C.c_char_p,
                            C.POINTER(hdg_field), C.POINTER(hdg_solver), dp, dp, dp, C.POINTER(hdg_stats)], ip),
+    "hdg_mesh_concat": ([vp, ip, C.POINTER(vp), C.POINTER(vp)], ip),
+    "hdg_mesh_problems": ([vp, intp, i32p, i32p, i32p], ip),
+    "hdg_assemble_condense_batch": ([vp, dp, C.POINTER(hdg_field), C.POINTER(hdg_field), dp, ip, C.POINTER(vp)], ip),
+    "hdg_system_reassemble_batch": ([vp, dp, C.POINTER(hdg_field), C.POINTER(hdg_field), dp], ip),
+    "hdg_solve_batch": ([ip, C.POINTER(vp), C.POINTER(hdg_solver), C.POINTER(hdg_stats)], ip),
+    "hdg_system_get_solution": ([vp, dp, dp], ip),
+    "hdg_engine_create": ([vp, C.c_double, ip, ip, C.POINTER(hdg_solver), C.POINTER(vp)], ip),
+    "hdg_engine_add_resident_mesh": ([vp, vp, ip, intp], ip),
+    "hdg_engine_submit": ([vp, ip, vp, ip, ip, C.POINTER(hdg_field), dp, C.c_double, i64p], ip),
+    "hdg_engine_step": ([vp, intp, intp], ip),
+    "hdg_engine_poll": ([vp, ip, i64p, dp, intp, dp, intp, intp], ip),
+    "hdg_engine_result": ([vp, C.c_int64, dp, dp, dp, intp, intp, intp], ip),
+    "hdg_engine_set_keep_results": ([vp, ip], ip),
+    "hdg_engine_destroy": ([vp], ip),
     "hdg_assembler_create": ([C.c_int64, C.POINTER(vp)], ip),
     "hdg_assembler_add": ([vp, ip, i64p, dp], ip),
     "hdg_assembler_finish": ([vp, i64p, i64p, i64p], ip),

@@ -35,9 +35,14 @@ int fail(hdg_ctx* ctx, int code, const std::string& msg) {
   return code;
 }
 
-void set_device(hdg_ctx* ctx) { HDG_CUDA(cudaSetDevice(ctx->device)); }
+void set_device(hdg_ctx* ctx) {
+  HDG_CUDA(cudaSetDevice(ctx->device));
+  g_alloc_stream = ctx->stream;
+}
 
 }  // namespace
+
+thread_local cudaStream_t g_alloc_stream = nullptr;
 
 hdg_system::~hdg_system() {
   if (cg) destroy_cg(cg);
@@ -56,6 +61,11 @@ int hdg_ctx_create(int device, hdg_ctx** out) {
     HDG_CUDA(cudaSetDevice(device));
     HDG_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     c->own_stream = true;
+    // keep freed blocks in this process's pool instead of returning them to the driver
+    cudaMemPool_t pool;
+    HDG_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+    uint64_t keep = UINT64_MAX;
+    HDG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
     *out = c;
     return HDG_OK;
   });
@@ -301,21 +311,53 @@ int hdg_space_destroy(hdg_space* s) {
 }
 
 // ---------------------------------------------------------------- assembly
-static void set_coefficients(hdg_system* s, double tau, const hdg_field* f, const hdg_field* kappa,
-                             const double* kappa_cell) {
+// Per-problem coefficients: f[P], kappa[P] (fields, or NULL), tau[P]; kappa_cell over all cells.
+static void set_coefficients_many(hdg_system* s, const double* taus, const hdg_field* const* f,
+                                  const hdg_field* const* kappa, const double* kappa_cell) {
   cudaStream_t st = s->ctx->stream;
-  s->tau = tau;
-  s->f = field_from(f, 0.0);
-  s->d_fprm.upload(s->f.prm.data(), s->f.prm.size(), st);
-  s->kappa_field = kappa != nullptr;
-  s->kappa = field_from(kappa, 1.0);
-  s->d_kprm.upload(s->kappa.prm.data(), s->kappa.prm.size(), st);
+  const int np = s->nprob;
+  s->fsp.assign(np, FieldSpec());
+  s->ksp.assign(np, FieldSpec());
+  s->taus.assign(np, 1.0);
+  std::vector<int32_t> fk(np), fo(np), kk(np), ko(np);
+  std::vector<double> fp, kp;
+  s->kappa_field = false;
+  for (int P = 0; P < np; ++P) {
+    s->taus[P] = taus ? taus[P] : 1.0;
+    if (!(s->taus[P] > 0.0)) throw HdgError{HDG_ERR_ARG, "tau must be positive"};
+    s->fsp[P] = field_from(f ? f[P] : nullptr, 0.0);
+    s->ksp[P] = field_from(kappa ? kappa[P] : nullptr, 1.0);
+    if (kappa && kappa[P]) s->kappa_field = true;
+    fk[P] = s->fsp[P].kind;
+    fo[P] = (int32_t)fp.size();
+    fp.insert(fp.end(), s->fsp[P].prm.begin(), s->fsp[P].prm.end());
+    kk[P] = s->ksp[P].kind;
+    ko[P] = (int32_t)kp.size();
+    kp.insert(kp.end(), s->ksp[P].prm.begin(), s->ksp[P].prm.end());
+  }
+  s->d_fkind.upload(fk.data(), np, st);
+  s->d_foff.upload(fo.data(), np, st);
+  s->d_fprm.upload(fp.data(), fp.size(), st);
+  s->d_kkind.upload(kk.data(), np, st);
+  s->d_koff.upload(ko.data(), np, st);
+  s->d_kprm.upload(kp.data(), kp.size(), st);
+  s->d_tau.upload(s->taus.data(), np, st);
+  s->tau = s->taus[0];
   s->kappa_cells = kappa_cell != nullptr;
   if (kappa_cell) {
     for (int c = 0; c < s->nc; ++c)
       if (!(kappa_cell[c] > 0.0)) throw HdgError{HDG_ERR_ARG, "kappa must be positive"};
     s->d_kappa.upload(kappa_cell, (size_t)s->nc, st);
   }
+  HDG_CUDA(cudaStreamSynchronize(st));  // the host staging vectors go out of scope
+}
+
+// The same source, coefficient and tau for every problem of the system.
+static void set_coefficients(hdg_system* s, double tau, const hdg_field* f, const hdg_field* kappa,
+                             const double* kappa_cell) {
+  std::vector<const hdg_field*> fs(s->nprob, f), ks(s->nprob, kappa);
+  std::vector<double> ts(s->nprob, tau);
+  set_coefficients_many(s, ts.data(), fs.data(), kappa ? ks.data() : nullptr, kappa_cell);
 }
 
 static void assemble_now(hdg_system* s) {
@@ -342,11 +384,13 @@ static void assemble_now(hdg_system* s) {
   s->have_recovery = false;
 }
 
-int hdg_assemble_condense(hdg_space* space, double tau, const hdg_field* f, const hdg_field* kappa,
-                          const double* kappa_cell, int precision, hdg_system** out) {
+static int assemble_condense_impl(hdg_space* space, double tau, const hdg_field* f, const hdg_field* kappa,
+                                  const double* kappa_cell, int precision, const double* taus_many,
+                                  const hdg_field* const* fields_many, const hdg_field* const* kappas_many,
+                                  hdg_system** out) {
   if (!space || !out) return HDG_ERR_ARG;
   hdg_ctx* ctx = space->mesh->ctx;
-  if (!(tau > 0.0)) return fail(ctx, HDG_ERR_ARG, "tau must be positive");
+  if (!fields_many && !(tau > 0.0)) return fail(ctx, HDG_ERR_ARG, "tau must be positive");
   if (precision != HDG_PREC_FP64 && precision != HDG_PREC_MIXED) return fail(ctx, HDG_ERR_ARG, "bad precision");
   return guard(ctx, [&]() -> int {
     set_device(ctx);
@@ -363,12 +407,15 @@ int hdg_assemble_condense(hdg_space* space, double tau, const hdg_field* f, cons
       s->nc = space->mesh->nc;
       s->nf = space->mesh->nf;
       s->ndofs = s->nf * s->nt;
-      set_coefficients(s, tau, f, kappa, kappa_cell);
+      s->nprob = space->mesh->nprob;
+      if (fields_many) set_coefficients_many(s, taus_many, fields_many, kappas_many, kappa_cell);
+      else set_coefficients(s, tau, f, kappa, kappa_cell);
       s->d_AB.alloc((size_t)s->nc * s->m * (s->m + 1));
       s->d_KB.alloc((size_t)s->nc * s->n * (s->m + 1));
       s->d_scal.alloc(4);
       build_block_structure(s);
-      s->d_val.alloc((size_t)s->nnz);
+      build_segments(s);
+      s->d_val.alloc((size_t)hdg_system::SLOTS * s->nt * s->ndofs);
       s->d_b.alloc((size_t)s->ndofs);
       assemble_now(s);
     } catch (...) {
@@ -376,6 +423,40 @@ int hdg_assemble_condense(hdg_space* space, double tau, const hdg_field* f, cons
       throw;
     }
     *out = s;
+    return HDG_OK;
+  });
+}
+
+int hdg_assemble_condense(hdg_space* space, double tau, const hdg_field* f, const hdg_field* kappa,
+                          const double* kappa_cell, int precision, hdg_system** out) {
+  return assemble_condense_impl(space, tau, f, kappa, kappa_cell, precision, nullptr, nullptr, nullptr, out);
+}
+
+int hdg_assemble_condense_batch(hdg_space* space, const double* tau, const hdg_field* f, const hdg_field* kappa,
+                                const double* kappa_cell, int precision, hdg_system** out) {
+  if (!space || !f || !out) return HDG_ERR_ARG;
+  const int np = space->mesh->nprob;
+  std::vector<const hdg_field*> fs(np), ks(np);
+  for (int P = 0; P < np; ++P) {
+    fs[P] = &f[P];
+    ks[P] = kappa ? &kappa[P] : nullptr;
+  }
+  return assemble_condense_impl(space, 1.0, nullptr, nullptr, kappa_cell, precision, tau, fs.data(),
+                                kappa ? ks.data() : nullptr, out);
+}
+
+int hdg_system_reassemble_batch(hdg_system* s, const double* tau, const hdg_field* f, const hdg_field* kappa,
+                                const double* kappa_cell) {
+  if (!s || !f) return HDG_ERR_ARG;
+  return guard(s->ctx, [&]() -> int {
+    set_device(s->ctx);
+    std::vector<const hdg_field*> fs(s->nprob), ks(s->nprob);
+    for (int P = 0; P < s->nprob; ++P) {
+      fs[P] = &f[P];
+      ks[P] = kappa ? &kappa[P] : nullptr;
+    }
+    set_coefficients_many(s, tau, fs.data(), kappa ? ks.data() : nullptr, kappa_cell);
+    assemble_now(s);
     return HDG_OK;
   });
 }
@@ -409,9 +490,12 @@ int hdg_system_get_csc(const hdg_system* s, int base, int64_t* colptr, int64_t* 
     const int nt = s->nt, nf = s->nf;
     std::vector<double> val;
     if (nzval) {
-      val.resize((size_t)s->nnz);
+      val.resize((size_t)hdg_system::SLOTS * nt * s->ndofs);
       s->d_val.download(val.data(), val.size(), st);
     }
+    const size_t nd = (size_t)s->ndofs;
+    // value of K[f nt + i, g nt + j] where g sits in slot k of block row f
+    auto kval = [&](int f, int k, int i, int j) { return val[(size_t)(k * nt + j) * nd + (size_t)f * nt + i]; };
     std::vector<double> b;
     if (rhs) {
       b.resize(s->ndofs);
@@ -433,14 +517,14 @@ int hdg_system_get_csc(const hdg_system* s, int base, int64_t* colptr, int64_t* 
       for (int j = 0; j < nt; ++j) {
         for (int k = k0; k < k1; ++k) {
           const int f = s->h_bcol[k];
-          // partner block (f, g)
+          // slot of block (f, g) in block row f
           int kp = -1;
           for (int q = s->h_browptr[f]; q < s->h_browptr[f + 1]; ++q)
-            if (s->h_bcol[q] == g) { kp = q; break; }
+            if (s->h_bcol[q] == g) { kp = q - s->h_browptr[f]; break; }
           for (int i = 0; i < nt; ++i) {
             const int row = f * nt + i;
             if (rowval) rowval[pos] = row + base;
-            if (nzval) nzval[pos] = sign(row) * val[(size_t)kp * nt * nt + i * nt + j];
+            if (nzval) nzval[pos] = sign(row) * kval(f, kp, i, j);
             ++pos;
           }
         }
@@ -645,6 +729,79 @@ int hdg_system_destroy(hdg_system* s) {
     cudaSetDevice(s->ctx->device);
     cudaStreamSynchronize(s->ctx->stream);
     delete s;
+  }
+  return HDG_OK;
+}
+
+int hdg_solve_batch(int nsys, hdg_system* const* systems, const hdg_solver* opts, hdg_stats* stats) {
+  if (nsys < 1 || !systems) return HDG_ERR_ARG;
+  hdg_ctx* ctx = systems[0]->ctx;
+  for (int i = 0; i < nsys; ++i) {
+    if (!systems[i]) return HDG_ERR_ARG;
+    if (!systems[i]->applied) return fail(systems[i]->ctx, HDG_ERR_ARG, "apply the Dirichlet conditions first");
+  }
+  return guard(ctx, [&]() -> int {
+    set_device(ctx);
+    hdg_solver o = solver_defaults(opts);
+    std::vector<hdg_system*> v(systems, systems + nsys);
+    std::vector<std::vector<hdg_stats>> st;
+    int rc = run_solve_many(v, o, &st);
+    size_t k = 0;
+    for (int i = 0; i < nsys; ++i) {
+      v[i]->have_solution = (rc == HDG_OK || rc == HDG_ERR_NO_CONVERGENCE);
+      for (auto& r : st[i]) {
+        if (stats) stats[k] = r;
+        ++k;
+      }
+    }
+    if (rc == HDG_ERR_NO_CONVERGENCE) return fail(ctx, rc, "some problem did not reach the tolerance within maxit");
+    if (rc == HDG_ERR_BREAKDOWN) return fail(ctx, rc, "CG breakdown in some problem");
+    return rc;
+  });
+}
+
+int hdg_system_get_solution(const hdg_system* s, double* uhat, double* qu) {
+  if (!s || !s->have_solution) return HDG_ERR_ARG;
+  return guard(s->ctx, [&]() -> int {
+    set_device(s->ctx);
+    if (uhat) s->d_x.download(uhat, (size_t)s->ndofs, s->ctx->stream);
+    if (qu) {
+      if (!s->have_recovery) return fail(s->ctx, HDG_ERR_ARG, "recover first");
+      s->d_qu.download(qu, (size_t)s->nc * s->n, s->ctx->stream);
+    }
+    HDG_CUDA(cudaStreamSynchronize(s->ctx->stream));
+    return HDG_OK;
+  });
+}
+
+int hdg_mesh_concat(hdg_ctx* ctx, int nparts, const hdg_mesh* const* parts, hdg_mesh** out) {
+  if (!out || nparts < 1 || !parts) return fail(ctx, HDG_ERR_ARG, "hdg_mesh_concat: bad arguments");
+  return guard(ctx, [&]() -> int {
+    if (ctx) set_device(ctx);
+    std::vector<const hdg_mesh*> v(parts, parts + nparts);
+    for (auto* p : v)
+      if (!p) return fail(ctx, HDG_ERR_ARG, "hdg_mesh_concat: null part");
+    hdg_mesh* m = new hdg_mesh();
+    m->ctx = ctx;
+    try {
+      mesh_concat(m, v);
+      if (ctx) m->upload();
+    } catch (...) {
+      delete m;
+      throw;
+    }
+    *out = m;
+    return HDG_OK;
+  });
+}
+
+int hdg_mesh_problems(const hdg_mesh* m, int* nprob, int32_t* node0, int32_t* cell0, int32_t* face0) {
+  if (!m || !nprob) return HDG_ERR_ARG;
+  *nprob = m->nprob;
+  for (int P = 0; P <= m->nprob; ++P) {
+    if (node0) node0[P] = m->prob_node0[P];
+    if (cell0) cell0[P] = m->prob_cell0[P];
+    if (face0) face0[P] = m->prob_face0[P];
   }
   return HDG_OK;
 }

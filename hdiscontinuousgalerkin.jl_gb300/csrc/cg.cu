@@ -1,21 +1,26 @@
 // Jacobi-preconditioned conjugate gradients on the trace system (stands in for the sparse
-// direct `K \ b` of examples/poisson2D_HDG.jl:195).
+// direct `K \ b` of examples/poisson2D_HDG.jl:195), for one or many independent problems.
 //
-// The matrix is the block-sparse solver form of K (free rows negated, so SPD).  One iteration
-// is two kernels, using q_{k+1} = A z_{k+1} + beta q_k so that p and q are updated in the same
-// pass as the product:
-//   A: beta = rz/rz_old;  q = A z + beta q;  p = z + beta p;  pq = p.q
-//   B: alpha = rz/pq;     x += alpha p;  r -= alpha q;  z = D^-1 r;  rz, rr
-// Reductions are deterministic: each CUDA block writes a partial and the last block of a problem
-// to finish (atomic ticket) sums that problem's partials in a fixed order.  Every CUDA block
-// belongs to exactly one problem ("segment"), so independent problems can share one launch; a
-// converged problem's blocks return at once.  CHUNK iterations are captured in a CUDA graph and
-// replayed; the host reads the per-problem status between replays.
+// The matrix is the block-ELL solver form of K (free rows negated, so SPD).  One iteration is
+// two kernels:
+//   A: q = A p_new, p_new = z + beta p, pq = p_new.q
+//   B: alpha = rz/pq;  x += alpha p_new;  r -= alpha q;  z = D^-1 r;  rz, rr
+// In FP64, A uses q_{k+1} = A z_{k+1} + beta q_k so that p and q update in place in the same pass.
+// Reductions are deterministic per problem (seg_finish in hdg_device.cuh).  Every CUDA block
+// belongs to one problem, so many problems share one launch and a converged problem's blocks
+// return at once.  CHUNK iterations are captured in a CUDA graph and replayed; the host reads the
+// per-problem status between replays, and drives several systems (degree bins of a batch) in one
+// loop.
 //
-// Precision.  FP64: matrix, vectors and scalars in FP64.  Mixed: the inner CG runs on an FP32
-// copy of the matrix with FP32 r, z, p, q, while the correction x, every dot product and every
-// scalar stay FP64; an outer loop in FP64 forms r = b - K x with the FP64 matrix and solves for
-// the next correction until |r| <= tol |b|.
+// Precision.  FP64: matrix, vectors and scalars in FP64.  Mixed: the Krylov iteration runs on an
+// FP32 copy of the matrix with FP32 r, z, p, q, while x, every dot product and every scalar stay
+// FP64.  Accuracy is won back by an FP64 refinement that keeps the Krylov space ("reliable
+// updates": Sleijpen & van der Vorst 1996; Clark et al. 2010): once a problem's recursive
+// residual has dropped by DELTA since its last refinement, its true residual r = b - K x is
+// formed in FP64 with the FP64 matrix and replaces the recursive one, and the iteration goes on
+// with the same search direction.  Convergence is declared on the true FP64 residual only.  In
+// FP32 the product is recomputed every iteration (no q recurrence, whose rounding would
+// accumulate), with p alternating between two buffers.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -25,24 +30,25 @@
 namespace {
 constexpr int CG_BLOCK = 256;
 constexpr int SAMPLE_EVERY = 8;  // with profiling on, every 8th chunk runs un-graphed and timed
+constexpr int SC = 10;           // per problem: rz, rz_old, pq, rr, bb, tol2, alpha, beta, rr_true, -
+constexpr int ST = 4;            // per problem: status, iterations, maxit, refine flag
+constexpr double DELTA = 0.1;    // refine once the recursive residual fell by this factor
+// status: 0 running, 1 converged (recursive, FP64), 2 iteration cap, 3 breakdown (p'Ap <= 0),
+//         4 converged (true residual, mixed), 5 stopped (mixed: cap or stagnation)
 }  // namespace
 
 struct CgState {
-  int nseg = 0, nrow = 0;
-  DevBuf<int32_t> seg_prob, seg_row0, seg_row1, prob_blk0, prob_nblk;
-  DevBuf<double> part;   // [nseg][2]
-  DevBuf<double> sc;     // per problem: rz, rzold, pq, rr, bb, tol2
-  DevBuf<int32_t> st;    // per problem: status, iters, maxit
-  DevBuf<unsigned> cnt;  // per problem tickets (2 per problem)
-  DevBuf<double> r, z, p, q, dinv;      // FP64 inner vectors
-  DevBuf<float> rf, zf, pf, qf, dinvf;  // FP32 inner vectors
-  DevBuf<double> r64, d;                // mixed: outer residual and inner correction
-  DevBuf<double> rpart, rsc;            // residual-norm reduction
-  DevBuf<unsigned> rcnt;
+  int nprob = 0, nrow = 0;
+  DevBuf<double> sc;
+  DevBuf<int32_t> st;
+  DevBuf<double> r, z, p, q, dinv;
+  DevBuf<float> rf, zf, pf, pf2, qf, dinvf;
   cudaGraphExec_t graph64 = nullptr, graph32 = nullptr;
   int chunk64 = 0, chunk32 = 0;
-  int32_t* h_st = nullptr;  // pinned
-  double* h_sc = nullptr;   // pinned
+  int32_t* h_st = nullptr;  // pinned mirrors
+  double* h_sc = nullptr;
+  std::vector<double> rr_ref, rr_best;
+  std::vector<int> stagnant, outer;
   ~CgState() {
     if (graph64) cudaGraphExecDestroy(graph64);
     if (graph32) cudaGraphExecDestroy(graph32);
@@ -56,13 +62,9 @@ void destroy_cg(CgState* c) { delete c; }
 namespace {
 
 template <typename T> struct CgArgs {
-  const int32_t* seg_prob;
-  const int32_t* seg_row0;
-  const int32_t* seg_row1;
-  const int32_t* prob_blk0;
-  const int32_t* prob_nblk;
-  const int32_t* browptr;
-  const int32_t* bcol;
+  SegArgs g;
+  const int32_t* bcol5;
+  int nf;
   const T* val;
   const double* b;
   const T* dinv;
@@ -71,62 +73,34 @@ template <typename T> struct CgArgs {
   T* z;
   T* p;
   T* q;
-  double* part;
+  T* p2;
   double* sc;
   int32_t* st;
-  unsigned* cnt;
 };
 
-template <typename T>
-__device__ __forceinline__ bool finish_reduce(const CgArgs<T>& a, int P, int slot, double v0, double v1, double* sh,
-                                              double* sum0, double* sum1) {
-  __shared__ bool last;
-  v0 = block_sum<CG_BLOCK>(v0, sh);
-  v1 = block_sum<CG_BLOCK>(v1, sh);
-  if (threadIdx.x == 0) {
-    a.part[2 * blockIdx.x] = v0;
-    a.part[2 * blockIdx.x + 1] = v1;
-    __threadfence();
-    unsigned t = atomicAdd(&a.cnt[2 * P + slot], 1u);
-    last = (t == (unsigned)a.prob_nblk[P] - 1);
-  }
-  __syncthreads();
-  if (!last) return false;
-  __threadfence();
-  const int b0 = a.prob_blk0[P], nb = a.prob_nblk[P];
-  double s0 = 0.0, s1 = 0.0;
-  for (int k = threadIdx.x; k < nb; k += CG_BLOCK) {
-    s0 += ((volatile double*)a.part)[2 * (b0 + k)];
-    s1 += ((volatile double*)a.part)[2 * (b0 + k) + 1];
-  }
-  *sum0 = block_sum<CG_BLOCK>(s0, sh);
-  *sum1 = block_sum<CG_BLOCK>(s1, sh);
-  if (threadIdx.x == 0) a.cnt[2 * P + slot] = 0;
-  return true;
-}
-
+// (A v)_row over the block-ELL layout: 5 block slots, values slot-major and row-contiguous.
 template <int NT, typename T, typename V>
-__device__ __forceinline__ double row_dot(const int32_t* __restrict__ browptr, const int32_t* __restrict__ bcol,
-                                          const T* __restrict__ val, int row, const V* __restrict__ v) {
-  const int f = row / NT, i = row - f * NT;
-  double s = 0.0;
-  const int k1 = browptr[f + 1];
-  for (int k = browptr[f]; k < k1; ++k) {
-    const int g = bcol[k];
-    const T* blk = val + (int64_t)k * NT * NT + i * NT;
-    T acc = T(0);
+__device__ __forceinline__ double row_dot(const int32_t* __restrict__ bcol5, int nf, const T* __restrict__ val, int row,
+                                          const V* __restrict__ v) {
+  const int f = row / NT;
+  const int64_t ndofs = (int64_t)nf * NT;
+  int g[5];
 #pragma unroll
-    for (int j = 0; j < NT; ++j) acc += blk[j] * (T)v[g * NT + j];
-    s += (double)acc;
+  for (int k = 0; k < 5; ++k) g[k] = __ldg(bcol5 + k * nf + f);
+  T acc = T(0);
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+#pragma unroll
+    for (int j = 0; j < NT; ++j) acc += __ldg(val + (k * NT + j) * ndofs + row) * (T)__ldg(v + g[k] * NT + j);
   }
-  return s;
+  return (double)acc;
 }
 
 template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_init(CgArgs<T> a) {
   __shared__ double sh[32];
-  const int P = a.seg_prob[blockIdx.x];
+  const int P = a.g.seg_prob[blockIdx.x];
   double rz = 0.0, bb = 0.0;
-  for (int row = a.seg_row0[blockIdx.x] + threadIdx.x; row < a.seg_row1[blockIdx.x]; row += CG_BLOCK) {
+  for (int row = a.g.seg_row0[blockIdx.x] + threadIdx.x; row < a.g.seg_row1[blockIdx.x]; row += CG_BLOCK) {
     const double bv = a.b[row];
     const T rv = (T)bv;
     const T zv = a.dinv[row] * rv;
@@ -134,84 +108,202 @@ template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_i
     a.r[row] = rv;
     a.z[row] = zv;
     a.p[row] = T(0);
+    a.p2[row] = T(0);
     a.q[row] = T(0);
     rz += (double)rv * (double)zv;
     bb += bv * bv;
   }
   double s0, s1;
-  if (finish_reduce(a, P, 0, rz, bb, sh, &s0, &s1) && threadIdx.x == 0) {
-    double* sc = a.sc + 6 * P;
+  if (seg_finish<CG_BLOCK>(a.g, P, 0, rz, bb, sh, &s0, &s1) && threadIdx.x == 0) {
+    double* sc = a.sc + SC * P;
     sc[0] = s0;
     sc[1] = s0;
     sc[3] = s1;
     sc[4] = s1;
-    a.st[3 * P] = (s1 == 0.0) ? 1 : 0;
-    a.st[3 * P + 1] = 0;
+    sc[6] = 0.0;
+    sc[7] = 0.0;
+    sc[8] = s1;
+    a.st[ST * P] = (s1 == 0.0) ? 1 : 0;
+    a.st[ST * P + 1] = 0;
   }
 }
 
+// FP64 product kernel with the q recurrence (p, q in place)
 template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_a(CgArgs<T> a) {
   __shared__ double sh[32];
-  const int P = a.seg_prob[blockIdx.x];
-  if (a.st[3 * P] != 0) return;
-  const double* sc = a.sc + 6 * P;
-  const double beta = (a.st[3 * P + 1] == 0) ? 0.0 : sc[0] / sc[1];
+  const int P = a.g.seg_prob[blockIdx.x];
+  if (a.st[ST * P] != 0) return;
+  const double beta = a.sc[SC * P + 7];  // formed once by the reducing block of the update kernel
   const T bt = (T)beta;
   double pq = 0.0;
-  for (int row = a.seg_row0[blockIdx.x] + threadIdx.x; row < a.seg_row1[blockIdx.x]; row += CG_BLOCK) {
-    const double w = row_dot<NT>(a.browptr, a.bcol, a.val, row, a.z);
-    const T qn = (T)(w + beta * (double)a.q[row]);
-    const T pn = a.z[row] + bt * a.p[row];
-    a.q[row] = qn;
-    a.p[row] = pn;
-    pq += (double)pn * (double)qn;
+  const int r0 = a.g.seg_row0[blockIdx.x], r1 = a.g.seg_row1[blockIdx.x];
+  // four rows per thread in flight together (independent gathers and accumulation chains)
+  for (int base = r0 + threadIdx.x; base < r1; base += 4 * CG_BLOCK) {
+    double w[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int row = min(base + u * CG_BLOCK, r1 - 1);
+      w[u] = row_dot<NT>(a.bcol5, a.nf, a.val, row, a.z);
+    }
+    T qo[4], po[4], zo[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int row = min(base + u * CG_BLOCK, r1 - 1);
+      qo[u] = a.q[row];
+      po[u] = a.p[row];
+      zo[u] = a.z[row];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int row = base + u * CG_BLOCK;
+      if (row < r1) {
+        const T qn = (T)(w[u] + beta * (double)qo[u]);
+        const T pn = zo[u] + bt * po[u];
+        a.q[row] = qn;
+        a.p[row] = pn;
+        pq += (double)pn * (double)qn;
+      }
+    }
   }
   double s0, s1;
-  if (finish_reduce(a, P, 0, pq, 0.0, sh, &s0, &s1) && threadIdx.x == 0) a.sc[6 * P + 2] = s0;
+  if (seg_finish<CG_BLOCK>(a.g, P, 0, pq, 0.0, sh, &s0, &s1) && threadIdx.x == 0) {
+    a.sc[SC * P + 2] = s0;
+    a.sc[SC * P + 6] = a.sc[SC * P] / s0;  // alpha = rz / p.q
+  }
 }
 
-template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_b(CgArgs<T> a) {
+// Low-precision product kernel: p_new = z + beta p_old formed on the fly for every column the row
+// touches, q = A p_new a fresh product; p_old / p_new alternate buffers (flip).
+template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_a_fresh(CgArgs<T> a, int flip) {
   __shared__ double sh[32];
-  const int P = a.seg_prob[blockIdx.x];
-  if (a.st[3 * P] != 0) return;
-  const double* sc = a.sc + 6 * P;
-  const double alpha = sc[0] / sc[2];
-  const T at = (T)alpha;
-  double rz = 0.0, rr = 0.0;
-  for (int row = a.seg_row0[blockIdx.x] + threadIdx.x; row < a.seg_row1[blockIdx.x]; row += CG_BLOCK) {
-    a.x[row] += alpha * (double)a.p[row];
-    const T rn = a.r[row] - at * a.q[row];
-    const T zn = a.dinv[row] * rn;
-    a.r[row] = rn;
-    a.z[row] = zn;
-    rz += (double)rn * (double)zn;
-    rr += (double)rn * (double)rn;
+  const int P = a.g.seg_prob[blockIdx.x];
+  if (a.st[ST * P] != 0) return;
+  const T bt = (T)a.sc[SC * P + 7];
+  const T* __restrict__ pin = flip ? a.p2 : a.p;
+  T* __restrict__ pout = flip ? a.p : a.p2;
+  const int64_t ndofs = (int64_t)a.nf * NT;
+  double pq = 0.0;
+  for (int row = a.g.seg_row0[blockIdx.x] + threadIdx.x; row < a.g.seg_row1[blockIdx.x]; row += CG_BLOCK) {
+    const int f = row / NT;
+    T acc = T(0);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      const int g = __ldg(a.bcol5 + k * a.nf + f);
+#pragma unroll
+      for (int j = 0; j < NT; ++j) {
+        const int c = g * NT + j;
+        acc += __ldg(a.val + (k * NT + j) * ndofs + row) * (__ldg(a.z + c) + bt * __ldg(pin + c));
+      }
+    }
+    const T pn = a.z[row] + bt * pin[row];
+    pout[row] = pn;
+    a.q[row] = acc;
+    pq += (double)pn * (double)acc;
   }
   double s0, s1;
-  if (finish_reduce(a, P, 1, rz, rr, sh, &s0, &s1) && threadIdx.x == 0) {
-    double* scw = a.sc + 6 * P;
-    const double pq = scw[2];
-    scw[1] = scw[0];
-    scw[0] = s0;
-    scw[3] = s1;
-    const int it = a.st[3 * P + 1] + 1;
-    a.st[3 * P + 1] = it;
+  if (seg_finish<CG_BLOCK>(a.g, P, 0, pq, 0.0, sh, &s0, &s1) && threadIdx.x == 0) {
+    a.sc[SC * P + 2] = s0;
+    a.sc[SC * P + 6] = a.sc[SC * P] / s0;
+  }
+}
+
+template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_b(CgArgs<T> a, int flip) {
+  __shared__ double sh[32];
+  const int P = a.g.seg_prob[blockIdx.x];
+  if (a.st[ST * P] != 0) return;
+  const double alpha = a.sc[SC * P + 6];
+  const T at = (T)alpha;
+  const T* __restrict__ pcur = flip ? a.p2 : a.p;  // the direction the product kernel just wrote
+  double rz = 0.0, rr = 0.0;
+  const int r0 = a.g.seg_row0[blockIdx.x], r1 = a.g.seg_row1[blockIdx.x];
+  // the loads of four rows are issued before any store (stores may alias the loads, so the
+  // compiler would not hoist the next row's loads above them by itself)
+  for (int base = r0 + threadIdx.x; base < r1; base += 4 * CG_BLOCK) {
+    double xv[4];
+    T pv[4], rv[4], qv[4], dv[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int row = min(base + u * CG_BLOCK, r1 - 1);
+      xv[u] = a.x[row];
+      pv[u] = pcur[row];
+      rv[u] = a.r[row];
+      qv[u] = a.q[row];
+      dv[u] = a.dinv[row];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int row = base + u * CG_BLOCK;
+      if (row < r1) {
+        a.x[row] = xv[u] + alpha * (double)pv[u];
+        const T rn = rv[u] - at * qv[u];
+        const T zn = dv[u] * rn;
+        a.r[row] = rn;
+        a.z[row] = zn;
+        rz += (double)rn * (double)zn;
+        rr += (double)rn * (double)rn;
+      }
+    }
+  }
+  double s0, s1;
+  if (seg_finish<CG_BLOCK>(a.g, P, 1, rz, rr, sh, &s0, &s1) && threadIdx.x == 0) {
+    double* sc = a.sc + SC * P;
+    const double pq = sc[2], rr_prev = sc[3];
+    sc[1] = sc[0];
+    sc[0] = s0;
+    sc[3] = s1;
+    sc[7] = s0 / sc[1];  // beta for the next product kernel
+    const int it = a.st[ST * P + 1] + 1;
+    a.st[ST * P + 1] = it;
     int status = 0;
-    if (!(pq > 0.0) || !isfinite(s1)) status = 3;
-    else if (s1 <= scw[5] * scw[4]) status = 1;
-    else if (it >= a.st[3 * P + 2]) status = 2;
-    a.st[3 * P] = status;
+    if (!(pq > 0.0) || !isfinite(s1)) {
+      // p'Ap <= 0 once the residual is at rounding level (tiny problems solved exactly in a few
+      // steps) is convergence, not breakdown
+      status = (isfinite(s1) && rr_prev <= fmax(1e-24, 100.0 * sc[5]) * sc[4]) ? 1 : 3;
+    } else if (s1 <= sc[5] * sc[4]) {
+      status = 1;
+    }
+    else if (it >= a.st[ST * P + 2]) status = 2;
+    a.st[ST * P] = status;
+  }
+}
+
+// True residual r = b - K x in FP64 (FP64 matrix) for the problems whose refine flag is set;
+// with `replace` it also replaces the Krylov residual: r = r_true, z = D^-1 r, rz, beta.
+template <int NT, typename T>
+__global__ void __launch_bounds__(CG_BLOCK) k_cg_residual(CgArgs<T> a, const double* __restrict__ val64, int replace) {
+  __shared__ double sh[32];
+  const int P = a.g.seg_prob[blockIdx.x];
+  if (a.st[ST * P + 3] == 0) return;
+  double rz = 0.0, rr = 0.0;
+  for (int row = a.g.seg_row0[blockIdx.x] + threadIdx.x; row < a.g.seg_row1[blockIdx.x]; row += CG_BLOCK) {
+    const double rv = a.b[row] - row_dot<NT>(a.bcol5, a.nf, val64, row, a.x);
+    rr += rv * rv;
+    if (replace) {
+      const T rt = (T)rv;
+      const T zt = a.dinv[row] * rt;
+      a.r[row] = rt;
+      a.z[row] = zt;
+      rz += (double)rt * (double)zt;
+    }
+  }
+  double s0, s1;
+  if (seg_finish<CG_BLOCK>(a.g, P, 2, rz, rr, sh, &s0, &s1) && threadIdx.x == 0) {
+    double* sc = a.sc + SC * P;
+    sc[8] = s1;
+    if (replace) {
+      sc[0] = s0;
+      sc[3] = s1;
+      sc[7] = (a.st[ST * P + 1] == 0) ? 0.0 : s0 / sc[1];
+    }
   }
 }
 
 template <int NT, typename T>
-__global__ void k_dinv(int nrow, const int32_t* browptr, const int32_t* bcol, const double* val, T* dinv) {
+__global__ void k_dinv(int nrow, const int8_t* kdiag, const double* val, T* dinv) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nrow) return;
   const int f = t / NT, i = t - f * NT;
-  double d = 1.0;
-  for (int k = browptr[f]; k < browptr[f + 1]; ++k)
-    if (bcol[k] == f) d = val[(int64_t)k * NT * NT + i * NT + i];
+  const double d = val[(int64_t)(kdiag[f] * NT + i) * nrow + t];
   dinv[t] = (T)(1.0 / d);
 }
 
@@ -220,233 +312,352 @@ __global__ void k_to_float(int64_t n, const double* __restrict__ a, float* __res
     b[t] = (float)a[t];
 }
 
-// r = b - A x in FP64, with |r|^2 and |b|^2 reduced by the last block into out[0], out[1]
-template <int NT>
-__global__ void k_residual(int nrow, const int32_t* browptr, const int32_t* bcol, const double* val,
-                           const double* __restrict__ b, const double* __restrict__ x, double* __restrict__ r,
-                           double* part, unsigned* cnt, double* out) {
-  __shared__ double sh[32];
-  __shared__ bool last;
-  double rr = 0.0, bb = 0.0;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nrow; t += gridDim.x * blockDim.x) {
-    double bv = b[t];
-    double rv = bv - row_dot<NT>(browptr, bcol, val, t, x);
-    if (r) r[t] = rv;
-    rr += rv * rv;
-    bb += bv * bv;
-  }
-  rr = block_sum<256>(rr, sh);
-  bb = block_sum<256>(bb, sh);
-  if (threadIdx.x == 0) {
-    part[2 * blockIdx.x] = rr;
-    part[2 * blockIdx.x + 1] = bb;
-    __threadfence();
-    last = (atomicAdd(cnt, 1u) == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (last) {
-    __threadfence();
-    double s0 = 0.0, s1 = 0.0;
-    for (int k = threadIdx.x; k < gridDim.x; k += blockDim.x) {
-      s0 += ((volatile double*)part)[2 * k];
-      s1 += ((volatile double*)part)[2 * k + 1];
-    }
-    s0 = block_sum<256>(s0, sh);
-    s1 = block_sum<256>(s1, sh);
-    if (threadIdx.x == 0) {
-      out[0] = s0;
-      out[1] = s1;
-      *cnt = 0;
-    }
-  }
-}
-
-__global__ void k_axpy_inplace(int n, double* __restrict__ x, const double* __restrict__ d) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < n) x[t] += d[t];
-}
-
-template <int NT> struct Runner {
-  hdg_system* s;
-  CgState& c;
+// ------------------------------------------------------------------ per-system solver (CgSolver)
+template <int NT> struct SolverNT : CgSolver {
+  CgState* c;
   cudaStream_t st;
-  int nrow;
+  int nrow, nprob, chunk = 32;
+  bool mixed = false;
+  CgArgs<double> a64;
+  CgArgs<float> a32;
+  // Segment compaction: once most problems have finished, the launch grid is rebuilt from the
+  // segments of the problems still running, so the tail of a batch does not pay for blocks that
+  // would only return.  The full tables are restored when the solve ends.
+  std::vector<int32_t> full_prob, full_r0, full_r1, full_b0, full_nb;
+  int nseg_full = 0;
 
-  Runner(hdg_system* s_) : s(s_), c(*s_->cg), st(s_->ctx->stream), nrow(s_->ndofs) {}
+  explicit SolverNT(hdg_system* s_) {
+    s = s_;
+    if (!s->cg) s->cg = new CgState();
+    c = s->cg;
+    st = s->ctx->stream;
+    nrow = s->ndofs;
+    nprob = s->nprob;
+  }
 
-  void setup() {
-    if (c.nseg && c.nrow == nrow) return;
-    const int nseg = std::max(1, std::min((nrow + 1023) / 1024, 152 * 4));
-    std::vector<int32_t> sp(nseg, 0), r0(nseg), r1(nseg);
-    const int per = (nrow + nseg - 1) / nseg;
-    for (int k = 0; k < nseg; ++k) {
-      r0[k] = std::min(nrow, k * per);
-      r1[k] = std::min(nrow, (k + 1) * per);
+  SegArgs seg() const {
+    return SegArgs{s->d_seg_prob.p, s->d_seg_row0.p, s->d_seg_row1.p, s->d_prob_blk0.p, s->d_prob_nblk.p,
+                   s->d_part.p, s->d_cnt.p};
+  }
+
+  template <typename T> void launch_pair(const CgArgs<T>& a, cudaStream_t stream, int it) {
+    if (sizeof(T) == sizeof(double)) {
+      k_cg_a<NT, T><<<s->nseg, CG_BLOCK, 0, stream>>>(a);
+      k_cg_b<NT, T><<<s->nseg, CG_BLOCK, 0, stream>>>(a, 0);
+    } else {
+      k_cg_a_fresh<NT, T><<<s->nseg, CG_BLOCK, 0, stream>>>(a, it & 1);
+      k_cg_b<NT, T><<<s->nseg, CG_BLOCK, 0, stream>>>(a, (it & 1) ^ 1);
     }
-    int32_t b0 = 0, nb = nseg;
-    c.seg_prob.upload(sp.data(), nseg, st);
-    c.seg_row0.upload(r0.data(), nseg, st);
-    c.seg_row1.upload(r1.data(), nseg, st);
-    c.prob_blk0.upload(&b0, 1, st);
-    c.prob_nblk.upload(&nb, 1, st);
-    c.part.alloc(2 * (size_t)nseg);
-    c.sc.alloc(6);
-    c.st.alloc(3);
-    c.cnt.alloc(2);
-    HDG_CUDA(cudaMemsetAsync(c.cnt.p, 0, 2 * sizeof(unsigned), st));
-    c.rpart.alloc(2 * 1024);
-    c.rsc.alloc(2);
-    c.rcnt.alloc(1);
-    HDG_CUDA(cudaMemsetAsync(c.rcnt.p, 0, sizeof(unsigned), st));
-    if (!c.h_st) HDG_CUDA(cudaMallocHost(&c.h_st, 3 * sizeof(int32_t)));
-    if (!c.h_sc) HDG_CUDA(cudaMallocHost(&c.h_sc, 2 * sizeof(double)));
-    c.nseg = nseg;
-    c.nrow = nrow;
   }
 
-  template <typename T> CgArgs<T> args(const T* val, const double* b, const T* dinv, double* x, T* r, T* z, T* p, T* q) {
-    return CgArgs<T>{c.seg_prob.p, c.seg_row0.p, c.seg_row1.p, c.prob_blk0.p, c.prob_nblk.p, s->d_browptr.p,
-                     s->d_bcol.p, val, b, dinv, x, r, z, p, q, c.part.p, c.sc.p, c.st.p, c.cnt.p};
+  template <typename T> void build_graph(const CgArgs<T>& a, cudaGraphExec_t* graph, int* graph_chunk) {
+    if (*graph && *graph_chunk == chunk) return;
+    if (*graph) cudaGraphExecDestroy(*graph);
+    cudaStream_t cap;
+    HDG_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaGraph_t g;
+    HDG_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    for (int it = 0; it < chunk; ++it) launch_pair<T>(a, cap, it);
+    HDG_CUDA(cudaStreamEndCapture(cap, &g));
+    HDG_CUDA(cudaGraphInstantiate(graph, g, 0));
+    cudaGraphDestroy(g);
+    cudaStreamDestroy(cap);
+    *graph_chunk = chunk;
   }
 
-  template <typename T> void launch_pair(const CgArgs<T>& a, cudaStream_t stream) {
-    k_cg_a<NT, T><<<c.nseg, CG_BLOCK, 0, stream>>>(a);
-    k_cg_b<NT, T><<<c.nseg, CG_BLOCK, 0, stream>>>(a);
-  }
-
-  // Runs the inner CG (x = A^-1 b approximately) to |r| <= tol |b|; returns status, adds iterations.
-  template <typename T> int cg(const CgArgs<T>& a, double tol, int maxit, int chunk, cudaGraphExec_t* graph,
-                               int* graph_chunk, int* iters_out) {
-    double tol2 = tol * tol;
-    HDG_CUDA(cudaMemcpyAsync(c.sc.p + 5, &tol2, sizeof(double), cudaMemcpyHostToDevice, st));
-    int32_t mx = maxit;
-    HDG_CUDA(cudaMemcpyAsync(c.st.p + 2, &mx, sizeof(int32_t), cudaMemcpyHostToDevice, st));
-    k_cg_init<NT, T><<<c.nseg, CG_BLOCK, 0, st>>>(a);
-    HDG_CUDA(cudaGetLastError());
-    s->ctx->launches++;
-    if (!*graph || *graph_chunk != chunk) {
-      if (*graph) cudaGraphExecDestroy(*graph);
-      cudaStream_t cap;
-      HDG_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
-      cudaGraph_t g;
-      HDG_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-      for (int it = 0; it < chunk; ++it) launch_pair<T>(a, cap);
-      HDG_CUDA(cudaStreamEndCapture(cap, &g));
-      HDG_CUDA(cudaGraphInstantiate(graph, g, 0));
-      cudaGraphDestroy(g);
-      cudaStreamDestroy(cap);
-      *graph_chunk = chunk;
+  void prepare(const hdg_solver& o) override {
+    mixed = (o.precision == HDG_PREC_MIXED);
+    chunk = o.chunk > 1 ? (o.chunk + 1) / 2 * 2 : 2;  // even: the FP32 iteration alternates p buffers
+    if (c->nprob != nprob || c->nrow != nrow) {
+      c->sc.alloc((size_t)SC * nprob);
+      c->st.alloc((size_t)ST * nprob);
+      if (c->h_st) cudaFreeHost(c->h_st);
+      if (c->h_sc) cudaFreeHost(c->h_sc);
+      HDG_CUDA(cudaMallocHost(&c->h_st, sizeof(int32_t) * ST * nprob));
+      HDG_CUDA(cudaMallocHost(&c->h_sc, sizeof(double) * SC * nprob));
+      c->nprob = nprob;
+      c->nrow = nrow;
+      if (c->graph64) { cudaGraphExecDestroy(c->graph64); c->graph64 = nullptr; }
+      if (c->graph32) { cudaGraphExecDestroy(c->graph32); c->graph32 = nullptr; }
     }
-    const bool prof = s->ctx->profiling;
-    int status = 0;
-    for (int rep = 0;; ++rep) {
-      if (prof && rep % SAMPLE_EVERY == SAMPLE_EVERY - 1) {
-        // a timed, un-graphed chunk: events around each kernel
-        for (int it = 0; it < chunk; ++it) {
-          EventPair* ea = new EventPair();
-          EventPair* eb = new EventPair();
-          ea->start(st);
-          k_cg_a<NT, T><<<c.nseg, CG_BLOCK, 0, st>>>(a);
-          ea->stop(st);
-          eb->start(st);
-          k_cg_b<NT, T><<<c.nseg, CG_BLOCK, 0, st>>>(a);
-          eb->stop(st);
-          s->ev_cg_a.push_back(ea);
-          s->ev_cg_b.push_back(eb);
-        }
-        HDG_CUDA(cudaGetLastError());
-      } else {
-        HDG_CUDA(cudaGraphLaunch(*graph, st));
-      }
-      s->ctx->launches += 2 * chunk;
-      HDG_CUDA(cudaMemcpyAsync(c.h_st, c.st.p, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-      HDG_CUDA(cudaStreamSynchronize(st));
-      status = c.h_st[0];
-      if (status != 0) break;
-    }
-    *iters_out += c.h_st[1];
-    return status;
-  }
-
-  // |b - K x| / |b| in FP64 (optionally storing r)
-  double residual(double* r) {
-    const int blocks = std::min(1024, (nrow + 255) / 256);
-    k_residual<NT><<<blocks, 256, 0, st>>>(nrow, s->d_browptr.p, s->d_bcol.p, s->d_val.p, s->d_b.p, s->d_x.p, r,
-                                           c.rpart.p, c.rcnt.p, c.rsc.p);
-    HDG_CUDA(cudaGetLastError());
-    s->ctx->launches++;
-    HDG_CUDA(cudaMemcpyAsync(c.h_sc, c.rsc.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
-    HDG_CUDA(cudaStreamSynchronize(st));
-    return c.h_sc[1] > 0 ? std::sqrt(c.h_sc[0] / c.h_sc[1]) : 0.0;
-  }
-
-  int run(const hdg_solver& o, hdg_stats* stats) {
-    setup();
+    s->ensure_reduction_buffers();
     s->d_x.alloc(nrow);
+    nseg_full = s->nseg;
+    full_prob.resize(nseg_full); full_r0.resize(nseg_full); full_r1.resize(nseg_full);
+    full_b0.resize(nprob); full_nb.resize(nprob);
+    s->d_seg_prob.download(full_prob.data(), nseg_full, st);
+    s->d_seg_row0.download(full_r0.data(), nseg_full, st);
+    s->d_seg_row1.download(full_r1.data(), nseg_full, st);
+    s->d_prob_blk0.download(full_b0.data(), nprob, st);
+    s->d_prob_nblk.download(full_nb.data(), nprob, st);
+    HDG_CUDA(cudaStreamSynchronize(st));
     for (auto* e : s->ev_cg_a) delete e;
     for (auto* e : s->ev_cg_b) delete e;
     s->ev_cg_a.clear();
     s->ev_cg_b.clear();
     if (s->ctx->profiling) s->ev_cg.start(st);
-    const int chunk = o.chunk > 0 ? o.chunk : 32;
-    int iters = 0, outer = 0, status = 0;
-    double relres = 0.0;
-    if (o.precision == HDG_PREC_FP64) {
-      c.r.alloc(nrow); c.z.alloc(nrow); c.p.alloc(nrow); c.q.alloc(nrow); c.dinv.alloc(nrow);
-      k_dinv<NT, double><<<(nrow + 255) / 256, 256, 0, st>>>(nrow, s->d_browptr.p, s->d_bcol.p, s->d_val.p, c.dinv.p);
-      s->ctx->launches++;
-      auto a = args<double>(s->d_val.p, s->d_b.p, c.dinv.p, s->d_x.p, c.r.p, c.z.p, c.p.p, c.q.p);
-      status = cg<double>(a, o.tol, o.maxit, chunk, &c.graph64, &c.chunk64, &iters);
-      outer = 1;
-      relres = residual(nullptr);
+    // per-problem tolerance (mixed: recursive convergence only triggers a refinement) and cap
+    for (int P = 0; P < nprob; ++P) {
+      std::memset(c->h_sc + SC * P, 0, sizeof(double) * SC);
+      c->h_sc[SC * P + 5] = mixed ? 0.0 : o.tol * o.tol;
+      c->h_st[ST * P + 0] = 0;
+      c->h_st[ST * P + 1] = 0;
+      c->h_st[ST * P + 2] = o.maxit;
+      c->h_st[ST * P + 3] = 0;
+    }
+    HDG_CUDA(cudaMemcpyAsync(c->sc.p, c->h_sc, sizeof(double) * SC * nprob, cudaMemcpyHostToDevice, st));
+    HDG_CUDA(cudaMemcpyAsync(c->st.p, c->h_st, sizeof(int32_t) * ST * nprob, cudaMemcpyHostToDevice, st));
+    if (!mixed) {
+      c->r.alloc(nrow); c->z.alloc(nrow); c->p.alloc(nrow); c->q.alloc(nrow); c->dinv.alloc(nrow);
+      k_dinv<NT, double><<<(nrow + 255) / 256, 256, 0, st>>>(nrow, s->d_kdiag.p, s->d_val.p, c->dinv.p);
+      a64 = CgArgs<double>{seg(), s->d_bcol5.p, s->nf, s->d_val.p, s->d_b.p, c->dinv.p, s->d_x.p, c->r.p, c->z.p,
+                           c->p.p, c->q.p, c->p.p, c->sc.p, c->st.p};
+      k_cg_init<NT, double><<<s->nseg, CG_BLOCK, 0, st>>>(a64);
+      build_graph<double>(a64, &c->graph64, &c->chunk64);
     } else {
-      // FP32 copy of the solver-form matrix and FP32 inner vectors
-      s->d_valf.alloc((size_t)s->nnz);
-      k_to_float<<<(unsigned)std::min<int64_t>((s->nnz + 255) / 256, 152 * 32), 256, 0, st>>>(s->nnz, s->d_val.p,
-                                                                                             s->d_valf.p);
-      c.rf.alloc(nrow); c.zf.alloc(nrow); c.pf.alloc(nrow); c.qf.alloc(nrow); c.dinvf.alloc(nrow);
-      c.r64.alloc(nrow); c.d.alloc(nrow);
-      k_dinv<NT, float><<<(nrow + 255) / 256, 256, 0, st>>>(nrow, s->d_browptr.p, s->d_bcol.p, s->d_val.p, c.dinvf.p);
-      s->ctx->launches += 2;
-      HDG_CUDA(cudaMemsetAsync(s->d_x.p, 0, nrow * sizeof(double), st));
-      auto a = args<float>(s->d_valf.p, c.r64.p, c.dinvf.p, c.d.p, c.rf.p, c.zf.p, c.pf.p, c.qf.p);
-      relres = residual(c.r64.p);  // r = b (x = 0)
-      const int max_outer = 60;
-      while (relres > o.tol && outer < max_outer && iters < o.maxit) {
-        // inner tolerance relative to the current residual; never ask for less than the target
-        const double itol = std::max(o.inner_tol, 0.5 * o.tol / std::max(relres, 1e-300));
-        status = cg<float>(a, std::min(itol, 0.5), o.maxit - iters, chunk, &c.graph32, &c.chunk32, &iters);
-        ++outer;
-        if (status == 3) break;
-        k_axpy_inplace<<<(nrow + 255) / 256, 256, 0, st>>>(nrow, s->d_x.p, c.d.p);
-        s->ctx->launches++;
-        relres = residual(c.r64.p);
+      const int64_t nval = (int64_t)hdg_system::SLOTS * NT * nrow;
+      s->d_valf.alloc((size_t)nval);
+      k_to_float<<<(unsigned)std::min<int64_t>((nval + 255) / 256, 152 * 32), 256, 0, st>>>(nval, s->d_val.p,
+                                                                                           s->d_valf.p);
+      c->rf.alloc(nrow); c->zf.alloc(nrow); c->pf.alloc(nrow); c->pf2.alloc(nrow); c->qf.alloc(nrow);
+      c->dinvf.alloc(nrow);
+      k_dinv<NT, float><<<(nrow + 255) / 256, 256, 0, st>>>(nrow, s->d_kdiag.p, s->d_val.p, c->dinvf.p);
+      a32 = CgArgs<float>{seg(), s->d_bcol5.p, s->nf, s->d_valf.p, s->d_b.p, c->dinvf.p, s->d_x.p, c->rf.p, c->zf.p,
+                          c->pf.p, c->qf.p, c->pf2.p, c->sc.p, c->st.p};
+      k_cg_init<NT, float><<<s->nseg, CG_BLOCK, 0, st>>>(a32);
+      build_graph<float>(a32, &c->graph32, &c->chunk32);
+      s->ctx->launches++;
+    }
+    HDG_CUDA(cudaGetLastError());
+    s->ctx->launches += 2;
+    c->rr_ref.assign(nprob, 0.0);
+    c->rr_best.assign(nprob, 0.0);
+    c->stagnant.assign(nprob, 0);
+    c->outer.assign(nprob, 0);
+  }
+
+  template <typename T> void chunk_t(const CgArgs<T>& a, cudaGraphExec_t graph, int rep) {
+    if (s->ctx->profiling && rep % SAMPLE_EVERY == SAMPLE_EVERY - 1) {
+      for (int it = 0; it < chunk; ++it) {
+        EventPair* ea = new EventPair();
+        EventPair* eb = new EventPair();
+        ea->start(st);
+        if (sizeof(T) == sizeof(double)) k_cg_a<NT, T><<<s->nseg, CG_BLOCK, 0, st>>>(a);
+        else k_cg_a_fresh<NT, T><<<s->nseg, CG_BLOCK, 0, st>>>(a, it & 1);
+        ea->stop(st);
+        eb->start(st);
+        k_cg_b<NT, T><<<s->nseg, CG_BLOCK, 0, st>>>(a, sizeof(T) == sizeof(double) ? 0 : ((it & 1) ^ 1));
+        eb->stop(st);
+        s->ev_cg_a.push_back(ea);
+        s->ev_cg_b.push_back(eb);
       }
-      if (status != 3) status = (relres <= o.tol) ? 1 : 2;
+      HDG_CUDA(cudaGetLastError());
+    } else {
+      HDG_CUDA(cudaGraphLaunch(graph, st));
     }
+    s->ctx->launches += 2 * chunk;
+  }
+
+  void launch_chunk(int rep) override {
+    if (mixed) chunk_t<float>(a32, c->graph32, rep);
+    else chunk_t<double>(a64, c->graph64, rep);
+  }
+
+  void enqueue_status_copy() override {
+    HDG_CUDA(cudaMemcpyAsync(c->h_st, c->st.p, sizeof(int32_t) * ST * nprob, cudaMemcpyDeviceToHost, st));
+    HDG_CUDA(cudaMemcpyAsync(c->h_sc, c->sc.p, sizeof(double) * SC * nprob, cudaMemcpyDeviceToHost, st));
+  }
+
+  // true residuals of the flagged problems (and replacement of their Krylov residual)
+  void residual(bool replace) {
+    HDG_CUDA(cudaMemcpyAsync(c->st.p, c->h_st, sizeof(int32_t) * ST * nprob, cudaMemcpyHostToDevice, st));
+    if (mixed) k_cg_residual<NT, float><<<s->nseg, CG_BLOCK, 0, st>>>(a32, s->d_val.p, replace ? 1 : 0);
+    else k_cg_residual<NT, double><<<s->nseg, CG_BLOCK, 0, st>>>(a64, s->d_val.p, replace ? 1 : 0);
+    HDG_CUDA(cudaGetLastError());
+    s->ctx->launches++;
+    HDG_CUDA(cudaMemcpyAsync(c->h_sc, c->sc.p, sizeof(double) * SC * nprob, cudaMemcpyDeviceToHost, st));
+    HDG_CUDA(cudaStreamSynchronize(st));
+  }
+
+  // Rebuilds the segment tables from the running problems (all = restore the full tables).
+  void set_segments(bool all) {
+    std::vector<int32_t> sp, r0, r1, b0(full_b0), nb(full_nb);
+    for (int P = 0; P < nprob; ++P) {
+      if (!all && c->h_st[ST * P] != 0) continue;
+      b0[P] = (int32_t)sp.size();
+      for (int k = full_b0[P]; k < full_b0[P] + full_nb[P]; ++k) {
+        sp.push_back(full_prob[k]);
+        r0.push_back(full_r0[k]);
+        r1.push_back(full_r1[k]);
+      }
+    }
+    if (sp.empty()) return;
+    const int n = (int)sp.size();
+    HDG_CUDA(cudaMemcpyAsync(s->d_seg_prob.p, sp.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    HDG_CUDA(cudaMemcpyAsync(s->d_seg_row0.p, r0.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    HDG_CUDA(cudaMemcpyAsync(s->d_seg_row1.p, r1.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    HDG_CUDA(cudaMemcpyAsync(s->d_prob_blk0.p, b0.data(), nprob * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    HDG_CUDA(cudaStreamSynchronize(st));  // host staging vectors go out of scope
+    if (n != s->nseg) {
+      s->nseg = n;
+      if (mixed) { c->chunk32 = 0; build_graph<float>(a32, &c->graph32, &c->chunk32); }
+      else { c->chunk64 = 0; build_graph<double>(a64, &c->graph64, &c->chunk64); }
+    }
+  }
+
+  void maybe_compact() {
+    int active = 0;
+    for (int P = 0; P < nprob; ++P)
+      if (c->h_st[ST * P] == 0) active += full_nb[P];
+    if (active > 0 && s->nseg >= 16 && 2 * active <= s->nseg) set_segments(false);
+  }
+
+  bool process(const hdg_solver& o) override {
+    bool done = process_impl(o);
+    if (!done) maybe_compact();
+    return done;
+  }
+
+  bool process_impl(const hdg_solver& o) {
+    if (!mixed) {
+      for (int P = 0; P < nprob; ++P)
+        if (c->h_st[ST * P] == 0) return false;
+      return true;
+    }
+    // mixed: pick the problems that need a refinement
+    bool any = false, running = false;
+    for (int P = 0; P < nprob; ++P) {
+      int32_t* stp = c->h_st + ST * P;
+      const double* scp = c->h_sc + SC * P;
+      if (c->rr_ref[P] == 0.0) c->rr_ref[P] = c->rr_best[P] = scp[4];
+      stp[3] = 0;
+      if (stp[0] >= 3) continue;  // breakdown or final
+      if (stp[0] != 0 || scp[3] <= DELTA * DELTA * c->rr_ref[P]) {
+        stp[3] = 1;
+        any = true;
+      } else {
+        running = true;
+      }
+    }
+    if (!any) return !running;
+    residual(true);
+    const double tol2 = o.tol * o.tol;
+    for (int P = 0; P < nprob; ++P) {
+      int32_t* stp = c->h_st + ST * P;
+      if (!stp[3]) continue;
+      const double* scp = c->h_sc + SC * P;
+      const double rr = scp[8], bb = scp[4];
+      c->outer[P]++;
+      c->rr_ref[P] = rr;
+      if (rr <= tol2 * bb) { stp[0] = 4; continue; }     // converged on the true residual
+      if (stp[0] == 2) { stp[0] = 5; continue; }          // iteration cap reached
+      c->stagnant[P] = (rr > 0.25 * c->rr_best[P]) ? c->stagnant[P] + 1 : 0;
+      c->rr_best[P] = std::min(c->rr_best[P], rr);
+      if (c->stagnant[P] >= 5) { stp[0] = 5; continue; }  // the FP32 operator limits the residual
+      stp[0] = 0;
+      running = true;
+    }
+    for (int P = 0; P < nprob; ++P) c->h_st[ST * P + 3] = 0;
+    HDG_CUDA(cudaMemcpyAsync(c->st.p, c->h_st, sizeof(int32_t) * ST * nprob, cudaMemcpyHostToDevice, st));
+    return !running;
+  }
+
+  void finish(const hdg_solver& o, std::vector<hdg_stats>* out) override {
+    (void)o;
+    if (s->nseg != nseg_full) set_segments(true);  // restore the full tables (other kernels use them)
+    if (!mixed) {  // report the true FP64 residual of every problem
+      for (int P = 0; P < nprob; ++P) c->h_st[ST * P + 3] = 1;
+      residual(false);
+      for (int P = 0; P < nprob; ++P) c->h_st[ST * P + 3] = 0;
+      HDG_CUDA(cudaMemcpyAsync(c->st.p, c->h_st, sizeof(int32_t) * ST * nprob, cudaMemcpyHostToDevice, st));
+    }
+    HDG_CUDA(cudaStreamSynchronize(st));
     if (s->ctx->profiling) s->ev_cg.stop(st);
-    s->cg_iterations = iters;
-    if (stats) {
-      stats->iterations = iters;
-      stats->outer = outer;
-      stats->rel_residual = relres;
-      stats->converged = (status == 1);
+    out->assign(nprob, hdg_stats{});
+    int itmax = 0;
+    for (int P = 0; P < nprob; ++P) {
+      const int status = c->h_st[ST * P];
+      hdg_stats& r = (*out)[P];
+      r.iterations = c->h_st[ST * P + 1];
+      r.outer = mixed ? c->outer[P] : 1;
+      const double bb = c->h_sc[SC * P + 4];
+      r.rel_residual = bb > 0 ? std::sqrt(c->h_sc[SC * P + 8] / bb) : 0.0;
+      r.converged = mixed ? (status == 4) : (status == 1);
+      if (status == 3) r.converged = -1;  // breakdown marker, mapped to an error by the caller
+      itmax = std::max(itmax, r.iterations);
     }
-    if (status == 3) return HDG_ERR_BREAKDOWN;
-    if (status == 2) return HDG_ERR_NO_CONVERGENCE;
-    return HDG_OK;
+    s->cg_iterations = itmax;
   }
 };
 
 }  // namespace
 
-int run_solve(hdg_system* s, const hdg_solver& o, hdg_stats* stats) {
-  if (!s->cg) s->cg = new CgState();
+CgSolver* make_cg_solver(hdg_system* s) {
   switch (s->nt) {
-    case 2: return Runner<2>(s).run(o, stats);
-    case 3: return Runner<3>(s).run(o, stats);
-    case 4: return Runner<4>(s).run(o, stats);
-    case 5: return Runner<5>(s).run(o, stats);
+    case 2: return new SolverNT<2>(s);
+    case 3: return new SolverNT<3>(s);
+    case 4: return new SolverNT<4>(s);
+    case 5: return new SolverNT<5>(s);
   }
-  return HDG_ERR_ARG;
+  throw HdgError{HDG_ERR_ARG, "degree not supported"};
+}
+
+// Solves every problem of every system; the systems' chunks are interleaved so that one host
+// loop drives a whole degree-binned batch.  stats[i] receives the per-problem results of sys[i].
+int run_solve_many(const std::vector<hdg_system*>& sys, const hdg_solver& o,
+                   std::vector<std::vector<hdg_stats>>* stats) {
+  std::vector<CgSolver*> sv;
+  struct Guard {
+    std::vector<CgSolver*>& v;
+    ~Guard() {
+      for (auto* p : v) delete p;
+    }
+  } guard{sv};
+  for (auto* s : sys) sv.push_back(make_cg_solver(s));
+  for (auto* x : sv) x->prepare(o);
+  std::vector<char> done(sv.size(), 0);
+  for (int rep = 0;; ++rep) {
+    bool all = true;
+    for (size_t i = 0; i < sv.size(); ++i)
+      if (!done[i]) {
+        sv[i]->launch_chunk(rep);
+        sv[i]->enqueue_status_copy();
+        all = false;
+      }
+    if (all) break;
+    for (size_t i = 0; i < sv.size(); ++i)
+      if (!done[i]) HDG_CUDA(cudaStreamSynchronize(sv[i]->s->ctx->stream));
+    for (size_t i = 0; i < sv.size(); ++i)
+      if (!done[i] && sv[i]->process(o)) done[i] = 1;
+  }
+  stats->resize(sv.size());
+  int rc = HDG_OK;
+  for (size_t i = 0; i < sv.size(); ++i) {
+    sv[i]->finish(o, &(*stats)[i]);
+    for (auto& r : (*stats)[i]) {
+      if (r.converged < 0) {
+        r.converged = 0;
+        rc = HDG_ERR_BREAKDOWN;
+      } else if (!r.converged && rc == HDG_OK) {
+        rc = HDG_ERR_NO_CONVERGENCE;
+      }
+    }
+  }
+  return rc;
+}
+
+int run_solve(hdg_system* s, const hdg_solver& o, hdg_stats* stats) {
+  std::vector<std::vector<hdg_stats>> st;
+  int rc = run_solve_many({s}, o, &st);
+  if (stats) {  // aggregate over the system's problems
+    hdg_stats agg{0, 0, 0.0, 1};
+    for (auto& r : st[0]) {
+      agg.iterations = std::max(agg.iterations, r.iterations);
+      agg.outer = std::max(agg.outer, r.outer);
+      agg.rel_residual = std::max(agg.rel_residual, r.rel_residual);
+      agg.converged = agg.converged && r.converged;
+    }
+    *stats = agg;
+  }
+  return rc;
 }

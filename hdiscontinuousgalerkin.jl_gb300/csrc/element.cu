@@ -23,10 +23,8 @@ struct ElemArgs {
   const double* ref;
   int ref_len, nq;
   int nc;
-  double tau;
-  FieldDev f;
-  FieldDev kf;
-  int kappa_mode;  // 0: kappa = 1, 1: per-cell array, 2: field
+  CoefDev co;      // per-problem source, coefficient and tau (one problem unless batched)
+  int kappa_mode;  // 0: kappa = 1, 1: per-cell array, 2: per-problem field
   const double* kcell;
   double* AB;
   double* KB;
@@ -59,7 +57,7 @@ template <int P> __global__ void __launch_bounds__(EWARPS * 32) k_element_conden
     return l;
   }();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int wstride = N * LD + 2 * nq + NW + 2;
+  const int wstride = N * LD + 2 * nq + NW + N + 2;
   double* W = smem + ((ref_len + 1) & ~1) + warp * wstride;
   double* sq = W + N * LD;  // per-warp scratch: f (or kappa^-1) at the quadrature points, be
   __syncthreads();
@@ -86,7 +84,10 @@ template <int P> __global__ void __launch_bounds__(EWARPS * 32) k_element_conden
 #pragma unroll
     for (int f = 0; f < 3; ++f) el[f] = sqrt(wn[f][0] * wn[f][0] + wn[f][1] * wn[f][1]);
     const unsigned ob = a.orient[e];
-    const double tau = a.tau;
+    const int prob = a.co.cell_prob[e];
+    const double tau = a.co.tau[prob];
+    const int fkind = a.co.fkind[prob];
+    const double* fprm = a.co.fprm + a.co.foff[prob];
     double kinv = 1.0;
     if (a.kappa_mode == 1) kinv = 1.0 / a.kcell[e];
     const double smass = kinv * detJ;
@@ -95,8 +96,8 @@ template <int P> __global__ void __launch_bounds__(EWARPS * 32) k_element_conden
       double xi = ref[L.Q + 2 * q], eta = ref[L.Q + 2 * q + 1];
       double xq = (1.0 - xi - eta) * x1 + xi * x2 + eta * x3;
       double yq = (1.0 - xi - eta) * y1 + xi * y2 + eta * y3;
-      sq[q] = eval_field_dev(a.f, xq, yq);
-      if (a.kappa_mode == 2) sq[nq + q] = 1.0 / eval_field_dev(a.kf, xq, yq);
+      sq[q] = eval_field_kind(fkind, fprm, xq, yq);
+      if (a.kappa_mode == 2) sq[nq + q] = 1.0 / eval_field_kind(a.co.kkind[prob], a.co.kprm + a.co.koff[prob], xq, yq);
     }
     __syncwarp();
     double* be = sq + 2 * nq;
@@ -156,20 +157,24 @@ template <int P> __global__ void __launch_bounds__(EWARPS * 32) k_element_conden
     }
     __syncwarp();
     // ---- Gaussian elimination with partial pivoting --------------------------------------
+    // The pivot search compares |a_ik| through its bit pattern: for non-negative IEEE doubles
+    // the unsigned-integer order of the bits is the numeric order, so the search runs on the
+    // integer pipe instead of the (narrow) FP64 pipe.  Ties keep the smallest row, as idamax.
+    double* rinv = be + NW;  // reciprocals of the pivots, reused by the back substitution
     for (int k = 0; k < N; ++k) {
-      double best = -1.0;
-      int bi = k;
+      unsigned long long best = 0ull;
+      int bi = N;
       for (int i = k + lane; i < N; i += 32) {
-        double v = fabs(W[i * LD + k]);
-        if (v > best) { best = v; bi = i; }
+        const unsigned long long v = (unsigned long long)__double_as_longlong(W[i * LD + k]) & 0x7fffffffffffffffull;
+        if (v > best || (v == best && i < bi)) { best = v; bi = i; }
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
-        double ov = __shfl_xor_sync(0xffffffffu, best, o);
-        int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        const unsigned long long ov = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
         if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
       }
-      if (best == 0.0 && lane == 0) atomicOr(a.err, 2);
+      if (best == 0ull && lane == 0) atomicOr(a.err, 2);
       if (bi != k) {
         for (int j = k + lane; j < NC; j += 32) {
           double t = W[k * LD + j];
@@ -179,6 +184,7 @@ template <int P> __global__ void __launch_bounds__(EWARPS * 32) k_element_conden
         __syncwarp();
       }
       const double pinv = 1.0 / W[k * LD + k];
+      if (lane == 0) rinv[k] = pinv;
       for (int i = k + 1 + lane; i < N; i += 32) W[i * LD + k] *= pinv;
       __syncwarp();
       const int cols = NC - k - 1, rows = N - k - 1;
@@ -190,7 +196,7 @@ template <int P> __global__ void __launch_bounds__(EWARPS * 32) k_element_conden
     }
     // ---- back substitution on the m+1 right-hand sides -----------------------------------
     for (int k = N - 1; k >= 0; --k) {
-      const double dinv = 1.0 / W[k * LD + k];
+      const double dinv = rinv[k];
       for (int j = lane; j <= M; j += 32) W[k * LD + N + j] *= dinv;
       __syncwarp();
       for (int t = lane; t < k * (M + 1); t += 32) {
@@ -238,7 +244,7 @@ template <int P> __global__ void __launch_bounds__(EWARPS * 32) k_element_conden
 template <int P> void launch_p(hdg_system* s, cudaStream_t st, const ElemArgs& a) {
   using D = Dims<P>;
   const int nq = a.nq;
-  const int wstride = D::N * D::LD + 2 * nq + D::NW + 2;
+  const int wstride = D::N * D::LD + 2 * nq + D::NW + D::N + 2;
   size_t smem = (size_t)(((a.ref_len + 1) & ~1) + EWARPS * wstride) * sizeof(double);
   static bool attr_set = false;
   if (!attr_set) {
@@ -271,9 +277,7 @@ void launch_element_condense(hdg_system* s, cudaStream_t st) {
   a.ref_len = (int)sp->t.packed.size();
   a.nq = sp->t.nq;
   a.nc = m->nc;
-  a.tau = s->tau;
-  a.f = FieldDev{s->f.kind, (int)s->f.prm.size(), s->d_fprm.p};
-  a.kf = FieldDev{s->kappa.kind, (int)s->kappa.prm.size(), s->d_kprm.p};
+  a.co = s->coef_dev();
   a.kappa_mode = s->kappa_cells ? 1 : (s->kappa_field ? 2 : 0);
   a.kcell = s->d_kappa.p;
   a.AB = s->d_AB.p;

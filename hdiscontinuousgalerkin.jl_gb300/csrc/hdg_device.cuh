@@ -16,9 +16,8 @@ template <int P> struct Dims {
 };
 
 // Field evaluation: the kinds of hdg.h (HDG_FIELD_*), parameters in device memory.
-__device__ __forceinline__ double eval_field_dev(const FieldDev& f, double x, double y) {
-  const double* p = f.prm;
-  switch (f.kind) {
+__device__ __forceinline__ double eval_field_kind(int kind, const double* __restrict__ p, double x, double y) {
+  switch (kind) {
     case HDG_FIELD_CONST: return p[0];
     case HDG_FIELD_SINSIN: return p[0] * sinpi(p[1] * x) * sinpi(p[2] * y);
     case HDG_FIELD_BUMPS: {
@@ -39,11 +38,16 @@ __device__ __forceinline__ double eval_field_dev(const FieldDev& f, double x, do
         const double* b = p + 2 + 4 * k;
         g += b[3] * cos(6.283185307179586 * (b[0] * x + b[1] * y) + b[2]);
       }
-      return f.kind == HDG_FIELD_EXP_FOURIER ? exp(g) : g;
+      return kind == HDG_FIELD_EXP_FOURIER ? exp(g) : g;
     }
   }
   return 0.0;
 }
+__device__ __forceinline__ double eval_field_dev(const FieldDev& f, double x, double y) {
+  return eval_field_kind(f.kind, f.prm, x, y);
+}
+
+
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -73,4 +77,46 @@ template <int BLOCK> __device__ __forceinline__ double block_sum(double v, doubl
   t = sh[0];
   __syncthreads();
   return t;
+}
+
+// Segments: every CUDA block of a row-parallel kernel covers rows [row0, row1) of one problem.
+// A per-problem sum is formed deterministically: each block writes its partial, and the last
+// block of the problem to finish (atomic ticket, no waiting) adds the problem's partials in
+// block order.  part holds 2 doubles per block; cnt holds one ticket per (problem, slot).
+struct SegArgs {
+  const int32_t* seg_prob;
+  const int32_t* seg_row0;
+  const int32_t* seg_row1;
+  const int32_t* prob_blk0;
+  const int32_t* prob_nblk;
+  double* part;
+  unsigned* cnt;  // [nprob][4]
+};
+
+template <int BLOCK>
+__device__ __forceinline__ bool seg_finish(const SegArgs& g, int P, int slot, double v0, double v1, double* sh,
+                                           double* sum0, double* sum1) {
+  __shared__ bool last;
+  v0 = block_sum<BLOCK>(v0, sh);
+  v1 = block_sum<BLOCK>(v1, sh);
+  if (threadIdx.x == 0) {
+    g.part[2 * blockIdx.x] = v0;
+    g.part[2 * blockIdx.x + 1] = v1;
+    __threadfence();
+    const unsigned t = atomicAdd(&g.cnt[4 * P + slot], 1u);
+    last = (t == (unsigned)g.prob_nblk[P] - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  const int b0 = g.prob_blk0[P], nb = g.prob_nblk[P];
+  double s0 = 0.0, s1 = 0.0;
+  for (int k = threadIdx.x; k < nb; k += BLOCK) {
+    s0 += ((volatile double*)g.part)[2 * (b0 + k)];
+    s1 += ((volatile double*)g.part)[2 * (b0 + k) + 1];
+  }
+  *sum0 = block_sum<BLOCK>(s0, sh);
+  *sum1 = block_sum<BLOCK>(s1, sh);
+  if (threadIdx.x == 0) g.cnt[4 * P + slot] = 0;
+  return true;
 }

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <map>
 #include <string>
 #include <vector>
@@ -25,15 +26,20 @@ struct HdgError {
   } while (0)
 
 // ------------------------------------------------------------------ device buffers
+// Device memory comes from the stream-ordered pool allocator on the stream of the context that
+// owns the object (set by every C-ABI entry point): a batch or a served request allocates and
+// frees its buffers without synchronising the device, and freed memory stays in the pool.
+extern thread_local cudaStream_t g_alloc_stream;
 template <class T> struct DevBuf {
   T* p = nullptr;
   size_t n = 0;
+  cudaStream_t s = nullptr;
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() { release(); }
   void release() {
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, s);
     p = nullptr;
     n = 0;
   }
@@ -41,7 +47,8 @@ template <class T> struct DevBuf {
     if (count == n && p) return;
     release();
     if (count == 0) return;
-    HDG_CUDA(cudaMalloc(&p, count * sizeof(T)));
+    s = g_alloc_stream;
+    HDG_CUDA(cudaMallocAsync((void**)&p, count * sizeof(T), s));
     n = count;
   }
   void upload(const T* h, size_t count, cudaStream_t s) {
@@ -66,6 +73,19 @@ struct FieldDev {
   int kind;
   int np;
   const double* prm;
+};
+
+// Per-problem coefficients of a system holding several independent problems (a batch): the
+// problem of a cell indexes the source/coefficient field kinds, parameter offsets and tau.
+struct CoefDev {
+  const int32_t* cell_prob;  // [ncells]
+  const int32_t* fkind;      // [nprob]
+  const int32_t* foff;       // [nprob] offset into fprm
+  const double* fprm;
+  const int32_t* kkind;      // [nprob] kappa field kind (kappa_mode 2)
+  const int32_t* koff;
+  const double* kprm;
+  const double* tau;         // [nprob]
 };
 
 // ------------------------------------------------------------------ objects
@@ -110,6 +130,16 @@ struct EventPair {
 struct hdg_mesh {
   hdg_ctx* ctx = nullptr;
   int nn = 0, nc = 0, nf = 0;
+  // A mesh may be the disjoint union of several problems' meshes (a batch): problem P owns
+  // nodes [prob_node0[P], prob_node0[P+1]) and likewise cells and faces.
+  int nprob = 1;
+  std::vector<int32_t> prob_node0, prob_cell0, prob_face0;
+  void single_problem() {
+    nprob = 1;
+    prob_node0 = {0, nn};
+    prob_cell0 = {0, nc};
+    prob_face0 = {0, nf};
+  }
   std::vector<double> xy;       // [nn][2]
   std::vector<int32_t> cells;   // [nc][3] 0-based
   std::vector<int32_t> cfaces;  // [nc][3] 0-based
@@ -124,6 +154,7 @@ struct hdg_mesh {
   DevBuf<uint8_t> d_orient;   // bit f = face_orientation(cell, f)
   DevBuf<int32_t> d_fcell;    // [nf][2] cells of a face (second -1 on the boundary)
   DevBuf<int8_t> d_flf;       // [nf][2] local face index in those cells
+  DevBuf<int32_t> d_cell_prob;  // [nc] problem of each cell
   void upload();
   void upload_coordinates();
 };
@@ -163,6 +194,28 @@ struct hdg_system {
   int nw, nt, n, m, nc, nf, ndofs;
   int64_t nblocks, nnz;
   double tau = 1.0;
+  // Problems held by this system (several when batched; all share the degree).  Problem P owns
+  // trace rows [h_prob_row0[P], h_prob_row0[P+1]).
+  int nprob = 1;
+  std::vector<int32_t> h_prob_row0;
+  std::vector<FieldSpec> fsp, ksp;  // per-problem source and coefficient fields
+  std::vector<double> taus;
+  DevBuf<int32_t> d_fkind, d_foff, d_kkind, d_koff, d_row_prob;
+  DevBuf<double> d_tau;
+  DevBuf<double> d_mdiag;           // [nprob] mean |diag K| per problem
+  DevBuf<int32_t> d_prob_row0;      // [nprob+1]
+  DevBuf<int32_t>& d_prob_row0_dev() {
+    if (!d_prob_row0.p) d_prob_row0.upload(h_prob_row0.data(), h_prob_row0.size(), ctx->stream);
+    return d_prob_row0;
+  }
+  // Segments: the CUDA blocks of the row-parallel kernels (CG, meandiag, residual); each block
+  // covers a row range inside one problem, so per-problem reductions need no cross-problem sums.
+  int nseg = 0;
+  DevBuf<int32_t> d_seg_prob, d_seg_row0, d_seg_row1, d_prob_blk0, d_prob_nblk;
+  CoefDev coef_dev() const {
+    return CoefDev{space->mesh->d_cell_prob.p, d_fkind.p, d_foff.p, d_fprm.p, d_kkind.p, d_koff.p, d_kprm.p,
+                   d_tau.p};
+  }
   // per-cell condensed blocks: AB = [Ate | bte] (m x (m+1)), KB = [K_e | b_e] (n x (m+1))
   DevBuf<double> d_AB, d_KB;
   DevBuf<float> d_ABf, d_KBf;
@@ -170,12 +223,20 @@ struct hdg_system {
   DevBuf<double> d_fprm, d_kprm;
   FieldSpec f, kappa;
   bool kappa_field = false, kappa_cells = false;
-  // block-sparse trace matrix, nt x nt blocks, one block row per face
+  // Trace matrix.  Host: block rows sorted by face id (h_browptr/h_bcol, the export pattern).
+  // Device: block-ELL with SLOTS block slots per face (an interior face couples to itself and
+  // the 4 other faces of its two cells, a boundary face to 3); missing slots are zero blocks
+  // that point at the face itself.  Values are slot-major, row-contiguous:
+  // val[(k*nt + j)*ndofs + f*nt + i] = K[f*nt + i, bcol5[k*nf + f]*nt + j], so that consecutive
+  // rows read consecutive addresses.
+  static constexpr int SLOTS = 5;
   std::vector<int32_t> h_browptr, h_bcol;
   std::vector<int32_t> h_bsrc;  // [nblocks][2] source (cell*9 + lf*3 + lg) or -1
-  DevBuf<int32_t> d_browptr, d_bcol, d_bsrc, d_dof_prob;
-  DevBuf<double> d_val;   // K values [nblocks][nt][nt]
-  DevBuf<float> d_valf;   // FP32 copy for the mixed solve
+  DevBuf<int32_t> d_bcol5;      // [SLOTS][nf]
+  DevBuf<int32_t> d_src5;       // [SLOTS][nf][2]
+  DevBuf<int8_t> d_kdiag;       // [nf] slot of the diagonal block
+  DevBuf<double> d_val;         // [SLOTS*nt*nt][ndofs] (as above)
+  DevBuf<float> d_valf;         // FP32 copy for the mixed solve
   DevBuf<double> d_b;     // rhs
   // Dirichlet state
   bool applied = false;   // apply! done: d_val/d_b are in solver form (free rows negated)
@@ -197,11 +258,13 @@ struct hdg_system {
   bool have_solution = false, have_recovery = false;
   CgState* cg = nullptr;
   ~hdg_system();
+  // partials: 2 per segment; tickets: 4 per problem (CG product, CG update, residual, meandiag)
   void ensure_reduction_buffers() {
-    if (!d_part.p) d_part.alloc(2048);
-    if (!d_cnt.p) {
-      d_cnt.alloc(8);
-      HDG_CUDA(cudaMemsetAsync(d_cnt.p, 0, 8 * sizeof(unsigned), ctx->stream));
+    const size_t np = 2 * (size_t)std::max(nseg, 1024), nc = 4 * (size_t)nprob;
+    if (d_part.n < np) d_part.alloc(np);
+    if (d_cnt.n < nc) {
+      d_cnt.alloc(nc);
+      HDG_CUDA(cudaMemsetAsync(d_cnt.p, 0, nc * sizeof(unsigned), ctx->stream));
     }
   }
 };
@@ -212,6 +275,22 @@ void launch_gather(hdg_system* s, cudaStream_t st);
 void launch_apply_dirichlet(hdg_system* s, const std::vector<int32_t>& dofs0, const std::vector<double>& vals,
                             cudaStream_t st);
 int run_solve(hdg_system* s, const hdg_solver& o, hdg_stats* st);
+int run_solve_many(const std::vector<hdg_system*>& sys, const hdg_solver& o,
+                   std::vector<std::vector<hdg_stats>>* stats);
+void build_segments(hdg_system* s);
+
+// The CG of one system, driven chunk by chunk by a host loop (run_solve_many, the serving engine).
+struct CgSolver {
+  virtual ~CgSolver() {}
+  virtual void prepare(const hdg_solver& o) = 0;      // allocate, initialise, capture the chunk graph
+  virtual void launch_chunk(int rep) = 0;             // enqueue one chunk of iterations
+  virtual void enqueue_status_copy() = 0;             // enqueue the per-problem status read-back
+  virtual bool process(const hdg_solver& o) = 0;      // after the read-back: true when all problems are done
+  virtual void finish(const hdg_solver& o, std::vector<hdg_stats>* out) = 0;
+  hdg_system* s = nullptr;
+};
+CgSolver* make_cg_solver(hdg_system* s);
+void mesh_concat(hdg_mesh* out, const std::vector<const hdg_mesh*>& parts);
 void launch_recover(hdg_system* s, cudaStream_t st);
 double run_errornorm(hdg_system* s, const FieldSpec& uex, cudaStream_t st);
 void destroy_cg(CgState* c);

@@ -105,6 +105,7 @@ void mesh_build_rectangle(hdg_mesh* m, int nx, int ny, const double LL[2], const
   m->facesets["top"] = top;
   m->facesets["left"] = left;
   m->facesets["boundary"] = all;
+  m->single_problem();
 }
 
 namespace {
@@ -166,7 +167,47 @@ int mesh_build_from_cells(hdg_mesh* m, int nnodes, const double* xy, int ncells,
   m->nf = (int)(m->faces.size() / 4);
   std::sort(bnd.begin(), bnd.end());
   m->facesets["boundary"] = bnd;
+  m->single_problem();
   return HDG_OK;
+}
+
+// Disjoint union of meshes (a batch of independent problems): node, cell and face ids of part P
+// are shifted by the totals of parts 0..P-1, so each part keeps its own numbering order (and its
+// face orientations, which depend only on the order of node ids); face sets are merged.
+void mesh_concat(hdg_mesh* out, const std::vector<const hdg_mesh*>& parts) {
+  out->structured = false;
+  out->nn = out->nc = out->nf = 0;
+  out->xy.clear(); out->cells.clear(); out->cfaces.clear(); out->faces.clear(); out->facesets.clear();
+  out->nprob = 0;
+  out->prob_node0 = {0};
+  out->prob_cell0 = {0};
+  out->prob_face0 = {0};
+  for (const hdg_mesh* m : parts) {
+    for (int P = 0; P < m->nprob; ++P) {  // a part may itself be a union
+      out->prob_node0.push_back(out->nn + m->prob_node0[P + 1]);
+      out->prob_cell0.push_back(out->nc + m->prob_cell0[P + 1]);
+      out->prob_face0.push_back(out->nf + m->prob_face0[P + 1]);
+    }
+    out->nprob += m->nprob;
+    out->xy.insert(out->xy.end(), m->xy.begin(), m->xy.end());
+    for (int32_t v : m->cells) out->cells.push_back(v + out->nn);
+    for (int32_t v : m->cfaces) out->cfaces.push_back(v + out->nf);
+    for (int f = 0; f < m->nf; ++f) {
+      const int32_t* r = &m->faces[4 * f];
+      out->faces.push_back(r[0] + out->nn);
+      out->faces.push_back(r[1] + out->nn);
+      out->faces.push_back(r[2] + out->nc);
+      out->faces.push_back(r[3] < 0 ? -1 : r[3] + out->nc);
+    }
+    for (const auto& kv : m->facesets) {
+      auto& dst = out->facesets[kv.first];
+      for (int32_t f : kv.second) dst.push_back(f + out->nf);
+    }
+    out->nn += m->nn;
+    out->nc += m->nc;
+    out->nf += m->nf;
+  }
+  for (auto& kv : out->facesets) std::sort(kv.second.begin(), kv.second.end());
 }
 
 void hdg_mesh::upload() {
@@ -196,6 +237,10 @@ void hdg_mesh::upload() {
   }
   d_fcell.upload(fcell.data(), fcell.size(), s);
   d_flf.upload(flf.data(), flf.size(), s);
+  std::vector<int32_t> cp(nc);
+  for (int P = 0; P < nprob; ++P)
+    for (int c = prob_cell0[P]; c < prob_cell0[P + 1]; ++c) cp[c] = P;
+  d_cell_prob.upload(cp.data(), cp.size(), s);
   HDG_CUDA(cudaStreamSynchronize(s));
 }
 

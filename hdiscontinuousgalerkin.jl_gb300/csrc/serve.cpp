@@ -1,0 +1,380 @@
+// Serving engine: continuous batching of HDG solve requests on one GPU.
+//
+// Requests (a mesh, a degree, a source, a per-cell coefficient) queue on the host.  Each engine
+// step
+//   1. admits pending requests into new "flights" while the HBM budget allows: the requests of one
+//      degree form a disjoint union mesh with one space and one trace system, assembled,
+//      condensed and gathered by the same launches as a batch;
+//   2. enqueues one chunk of CG iterations for every flight in progress, each flight on its own
+//      CUDA stream so that flights overlap on the device;
+//   3. reads the flights' per-problem status and completes the flights whose problems are all done
+//      (recovery, result copy, latency stamp), freeing their memory for the next admissions.
+// So requests that arrive while others are on the GPU join at the next chunk boundary: admission
+// is by memory and slots, not by waiting for the device to drain.  Meshes registered as
+// resident keep their host topology in the engine, so a request on a resident mesh costs no mesh
+// construction.  No reference counterpart: the reference is a single-problem script.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <unordered_map>
+
+#include "hdg_internal.h"
+
+namespace {
+
+double now_s() {
+  using namespace std::chrono;
+  return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+struct Request {
+  int64_t id;
+  int mesh_id;                       // resident mesh, or -1
+  std::shared_ptr<hdg_mesh> mesh;    // the request's own host mesh when mesh_id < 0
+  int p, qd;
+  FieldSpec f;
+  std::vector<double> kappa;         // per cell (empty = 1)
+  double tau;
+  double t_submit;
+};
+
+struct Result {
+  int64_t id;
+  double t_submit, t_done;
+  hdg_stats stats;
+  std::vector<double> uhat, q, u;
+};
+
+// Bytes a flight holds on the device, per cell of degree p (condensed blocks, FP64 and FP32
+// matrix, CG vectors); a conservative estimate used for admission.
+size_t bytes_per_cell(int p) {
+  const size_t nt = p + 1, nw = (p + 1) * (p + 2) / 2, m = 3 * nt, n = 3 * nw;
+  const double faces_per_cell = 1.6;
+  return (size_t)(8 * (m * (m + 1) + n * (m + 1)) + faces_per_cell * (5 * nt * nt * 12 + 16 * nt * 8) + 64);
+}
+
+}  // namespace
+
+struct Flight {
+  hdg_ctx ctx;  // own stream
+  std::vector<Request> reqs;
+  hdg_mesh* mesh = nullptr;
+  hdg_space* space = nullptr;
+  hdg_system* sys = nullptr;
+  CgSolver* cg = nullptr;
+  int rep = 0;
+  size_t bytes = 0;
+  ~Flight() {
+    delete cg;
+    if (sys) hdg_system_destroy(sys);
+    if (space) hdg_space_destroy(space);
+    if (mesh) hdg_mesh_destroy(mesh);
+  }
+};
+
+struct hdg_engine {
+  hdg_ctx* ctx = nullptr;
+  double budget = 0;
+  int max_batch = 256;
+  int max_flights = 8;
+  hdg_solver solver{};
+  std::vector<std::shared_ptr<hdg_mesh>> resident;
+  std::vector<int> resident_p;
+  std::deque<Request> pending;
+  std::vector<std::unique_ptr<Flight>> flights;
+  std::deque<Result> done;
+  std::vector<cudaStream_t> streams;  // pool, one per flight slot
+  std::vector<char> stream_busy;
+  size_t in_use = 0;
+  int64_t next_id = 1;
+  bool keep_results = true;
+};
+
+namespace {
+
+std::shared_ptr<hdg_mesh> copy_host_mesh(const hdg_mesh* m) {
+  auto c = std::make_shared<hdg_mesh>();
+  c->ctx = nullptr;
+  c->nn = m->nn; c->nc = m->nc; c->nf = m->nf;
+  c->xy = m->xy; c->cells = m->cells; c->cfaces = m->cfaces; c->faces = m->faces; c->facesets = m->facesets;
+  c->structured = m->structured; c->nx = m->nx; c->ny = m->ny;
+  c->LL[0] = m->LL[0]; c->LL[1] = m->LL[1]; c->UR[0] = m->UR[0]; c->UR[1] = m->UR[1];
+  c->nprob = m->nprob; c->prob_node0 = m->prob_node0; c->prob_cell0 = m->prob_cell0; c->prob_face0 = m->prob_face0;
+  return c;
+}
+
+const hdg_mesh* request_mesh(const hdg_engine* e, const Request& r) {
+  return r.mesh_id >= 0 ? e->resident[r.mesh_id].get() : r.mesh.get();
+}
+
+// Builds and starts a flight from `reqs` (same degree and quadrature) on stream slot `slot`.
+Flight* launch_flight(hdg_engine* e, std::vector<Request>&& reqs, int slot) {
+  std::unique_ptr<Flight> fl(new Flight());
+  fl->ctx.device = e->ctx->device;
+  fl->ctx.stream = e->streams[slot];
+  fl->ctx.own_stream = false;
+  fl->ctx.profiling = false;
+  fl->reqs = std::move(reqs);
+  std::vector<const hdg_mesh*> parts;
+  for (auto& r : fl->reqs) parts.push_back(request_mesh(e, r));
+  hdg_ctx* c = &fl->ctx;
+  int rc = hdg_mesh_concat(c, (int)parts.size(), parts.data(), &fl->mesh);
+  if (rc != HDG_OK) throw HdgError{rc, c->err};
+  const int p = fl->reqs[0].p, qd = fl->reqs[0].qd;
+  rc = hdg_space_create(fl->mesh, p, qd, &fl->space);
+  if (rc != HDG_OK) throw HdgError{rc, c->err};
+  const int np = (int)fl->reqs.size();
+  std::vector<hdg_field> fs(np);
+  std::vector<double> taus(np), kappa;
+  bool any_kappa = false;
+  for (auto& r : fl->reqs) any_kappa |= !r.kappa.empty();
+  for (int P = 0; P < np; ++P) {
+    const Request& r = fl->reqs[P];
+    fs[P] = hdg_field{r.f.kind, (int)r.f.prm.size(), r.f.prm.data()};
+    taus[P] = r.tau;
+    if (any_kappa) {
+      const int nc = request_mesh(e, r)->nc;
+      if (r.kappa.empty()) kappa.insert(kappa.end(), nc, 1.0);
+      else kappa.insert(kappa.end(), r.kappa.begin(), r.kappa.end());
+    }
+  }
+  rc = hdg_assemble_condense_batch(fl->space, taus.data(), fs.data(), nullptr, any_kappa ? kappa.data() : nullptr,
+                                   e->solver.precision, &fl->sys);
+  if (rc != HDG_OK) throw HdgError{rc, c->err};
+  int cnt = 0;
+  hdg_field zero{HDG_FIELD_CONST, 0, nullptr};
+  rc = hdg_dirichlet(fl->space, "boundary", &zero, nullptr, nullptr, &cnt);
+  if (rc != HDG_OK) throw HdgError{rc, c->err};
+  std::vector<int32_t> dofs(cnt);
+  std::vector<double> vals(cnt);
+  rc = hdg_dirichlet(fl->space, "boundary", &zero, dofs.data(), vals.data(), &cnt);
+  if (rc == HDG_OK) rc = hdg_apply_dirichlet(fl->sys, dofs.data(), vals.data(), cnt);
+  if (rc != HDG_OK) throw HdgError{rc, c->err};
+  g_alloc_stream = c->stream;
+  fl->cg = make_cg_solver(fl->sys);
+  fl->cg->prepare(e->solver);
+  return fl.release();
+}
+
+void complete_flight(hdg_engine* e, Flight* fl) {
+  std::vector<hdg_stats> st;
+  g_alloc_stream = fl->ctx.stream;
+  fl->cg->finish(e->solver, &st);
+  fl->sys->have_solution = true;
+  launch_recover(fl->sys, fl->ctx.stream);
+  fl->sys->have_recovery = true;
+  hdg_system* s = fl->sys;
+  std::vector<double> x, qu;
+  if (e->keep_results) {
+    x.resize(s->ndofs);
+    qu.resize((size_t)s->nc * s->n);
+    s->d_x.download(x.data(), x.size(), fl->ctx.stream);
+    s->d_qu.download(qu.data(), qu.size(), fl->ctx.stream);
+  }
+  HDG_CUDA(cudaStreamSynchronize(fl->ctx.stream));
+  const double t = now_s();
+  const hdg_mesh* m = fl->mesh;
+  const int nv = 2 * s->nw;
+  for (size_t P = 0; P < fl->reqs.size(); ++P) {
+    Result r;
+    r.id = fl->reqs[P].id;
+    r.t_submit = fl->reqs[P].t_submit;
+    r.t_done = t;
+    r.stats = st[P];
+    if (e->keep_results) {
+      r.uhat.assign(x.begin() + (size_t)m->prob_face0[P] * s->nt, x.begin() + (size_t)m->prob_face0[P + 1] * s->nt);
+      for (int c = m->prob_cell0[P]; c < m->prob_cell0[P + 1]; ++c) {
+        r.q.insert(r.q.end(), qu.begin() + (size_t)c * s->n, qu.begin() + (size_t)c * s->n + nv);
+        r.u.insert(r.u.end(), qu.begin() + (size_t)c * s->n + nv, qu.begin() + (size_t)(c + 1) * s->n);
+      }
+    }
+    e->done.push_back(std::move(r));
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int hdg_engine_create(hdg_ctx* ctx, double hbm_budget_gb, int max_batch, int max_flights, const hdg_solver* opts,
+                      hdg_engine** out) {
+  if (!ctx || !out || !(hbm_budget_gb > 0) || max_batch < 1 || max_flights < 1) return HDG_ERR_ARG;
+  try {
+    HDG_CUDA(cudaSetDevice(ctx->device));
+    hdg_engine* e = new hdg_engine();
+    e->ctx = ctx;
+    e->budget = hbm_budget_gb * 1e9;
+    e->max_batch = max_batch;
+    e->max_flights = max_flights;
+    hdg_solver d{1e-10, 100000, HDG_PREC_MIXED, 32, 1e-5};
+    e->solver = opts ? *opts : d;
+    if (!(e->solver.tol > 0)) e->solver.tol = d.tol;
+    if (e->solver.maxit <= 0) e->solver.maxit = d.maxit;
+    if (e->solver.chunk <= 0) e->solver.chunk = d.chunk;
+    e->streams.resize(max_flights);
+    e->stream_busy.assign(max_flights, 0);
+    for (auto& s : e->streams) HDG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    *out = e;
+    return HDG_OK;
+  } catch (const HdgError& err) {
+    ctx->err = err.msg;
+    return err.code;
+  }
+}
+
+int hdg_engine_add_resident_mesh(hdg_engine* e, const hdg_mesh* host_mesh, int p, int* mesh_id) {
+  if (!e || !host_mesh || !mesh_id) return HDG_ERR_ARG;
+  e->resident.push_back(copy_host_mesh(host_mesh));
+  e->resident_p.push_back(p);
+  *mesh_id = (int)e->resident.size() - 1;
+  return HDG_OK;
+}
+
+int hdg_engine_submit(hdg_engine* e, int mesh_id, const hdg_mesh* mesh, int p, int quad_degree, const hdg_field* f,
+                      const double* kappa_cell, double tau, int64_t* request_id) {
+  if (!e || !f || (mesh_id < 0 && !mesh) || mesh_id >= (int)e->resident.size() || p < 1 || p > HDG_MAX_P)
+    return HDG_ERR_ARG;
+  Request r;
+  r.id = e->next_id++;
+  r.mesh_id = mesh_id;
+  if (mesh_id < 0) r.mesh = copy_host_mesh(mesh);
+  r.p = p;
+  r.qd = quad_degree > 0 ? quad_degree : p + 1;
+  r.f = field_from(f, 0.0);
+  const int nc = mesh_id >= 0 ? e->resident[mesh_id]->nc : mesh->nc;
+  if (kappa_cell) r.kappa.assign(kappa_cell, kappa_cell + nc);
+  r.tau = tau > 0 ? tau : 1.0;
+  r.t_submit = now_s();
+  e->pending.push_back(std::move(r));
+  if (request_id) *request_id = e->pending.back().id;
+  return HDG_OK;
+}
+
+// One engine step: admit, advance every flight by one chunk, complete finished flights.
+int hdg_engine_step(hdg_engine* e, int* n_inflight, int* n_pending) {
+  if (!e) return HDG_ERR_ARG;
+  try {
+    HDG_CUDA(cudaSetDevice(e->ctx->device));
+    // 1. admission: one flight per (degree, quadrature) group of the pending queue, FIFO order
+    while (!e->pending.empty() && (int)e->flights.size() < e->max_flights) {
+      const int p = e->pending.front().p, qd = e->pending.front().qd;
+      std::vector<Request> take;
+      size_t bytes = 0;
+      for (auto it = e->pending.begin(); it != e->pending.end() && (int)take.size() < e->max_batch;) {
+        if (it->p != p || it->qd != qd) { ++it; continue; }
+        const size_t b = bytes_per_cell(p) * (size_t)request_mesh(e, *it)->nc;
+        if (e->in_use + bytes + b > e->budget && !take.empty()) break;
+        if (e->in_use + bytes + b > e->budget && !e->flights.empty()) break;  // wait for memory
+        bytes += b;
+        take.push_back(std::move(*it));
+        it = e->pending.erase(it);
+      }
+      if (take.empty()) break;
+      int slot = 0;
+      while (e->stream_busy[slot]) ++slot;
+      Flight* fl = launch_flight(e, std::move(take), slot);
+      fl->bytes = bytes;
+      e->stream_busy[slot] = 1;
+      e->in_use += bytes;
+      e->flights.emplace_back(fl);
+    }
+    // 2. one chunk for every flight, each on its own stream
+    for (auto& fl : e->flights) {
+      g_alloc_stream = fl->ctx.stream;
+      fl->cg->launch_chunk(fl->rep++);
+      fl->cg->enqueue_status_copy();
+    }
+    // 3. status, completion
+    for (auto& fl : e->flights) HDG_CUDA(cudaStreamSynchronize(fl->ctx.stream));
+    for (size_t i = 0; i < e->flights.size();) {
+      Flight* fl = e->flights[i].get();
+      g_alloc_stream = fl->ctx.stream;
+      if (fl->cg->process(e->solver)) {
+        complete_flight(e, fl);
+        e->ctx->launches += fl->ctx.launches;
+        for (size_t k = 0; k < e->streams.size(); ++k)
+          if (e->streams[k] == fl->ctx.stream) e->stream_busy[k] = 0;
+        e->in_use -= fl->bytes;
+        e->flights.erase(e->flights.begin() + i);
+      } else {
+        ++i;
+      }
+    }
+    if (n_inflight) {
+      int n = 0;
+      for (auto& fl : e->flights) n += (int)fl->reqs.size();
+      *n_inflight = n;
+    }
+    if (n_pending) *n_pending = (int)e->pending.size();
+    return HDG_OK;
+  } catch (const HdgError& err) {
+    e->ctx->err = err.msg;
+    return err.code;
+  }
+}
+
+// Completed requests since the last poll: ids, latency (s), CG iterations, final relative
+// residual, converged flag.  Results stay available to hdg_engine_result until taken.
+int hdg_engine_poll(hdg_engine* e, int max, int64_t* ids, double* latency, int* iterations, double* residual,
+                    int* converged, int* n) {
+  if (!e || !n) return HDG_ERR_ARG;
+  int k = 0;
+  for (auto& r : e->done) {
+    if (k >= max) break;
+    if (r.t_done < 0) continue;  // already polled
+    if (ids) ids[k] = r.id;
+    if (latency) latency[k] = r.t_done - r.t_submit;
+    if (iterations) iterations[k] = r.stats.iterations;
+    if (residual) residual[k] = r.stats.rel_residual;
+    if (converged) converged[k] = r.stats.converged;
+    r.t_done = -1.0;
+    ++k;
+  }
+  *n = k;
+  while (!e->done.empty() && e->done.front().t_done < 0 && e->done.front().uhat.empty()) e->done.pop_front();
+  return HDG_OK;
+}
+
+// Solution of a completed request (trace values, q per cell, u per cell; any may be NULL to query
+// sizes); the result is released after this call.
+int hdg_engine_result(hdg_engine* e, int64_t id, double* uhat, double* q, double* u, int* nuhat, int* nq, int* nu) {
+  if (!e) return HDG_ERR_ARG;
+  for (auto it = e->done.begin(); it != e->done.end(); ++it) {
+    if (it->id != id) continue;
+    if (nuhat) *nuhat = (int)it->uhat.size();
+    if (nq) *nq = (int)it->q.size();
+    if (nu) *nu = (int)it->u.size();
+    if (!uhat && !q && !u) return HDG_OK;
+    if (uhat) std::memcpy(uhat, it->uhat.data(), it->uhat.size() * sizeof(double));
+    if (q) std::memcpy(q, it->q.data(), it->q.size() * sizeof(double));
+    if (u) std::memcpy(u, it->u.data(), it->u.size() * sizeof(double));
+    it->uhat.clear(); it->uhat.shrink_to_fit();
+    it->q.clear(); it->q.shrink_to_fit();
+    it->u.clear(); it->u.shrink_to_fit();
+    return HDG_OK;
+  }
+  return HDG_ERR_ARG;
+}
+
+int hdg_engine_set_keep_results(hdg_engine* e, int keep) {
+  if (!e) return HDG_ERR_ARG;
+  e->keep_results = keep != 0;
+  return HDG_OK;
+}
+
+int hdg_engine_destroy(hdg_engine* e) {
+  if (!e) return HDG_OK;
+  cudaSetDevice(e->ctx->device);
+  for (auto& fl : e->flights) cudaStreamSynchronize(fl->ctx.stream);
+  e->flights.clear();
+  for (auto s : e->streams) {
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+  }
+  delete e;
+  return HDG_OK;
+}
+
+}  // extern "C"

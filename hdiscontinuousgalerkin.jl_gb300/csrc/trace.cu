@@ -1,13 +1,16 @@
-// Global trace system: deterministic gather of the condensed cell blocks into a block-sparse
-// matrix, and the Dirichlet treatment of apply!.
+// Global trace system: deterministic gather of the condensed cell blocks into the trace matrix,
+// and the Dirichlet treatment of apply!.
 //
-// The reference appends every cell's Ate as COO triplets and lets `sparse(I,J,V)` sort them
-// and sum duplicates (src/assembler.jl:31-49).  Here the pattern is known from the topology:
-// block row f (a face) holds nt x nt blocks for f itself and for the other faces of its one or
-// two cells, sorted by face id.  Each block has at most two sources (cell, local face pair): the
-// diagonal block sums the blocks of the face's two cells, an off-diagonal block has exactly one.
-// The source map is built once per mesh, so assembly is an atomic-free gather, and because a
-// sum of two terms does not depend on their order it reproduces the reference values exactly.
+// The reference appends every cell's Ate as COO triplets and lets `sparse(I,J,V)` sort them and
+// sum duplicates (src/assembler.jl:31-49).  Here the pattern is known from the topology: block
+// row f (a face) holds nt x nt blocks for f itself and for the other faces of its one or two
+// cells.  Each block has at most two sources (cell, local face pair): the diagonal block sums the
+// blocks of the face's two cells, an off-diagonal block has exactly one.  The source map is built
+// once per mesh, so assembly is an atomic-free gather; a sum of two terms does not depend on
+// their order, so it reproduces the reference values exactly.
+//
+// Device layout (block-ELL, see hdg_internal.h): 5 slots per face, slot-major and
+// row-contiguous, so every warp-wide load of the matrix in the CG is one contiguous segment.
 #include <algorithm>
 
 #include "hdg_device.cuh"
@@ -15,11 +18,14 @@
 void build_block_structure(hdg_system* s) {
   const hdg_mesh* m = s->space->mesh;
   const int nf = m->nf;
+  constexpr int S = hdg_system::SLOTS;
   s->h_browptr.assign(nf + 1, 0);
   s->h_bcol.clear();
   s->h_bsrc.clear();
-  s->h_bcol.reserve((size_t)nf * 5);
-  s->h_bsrc.reserve((size_t)nf * 10);
+  s->h_bcol.reserve((size_t)nf * S);
+  s->h_bsrc.reserve((size_t)nf * S * 2);
+  std::vector<int32_t> bcol5((size_t)S * nf), src5((size_t)S * nf * 2, -1);
+  std::vector<int8_t> kdiag(nf, 0);
   int nb[8];
   for (int f = 0; f < nf; ++f) {
     const int c1 = m->faces[4 * f + 2], c2 = m->faces[4 * f + 3];
@@ -34,8 +40,11 @@ void build_block_structure(hdg_system* s) {
     }
     std::sort(nb, nb + cnt);
     cnt = (int)(std::unique(nb, nb + cnt) - nb);
+    if (cnt > S) throw HdgError{HDG_ERR_ARG, "a face couples to more than 4 other faces (invalid triangle mesh)"};
+    for (int k = 0; k < S; ++k) bcol5[(size_t)k * nf + f] = f;
     for (int k = 0; k < cnt; ++k) {
       const int g = nb[k];
+      if (g == f) kdiag[f] = (int8_t)k;
       int src[2] = {-1, -1}, ns = 0;
       for (int c : {c1, c2}) {
         if (c < 0) continue;
@@ -49,33 +58,77 @@ void build_block_structure(hdg_system* s) {
       s->h_bcol.push_back(g);
       s->h_bsrc.push_back(src[0]);
       s->h_bsrc.push_back(src[1]);
+      bcol5[(size_t)k * nf + f] = g;
+      src5[((size_t)k * nf + f) * 2] = src[0];
+      src5[((size_t)k * nf + f) * 2 + 1] = src[1];
     }
     s->h_browptr[f + 1] = (int32_t)s->h_bcol.size();
   }
   s->nblocks = (int64_t)s->h_bcol.size();
   s->nnz = s->nblocks * s->nt * s->nt;
   cudaStream_t st = s->ctx->stream;
-  s->d_browptr.upload(s->h_browptr.data(), s->h_browptr.size(), st);
-  s->d_bcol.upload(s->h_bcol.data(), s->h_bcol.size(), st);
-  s->d_bsrc.upload(s->h_bsrc.data(), s->h_bsrc.size(), st);
+  s->d_bcol5.upload(bcol5.data(), bcol5.size(), st);
+  s->d_src5.upload(src5.data(), src5.size(), st);
+  s->d_kdiag.upload(kdiag.data(), kdiag.size(), st);
+  HDG_CUDA(cudaStreamSynchronize(st));
+}
+
+// Segments of the row-parallel kernels: every problem's trace rows are cut into ranges of at most
+// SEG_ROWS rows, one CUDA block each, so a block never spans two problems.
+void build_segments(hdg_system* s) {
+  constexpr int SEG_ROWS = 1024;  // 4 rows per thread (interleaved in the CG kernels for ILP)
+  const hdg_mesh* m = s->space->mesh;
+  s->nprob = m->nprob;
+  s->h_prob_row0.assign(s->nprob + 1, 0);
+  std::vector<int32_t> sp, r0, r1, b0(s->nprob), nb(s->nprob), rowp((size_t)s->ndofs);
+  for (int P = 0; P < s->nprob; ++P) {
+    const int a = m->prob_face0[P] * s->nt, e = m->prob_face0[P + 1] * s->nt;
+    s->h_prob_row0[P] = a;
+    s->h_prob_row0[P + 1] = e;
+    const int rows = std::max(e - a, 1);
+    const int n = std::max(1, std::min((rows + SEG_ROWS - 1) / SEG_ROWS, 1216));
+    const int per = (rows + n - 1) / n;
+    b0[P] = (int32_t)sp.size();
+    nb[P] = n;
+    for (int k = 0; k < n; ++k) {
+      sp.push_back(P);
+      r0.push_back(std::min(e, a + k * per));
+      r1.push_back(std::min(e, a + (k + 1) * per));
+    }
+    for (int r = a; r < e; ++r) rowp[r] = P;
+  }
+  s->nseg = (int)sp.size();
+  cudaStream_t st = s->ctx->stream;
+  s->d_seg_prob.upload(sp.data(), sp.size(), st);
+  s->d_seg_row0.upload(r0.data(), r0.size(), st);
+  s->d_seg_row1.upload(r1.data(), r1.size(), st);
+  s->d_prob_blk0.upload(b0.data(), b0.size(), st);
+  s->d_prob_nblk.upload(nb.data(), nb.size(), st);
+  s->d_row_prob.upload(rowp.data(), rowp.size(), st);
+  s->ensure_reduction_buffers();
+  HDG_CUDA(cudaStreamSynchronize(st));
 }
 
 namespace {
+constexpr int S5 = hdg_system::SLOTS;
 
-// value entry t of block b: K[f nt + i, g nt + j] = sum over sources of Ate_c[lf nt + i, lg nt + j]
+// val[(k nt + j) ndofs + r] = sum over sources of Ate_c[lf nt + i, lg nt + j], r = f nt + i
 template <int NT>
-__global__ void k_gather(const int64_t nval, const int32_t* __restrict__ bsrc, const double* __restrict__ AB,
+__global__ void k_gather(const int nf, const int32_t* __restrict__ src5, const double* __restrict__ AB,
                          double* __restrict__ val) {
-  constexpr int M = 3 * NT, MS = M + 1, BB = NT * NT;
+  constexpr int M = 3 * NT, MS = M + 1;
+  const int64_t ndofs = (int64_t)nf * NT, nval = ndofs * S5 * NT;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nval; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t b = t / BB;
-    const int ij = (int)(t - b * BB), i = ij / NT, j = ij - (ij / NT) * NT;
+    const int s = (int)(t / ndofs);
+    const int r = (int)(t - (int64_t)s * ndofs);
+    const int f = r / NT, i = r - f * NT, k = s / NT, j = s - k * NT;
+    const int* sp = src5 + ((int64_t)k * nf + f) * 2;
     double v = 0.0;
 #pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      const int s = bsrc[2 * b + k];
-      if (s >= 0) {
-        const int c = s / 9, lf = (s / 3) % 3, lg = s % 3;
+    for (int q = 0; q < 2; ++q) {
+      const int sr = sp[q];
+      if (sr >= 0) {
+        const int c = sr / 9, lf = (sr / 3) % 3, lg = sr % 3;
         v += AB[(int64_t)c * M * MS + (lf * NT + i) * MS + lg * NT + j];
       }
     }
@@ -100,55 +153,41 @@ __global__ void k_gather_rhs(const int nf, const int32_t* __restrict__ fcell, co
   b[t] = v;
 }
 
-// meandiag(K) = mean |K_ii| (src/boundary.jl:374-380): fixed-order per-block partial sums,
-// reduced by the last block to finish (deterministic, no floating-point atomics).
+// meandiag(K) = mean |K_ii| of each problem (src/boundary.jl:374-380), a deterministic
+// per-problem reduction over the segments.
 template <int NT>
-__global__ void k_meandiag(const int nf, const int32_t* __restrict__ browptr, const int32_t* __restrict__ bcol,
-                           const double* __restrict__ val, double* __restrict__ partial, unsigned* counter,
-                           double* out) {
+__global__ void k_meandiag(SegArgs g, const int32_t* __restrict__ prob_row0, const int nf,
+                           const int8_t* __restrict__ kdiag, const double* __restrict__ val, double* __restrict__ mdiag) {
   __shared__ double sh[32];
-  __shared__ bool last;
+  const int P = g.seg_prob[blockIdx.x];
+  const int ndofs = nf * NT;
   double acc = 0.0;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nf * NT; t += gridDim.x * blockDim.x) {
-    const int f = t / NT, i = t - f * NT;
-    for (int b = browptr[f]; b < browptr[f + 1]; ++b)
-      if (bcol[b] == f) acc += fabs(val[(int64_t)b * NT * NT + i * NT + i]);
+  for (int r = g.seg_row0[blockIdx.x] + threadIdx.x; r < g.seg_row1[blockIdx.x]; r += blockDim.x) {
+    const int f = r / NT, i = r - f * NT;
+    acc += fabs(val[(int64_t)(kdiag[f] * NT + i) * ndofs + r]);
   }
-  acc = block_sum<256>(acc, sh);
-  if (threadIdx.x == 0) {
-    partial[blockIdx.x] = acc;
-    __threadfence();
-    unsigned v = atomicAdd(counter, 1u);
-    last = (v == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (last) {
-    __threadfence();
-    double s = 0.0;
-    for (int k = threadIdx.x; k < gridDim.x; k += blockDim.x) s += ((volatile double*)partial)[k];
-    s = block_sum<256>(s, sh);
-    if (threadIdx.x == 0) {
-      out[0] = s / (double)(nf * NT);
-      *counter = 0;
-    }
-  }
+  double s0, s1;
+  if (seg_finish<256>(g, P, 3, acc, 0.0, sh, &s0, &s1) && threadIdx.x == 0)
+    mdiag[P] = s0 / (double)(prob_row0[P + 1] - prob_row0[P]);
 }
 
 // b -= sum_d v_d K[:, d] over prescribed dofs with v_d != 0 (src/boundary.jl:334-343); gv holds
-// v at prescribed dofs and 0 elsewhere, so this is one block-sparse product with gv.
+// v at prescribed dofs and 0 elsewhere, so this is one sparse product with gv.
 template <int NT>
-__global__ void k_lift(const int nf, const int32_t* __restrict__ browptr, const int32_t* __restrict__ bcol,
-                       const double* __restrict__ val, const double* __restrict__ gv, double* __restrict__ b) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nf * NT) return;
-  const int f = t / NT, i = t - f * NT;
+__global__ void k_lift(const int nf, const int32_t* __restrict__ bcol5, const double* __restrict__ val,
+                       const double* __restrict__ gv, double* __restrict__ b) {
+  const int ndofs = nf * NT;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= ndofs) return;
+  const int f = r / NT;
   double s = 0.0;
-  for (int k = browptr[f]; k < browptr[f + 1]; ++k) {
-    const int g = bcol[k];
 #pragma unroll
-    for (int j = 0; j < NT; ++j) s += val[(int64_t)k * NT * NT + i * NT + j] * gv[g * NT + j];
+  for (int k = 0; k < S5; ++k) {
+    const int g = bcol5[k * nf + f];
+#pragma unroll
+    for (int j = 0; j < NT; ++j) s += val[(int64_t)(k * NT + j) * ndofs + r] * gv[g * NT + j];
   }
-  b[t] -= s;
+  b[r] -= s;
 }
 
 // Rows and columns of prescribed dofs zeroed, K[d,d] = m, b[d] = v m (src/boundary.jl:344-362).
@@ -156,37 +195,26 @@ __global__ void k_lift(const int nf, const int32_t* __restrict__ browptr, const 
 // symmetric positive definite (the condensed HDG trace operator is negative definite on the free
 // dofs).  hdg_system_get_csc undoes the sign when exporting.
 template <int NT>
-__global__ void k_apply(const int nf, const int32_t* __restrict__ browptr, const int32_t* __restrict__ bcol,
+__global__ void k_apply(const int nf, const int32_t* __restrict__ bcol5, const int8_t* __restrict__ kdiag,
                         const uint8_t* __restrict__ pres, const double* __restrict__ gv, const double* __restrict__ md,
-                        double* __restrict__ val, double* __restrict__ b) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nf * NT) return;
-  const int f = t / NT, i = t - f * NT;
-  const double m = md[0];
-  const bool pr = pres[t];
-  for (int k = browptr[f]; k < browptr[f + 1]; ++k) {
-    const int g = bcol[k];
+                        const int32_t* __restrict__ row_prob, double* __restrict__ val, double* __restrict__ b) {
+  const int ndofs = nf * NT;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= ndofs) return;
+  const int f = r / NT, i = r - f * NT, kd = kdiag[f];
+  const double m = md[row_prob[r]];
+  const bool pr = pres[r];
+#pragma unroll
+  for (int k = 0; k < S5; ++k) {
+    const int g = bcol5[k * nf + f];
 #pragma unroll
     for (int j = 0; j < NT; ++j) {
-      const int c = g * NT + j;
-      double& v = val[(int64_t)k * NT * NT + i * NT + j];
-      if (pr || pres[c]) v = (c == t) ? m : 0.0;
+      double& v = val[(int64_t)(k * NT + j) * ndofs + r];
+      if (pr || pres[g * NT + j]) v = (k == kd && j == i) ? m : 0.0;
       else v = -v;
     }
   }
-  b[t] = pr ? gv[t] * m : -b[t];
-}
-
-template <int NT> void gather_t(hdg_system* s, cudaStream_t st) {
-  hdg_mesh* m = s->space->mesh;
-  const int64_t nval = s->nblocks * NT * NT;
-  int blocks = (int)std::min<int64_t>((nval + 255) / 256, 152 * 32);
-  k_gather<NT><<<blocks, 256, 0, st>>>(nval, s->d_bsrc.p, s->d_AB.p, s->d_val.p);
-  HDG_CUDA(cudaGetLastError());
-  const int nrow = m->nf * NT;
-  k_gather_rhs<NT><<<(nrow + 255) / 256, 256, 0, st>>>(m->nf, m->d_fcell.p, m->d_flf.p, s->d_AB.p, s->d_b.p);
-  HDG_CUDA(cudaGetLastError());
-  s->ctx->launches += 2;
+  b[r] = pr ? gv[r] * m : -b[r];
 }
 
 // prescribed dofs -> per-dof flag and value
@@ -196,6 +224,18 @@ __global__ void k_scatter_dirichlet(const int n, const int32_t* __restrict__ dof
   if (k >= n) return;
   pres[dofs[k]] = 1;
   gv[dofs[k]] = vals[k];
+}
+
+template <int NT> void gather_t(hdg_system* s, cudaStream_t st) {
+  hdg_mesh* m = s->space->mesh;
+  const int64_t nval = (int64_t)s->ndofs * S5 * NT;
+  int blocks = (int)std::min<int64_t>((nval + 255) / 256, 152 * 32);
+  k_gather<NT><<<blocks, 256, 0, st>>>(m->nf, s->d_src5.p, s->d_AB.p, s->d_val.p);
+  HDG_CUDA(cudaGetLastError());
+  const int nrow = m->nf * NT;
+  k_gather_rhs<NT><<<(nrow + 255) / 256, 256, 0, st>>>(m->nf, m->d_fcell.p, m->d_flf.p, s->d_AB.p, s->d_b.p);
+  HDG_CUDA(cudaGetLastError());
+  s->ctx->launches += 2;
 }
 
 template <int NT>
@@ -218,17 +258,19 @@ void apply_t(hdg_system* s, const std::vector<int32_t>& dofs0, const std::vector
     HDG_CUDA(cudaGetLastError());
     s->ctx->launches++;
   }
-  const int rb = std::min(1024, (nrow + 255) / 256);
-  k_meandiag<NT><<<rb, 256, 0, st>>>(m->nf, s->d_browptr.p, s->d_bcol.p, s->d_val.p, s->d_part.p, s->d_cnt.p,
-                                     s->d_scal.p);
+  s->d_mdiag.alloc(s->nprob);
+  DevBuf<int32_t>& prow = s->d_prob_row0_dev();
+  const SegArgs g{s->d_seg_prob.p, s->d_seg_row0.p, s->d_seg_row1.p, s->d_prob_blk0.p, s->d_prob_nblk.p, s->d_part.p,
+                  s->d_cnt.p};
+  k_meandiag<NT><<<s->nseg, 256, 0, st>>>(g, prow.p, m->nf, s->d_kdiag.p, s->d_val.p, s->d_mdiag.p);
   HDG_CUDA(cudaGetLastError());
   if (lift) {
-    k_lift<NT><<<(nrow + 255) / 256, 256, 0, st>>>(m->nf, s->d_browptr.p, s->d_bcol.p, s->d_val.p, s->d_gv.p, s->d_b.p);
+    k_lift<NT><<<(nrow + 255) / 256, 256, 0, st>>>(m->nf, s->d_bcol5.p, s->d_val.p, s->d_gv.p, s->d_b.p);
     HDG_CUDA(cudaGetLastError());
     s->ctx->launches++;
   }
-  k_apply<NT><<<(nrow + 255) / 256, 256, 0, st>>>(m->nf, s->d_browptr.p, s->d_bcol.p, s->d_pres.p, s->d_gv.p,
-                                                  s->d_scal.p, s->d_val.p, s->d_b.p);
+  k_apply<NT><<<(nrow + 255) / 256, 256, 0, st>>>(m->nf, s->d_bcol5.p, s->d_kdiag.p, s->d_pres.p, s->d_gv.p,
+                                                  s->d_mdiag.p, s->d_row_prob.p, s->d_val.p, s->d_b.p);
   HDG_CUDA(cudaGetLastError());
   s->ctx->launches += 2;
 }

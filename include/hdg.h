@@ -194,6 +194,52 @@ typedef struct {
 /* Per-phase device times recorded while profiling was on (0 where nothing was recorded). */
 int hdg_system_timings(hdg_system* sys, hdg_timings* out);
 
+/* ---- batches of independent problems ------------------------------------------------ */
+/* No reference counterpart: the reference solves one problem per script run.  A batch is a
+ * disjoint union of problem meshes of one degree: one space, one system, one set of launches. */
+/* Disjoint union of meshes (host-only parts, built with ctx == NULL, are fine): ids of part P are
+ * shifted by the sizes of the parts before it; face sets are merged. */
+int hdg_mesh_concat(hdg_ctx* ctx, int nparts, const hdg_mesh* const* parts, hdg_mesh** out);
+/* Problems of a (union) mesh and their first node/cell/face (arrays of nprob+1, 0-based; NULL skips). */
+int hdg_mesh_problems(const hdg_mesh* mesh, int* nprob, int32_t* node0, int32_t* cell0, int32_t* face0);
+/* As hdg_assemble_condense, with one tau / source / kappa field per problem (arrays of nprob;
+ * tau and kappa may be NULL). */
+int hdg_assemble_condense_batch(hdg_space* space, const double* tau, const hdg_field* f, const hdg_field* kappa,
+                                const double* kappa_cell, int precision, hdg_system** out);
+int hdg_system_reassemble_batch(hdg_system* sys, const double* tau, const hdg_field* f, const hdg_field* kappa,
+                                const double* kappa_cell);
+/* Solves every problem of several systems (for example one per degree) in one interleaved loop;
+ * each problem stops independently.  stats: one entry per problem, systems in order. */
+int hdg_solve_batch(int nsys, hdg_system* const* systems, const hdg_solver* opts, hdg_stats* stats);
+/* Device solution of a system: trace values (ndofs) and, after recovery, [q; u] per cell (ncells x n). */
+int hdg_system_get_solution(const hdg_system* sys, double* uhat, double* qu);
+
+/* ---- serving: continuous batching of solve requests ----------------------------------- */
+/* No reference counterpart.  Requests queue on the host; every hdg_engine_step admits pending
+ * requests into "flights" (one disjoint union system per degree, at most max_batch requests)
+ * while the HBM budget and the flight slots allow, advances every flight by one chunk of CG
+ * iterations on its own CUDA stream, and completes the flights whose problems are all done.
+ * Requests arriving while others run join at the next step; flights overlap on the device. */
+typedef struct hdg_engine hdg_engine;
+int hdg_engine_create(hdg_ctx* ctx, double hbm_budget_gb, int max_batch, int max_flights, const hdg_solver* opts,
+                      hdg_engine** out);
+/* Registers a host mesh (built with ctx == NULL) of degree p as resident: requests on it need no
+ * mesh construction. */
+int hdg_engine_add_resident_mesh(hdg_engine* e, const hdg_mesh* host_mesh, int p, int* mesh_id);
+/* Queues a request on resident mesh `mesh_id`, or (mesh_id < 0) on its own host mesh `mesh`. */
+int hdg_engine_submit(hdg_engine* e, int mesh_id, const hdg_mesh* mesh, int p, int quad_degree, const hdg_field* f,
+                      const double* kappa_cell, double tau, int64_t* request_id);
+int hdg_engine_step(hdg_engine* e, int* n_inflight, int* n_pending);
+/* Completed requests since the last poll (at most max): id, latency in seconds, iterations,
+ * true relative residual, converged flag.  NULL arrays are skipped. */
+int hdg_engine_poll(hdg_engine* e, int max, int64_t* ids, double* latency, int* iterations, double* residual,
+                    int* converged, int* n);
+/* Solution of a completed request: û (its trace dofs), q (ncells x nv), u (ncells x nw); with all
+ * three NULL only the sizes are returned.  Released after the copy. */
+int hdg_engine_result(hdg_engine* e, int64_t id, double* uhat, double* q, double* u, int* nuhat, int* nq, int* nu);
+int hdg_engine_set_keep_results(hdg_engine* e, int keep);
+int hdg_engine_destroy(hdg_engine* e);
+
 /* ---- whole flow ---------------------------------------------------------------------- */
 /* The poisson2D_HDG flow in one call: assemble+condense, Dirichlet on `faceset` with g,
  * apply!, solve, recover.  Outputs are host arrays (any may be NULL). */

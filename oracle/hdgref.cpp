@@ -2,12 +2,12 @@
 //
 // TEST INFRASTRUCTURE ONLY.  This file is the oracle that the GPU library is checked
 // against.  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it,
-// and only as the checker or the timed CPU baseline; the product (libhdg) never links it.
+// and only as the test oracle or the timed CPU baseline; the product (libhdg) never links it.
 //
 // Every routine restates one piece of the reference (Julia) and cites the file:line it
 // follows.  The reference's quirks are kept on purpose (quadrature degree p+1, face
 // orientation flips, He without tau, the trace-Dirichlet projection), because parity is
-// judged against the reference's behaviour, not against textbook HDG.  The one deliberate
+// defined by the reference's behaviour, not against textbook HDG.  The one deliberate
 // generalisation is the recovery slice (examples/poisson2D_HDG.jl:205-206 hard-codes two
 // trace functions per edge); here it is (f-1)*nt+1 : f*nt for any nt.
 //

@@ -1,7 +1,7 @@
 """hdgref — Python side of the CPU oracle for the HDG Poisson flow.
 
 TEST INFRASTRUCTURE ONLY.  Loaded by tests/, ``__graft_entry__.smoke()`` and bench.py's
-CPU-baseline leg as the checker; the product never imports it.
+CPU-baseline leg as the test oracle; the product never imports it.
 
 The C++ half (``hdgref.cpp``) restates the reference's element loop, condensation and
 assembly; this half restates the Triangle-format reader (src/triangle_mesh.jl:47-172) and

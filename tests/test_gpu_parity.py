@@ -177,3 +177,83 @@ def test_error_paths(H):
     with pytest.raises(H.HDGError) as e:
         H.doassemble(Vh, Wh, Mh, 1.0, H.MANUFACTURED_F)
     assert e.value.code == -2
+
+
+@pytest.mark.parametrize("n,p,qd", [(32, 2, None), (16, 3, 6)])
+def test_mixed_precision_solve(H, oracle, n, p, qd):
+    """FP32 Krylov iteration with FP64 reliable updates reaches the FP64 tolerance: the solution
+    agrees with the FP64 solve and with the oracle's direct solve."""
+    mesh = H.rectangle_mesh(H.TriangleCell, (n, n), (0.0, 0.0), (1.0, 1.0))
+    Vh, Wh, Mh = spaces(H, mesh, p, qd)
+    K, b, _, _ = H.doassemble(Vh, Wh, Mh, 1.0, H.MANUFACTURED_F)
+    H.apply_(K, b, H.Dirichlet(H.TrialFunction(Mh), mesh, "boundary"))
+    u64 = H.solve(K, b, tol=1e-11)
+    it64 = K.stats.iterations
+    # the FP32 operator limits the attainable true residual to ~1e-12 on these systems
+    umx = H.solve(K, b, tol=1e-10, precision=H.PREC_MIXED)
+    assert K.stats.converged and K.stats.rel_residual <= 1e-10
+    assert K.stats.iterations < 3 * it64
+    S = oracle.System(oracle.rectangle_mesh(n, n), p, qd, 1.0, H.MANUFACTURED_F.as_oracle())
+    S.apply(*S.dirichlet())
+    ref = S.solve()
+    assert rel(umx, ref) < 1e-8
+    assert rel(umx, u64) < 1e-8
+
+
+def test_batch_matches_single_problems(H, oracle):
+    """A degree-binned batch (uneven sizes, p = 1..4, jitter, per-cell kappa, bump sources) gives
+    each problem the solution of the oracle run on that problem alone."""
+    rng = np.random.default_rng(7)
+    probs = []
+    for k, (n, p) in enumerate([(4, 1), (7, 2), (3, 3), (5, 4), (6, 1), (2, 2), (4, 3)]):
+        f = H.Field.bumps(rng.random((8, 2)), 0.1 + 0.1 * rng.random(8), rng.standard_normal(8))
+        kc = np.exp(rng.uniform(np.log(1e-2), np.log(1e2), 2 * n * n))
+        probs.append(H.Problem(n=n, p=p, f=f, kappa_cell=kc, jitter=0.2, seed=100 + k))
+    ctx = H.default_context()
+    for prec, tol, rtol in ((H.PREC_FP64, 1e-12, 1e-10), (H.PREC_MIXED, 1e-10, 1e-8)):
+        B = H.Batch(ctx, probs, precision=prec)
+        stats = B.solve(tol=tol)
+        assert all(s.converged for s in stats)
+        sols = B.solutions()
+        for pr, (uh, q, u) in zip(probs, sols):
+            om = oracle.rectangle_mesh(pr.n, pr.n)
+            hm = H.batch.host_mesh(pr)
+            om.set_xy(hm._topology()[0])
+            r = oracle.solve_poisson(om, pr.p, qd=pr.qd(), f=pr.f.as_oracle(), kappa_cell=pr.kappa_cell)
+            assert rel(uh, r["uhat"]) < rtol, (pr.n, pr.p, prec)
+            assert rel(u, r["u"]) < rtol * 10
+
+
+def test_serving_same_alone_and_in_mix(H):
+    """Continuous batching: every request's result is the same when served alone and when served
+    in a mix of requests of several sizes and degrees (resident and new meshes), within 1e-8."""
+    rng = np.random.default_rng(11)
+    ctx = H.default_context()
+    specs = []
+    for k, (n, p) in enumerate([(6, 1), (9, 2), (4, 3), (5, 4), (8, 2), (3, 1), (7, 3), (6, 2)]):
+        f = H.Field.bumps(rng.random((8, 2)), 0.05 + 0.1 * rng.random(8), 10 * rng.standard_normal(8))
+        kc = np.exp(rng.uniform(np.log(1e-2), np.log(1e2), 2 * n * n))
+        specs.append((H.Problem(n=n, p=p, f=f, kappa_cell=kc, jitter=0.2, seed=500 + k)))
+
+    def serve(subset, resident):
+        eng = H.Engine(ctx, hbm_budget_gb=8, max_batch=8, max_flights=4, tol=1e-11)
+        mids = {}
+        if resident:
+            for i in subset[::2]:
+                mids[i] = eng.add_resident(H.batch.host_mesh(specs[i]), specs[i].p)
+        rid = {}
+        for i in subset:
+            pr = specs[i]
+            if i in mids:
+                rid[i] = eng.submit(pr.p, pr.f, pr.kappa_cell, mesh_id=mids[i])
+            else:
+                rid[i] = eng.submit(pr.p, pr.f, pr.kappa_cell, mesh=H.batch.host_mesh(pr))
+        done = eng.run_until_idle()
+        assert len(done) == len(subset) and all(d["converged"] for d in done)
+        return {i: eng.result(rid[i]) for i in subset}
+
+    mix = serve(list(range(len(specs))), resident=True)
+    for i in range(len(specs)):
+        alone = serve([i], resident=False)[i]
+        for a, b in zip(mix[i], alone):
+            assert rel(a, b) < 1e-8, i

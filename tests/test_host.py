@@ -104,3 +104,24 @@ def test_fields_host_eval(H, oracle):
               H.Field.fourier(0.1, [[1, 2, 0.3, 0.5], [0, 3, 1.0, -0.2]], exponential=True)):
         for x, y in ((0.1, 0.2), (0.5, 0.9)):
             assert f(x, y) == pytest.approx(oracle.eval_field(f.as_oracle(), x, y), rel=1e-14)
+
+
+def test_mesh_concat_offsets(H, oracle):
+    """A batch mesh is the disjoint union of its problems' meshes, each with its own numbering."""
+    parts = [H.rectangle_mesh(H.TriangleCell, (n, n), ctx=None) for n in (2, 3, 5)]
+    u = H.concat_meshes(None, parts)
+    node0, cell0, face0 = H.problem_offsets(u)
+    assert node0.tolist() == [0, 9, 25, 61] and cell0.tolist() == [0, 8, 26, 76]
+    xy, cn, cf, fc = u._topology()
+    for k, n in enumerate((2, 3, 5)):
+        r = oracle.rectangle_mesh(n, n)
+        np.testing.assert_array_equal(cn[cell0[k]:cell0[k + 1]] - node0[k], r.cells)
+        np.testing.assert_array_equal(cf[cell0[k]:cell0[k + 1]] - face0[k], r.cell_faces)
+        f = fc[face0[k]:face0[k + 1]].copy()
+        f[:, :2] -= node0[k]
+        f[:, 2] -= cell0[k]
+        f[:, 3] = np.where(f[:, 3] > 0, f[:, 3] - cell0[k], 0)
+        np.testing.assert_array_equal(f, r.faces)
+    b = sorted(H.getfaceset(u, "boundary"))
+    ref = sorted(int(v) + int(face0[k]) for k, n in enumerate((2, 3, 5)) for v in oracle.rectangle_mesh(n, n).faceset("boundary"))
+    assert b == ref
