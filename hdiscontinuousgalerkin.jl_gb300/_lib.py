@@ -89,6 +89,8 @@ SIGNATURES = {
     "hdg_recover": ([vp, dp, dp, dp], ip),
     "hdg_errornorm_l2sq": ([vp, C.POINTER(hdg_field), dp], ip),
     "hdg_system_destroy": ([vp], ip),
+    "hdg_errornorm_l2sq_noalloc": ([ip, vp, ip, ip, ip, vp, vp, vp, C.POINTER(hdg_field), dp], ip),
+    "hdg_noalloc_last_error": ([], C.c_char_p),
     "hdg_solve_poisson": ([vp, C.c_double, C.POINTER(hdg_field), C.POINTER(hdg_field), dp, C.c_char_p,
                            C.POINTER(hdg_field), C.POINTER(hdg_solver), dp, dp, dp, C.POINTER(hdg_stats)], ip),
     "hdg_mesh_concat": ([vp, ip, C.POINTER(vp), C.POINTER(vp)], ip),

@@ -180,6 +180,20 @@ int hdg_recover(hdg_system* sys, double* q, double* u, double* uhat_cell);
 int hdg_errornorm_l2sq(hdg_system* sys, const hdg_field* u_exact, double* out);
 int hdg_system_destroy(hdg_system* sys);
 
+/* No counterpart in the reference.  The squared L2 error of hdg_errornorm_l2sq for callers that
+ * cannot allocate device memory: a runtime that owns the whole device heap, or code inside a
+ * region where allocation is forbidden.  All inputs are caller-owned DEVICE arrays: xy
+ * (nnodes x 2), cells (ncells x 3, 0-based), u (ncells x nw, the recovered Dubiner coefficients).
+ * The result goes to the host double *out.  The scratch is one fixed 32.8 KB device array per
+ * device (at most 2048 doubles of tables, enough for p <= 4, and 1024 field parameters; larger
+ * requests return HDG_ERR_CAPACITY).  The call allocates nothing.  Calls that overlap on one
+ * device race on that array, so the caller serialises them.  The first call on a device looks
+ * up the array's address and must come before any stream capture.  Errors go to
+ * hdg_noalloc_last_error(). */
+int hdg_errornorm_l2sq_noalloc(int device, void* stream, int p, int quad_degree, int ncells, const double* xy,
+                               const int32_t* cells, const double* u, const hdg_field* u_exact, double* out);
+const char* hdg_noalloc_last_error(void);
+
 typedef struct {
   double element_ms;   /* element assemble+condense kernel of the last (re)assembly */
   double gather_ms;    /* matrix + rhs gather of the last (re)assembly */
