@@ -15,7 +15,9 @@ from .fields import MANUFACTURED_F, MANUFACTURED_U, Field
 from .mesh import (Cell, PolygonalMesh, TriangleCell, cell_diameter, face_orientation, get_coordinates,
                    get_vertices_matrix, getcells_matrix, getfaceset, getncells, getnfaces, getnnodes,
                    n_faces_per_cell, parse_mesh_triangle, rectangle_mesh)
-from .spaces import (Dubiner, GenericFiniteElement, Legendre, RefTetrahedron, ScalarFunctionSpace,
+from .dofhandler import (AssemblerSparsityPattern, DofHandler, celldofs_, create_sparsity_pattern,
+                         create_symmetric_sparsity_pattern, dof_range, ndofs, ndofs_per_cell, nvariables)
+from .spaces import (ContinuousLagrange, Dubiner, GenericFiniteElement, Legendre, RefTetrahedron, ScalarFunctionSpace,
                      ScalarTraceFunctionSpace, VectorFunctionSpace, get_normal, getdetJdV, getfacedetJdS,
                      getnbasefunctions, getnfacequadpoints, getnlocaldofs, getnquadpoints, reinit_, shape_divergence,
                      shape_gradient, shape_value)

@@ -42,7 +42,8 @@ class hdg_solver(C.Structure):
 class hdg_timings(C.Structure):
     _fields_ = [("element_ms", C.c_double), ("gather_ms", C.c_double), ("apply_ms", C.c_double),
                 ("cg_ms", C.c_double), ("cg_a_ms", C.c_double), ("cg_b_ms", C.c_double), ("cg_samples", C.c_int),
-                ("cg_iterations", C.c_int), ("recover_ms", C.c_double)]
+                ("cg_iterations", C.c_int), ("recover_ms", C.c_double), ("cg_a_bytes", C.c_double),
+                ("cg_b_bytes", C.c_double)]
 
 
 class hdg_stats(C.Structure):
@@ -80,6 +81,7 @@ SIGNATURES = {
     "hdg_space_destroy": ([vp], ip),
     "hdg_assemble_condense": ([vp, C.c_double, C.POINTER(hdg_field), C.POINTER(hdg_field), dp, ip, C.POINTER(vp)], ip),
     "hdg_system_reassemble": ([vp, C.c_double, C.POINTER(hdg_field), C.POINTER(hdg_field), dp], ip),
+    "hdg_system_reassemble_resident": ([vp], ip),
     "hdg_system_sizes": ([vp, intp, i64p, intp, intp], ip),
     "hdg_system_get_csc": ([vp, ip, i64p, i64p, dp, dp], ip),
     "hdg_system_get_element_blocks": ([vp, dp, dp, dp, dp], ip),
@@ -107,6 +109,15 @@ SIGNATURES = {
     "hdg_engine_result": ([vp, C.c_int64, dp, dp, dp, intp, intp, intp], ip),
     "hdg_engine_set_keep_results": ([vp, ip], ip),
     "hdg_engine_destroy": ([vp], ip),
+    "hdg_dofhandler_create": ([vp, ip, intp, intp, intp, intp, C.POINTER(vp)], ip),
+    "hdg_dofhandler_sizes": ([vp, intp, i64p], ip),
+    "hdg_dofhandler_cell_dofs": ([vp, i32p, i32p], ip),
+    "hdg_dofhandler_field_range": ([vp, ip, intp, intp], ip),
+    "hdg_dofhandler_sparsity": ([vp, ip, ip, i64p, i64p, i64p], ip),
+    "hdg_dofhandler_dirichlet": ([vp, C.c_char_p, ip, i32p, i32p, i32p, intp], ip),
+    "hdg_dofhandler_destroy": ([vp], ip),
+    "hdg_dofhandler_last_error": ([], C.c_char_p),
+    "hdg_csc_assemble": ([C.c_int64, i64p, i64p, ip, dp, dp, ip, ip, ip, i64p, dp, dp], ip),
     "hdg_assembler_create": ([C.c_int64, C.POINTER(vp)], ip),
     "hdg_assembler_add": ([vp, ip, i64p, dp], ip),
     "hdg_assembler_finish": ([vp, i64p, i64p, i64p], ip),

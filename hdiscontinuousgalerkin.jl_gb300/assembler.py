@@ -39,12 +39,22 @@ class SparseMatrixCSC:
         return sp.csc_matrix((self.nzval, self.rowval - 1, self.colptr - 1), shape=self.shape)
 
 
-def start_assemble(N: int = 0) -> Assembler:
-    return Assembler(N)
+def start_assemble(N=0, f=None, symmetric: bool = False):
+    """start_assemble(N) -> triplet Assembler (src/assembler.jl:23-29), or start_assemble(K, f)
+    on a stored sparsity pattern K (scipy CSC from create_sparsity_pattern) -> an in-place
+    assembler (src/assembler.jl:72-86)."""
+    if hasattr(N, "indptr"):
+        from .dofhandler import start_assemble as _pattern
+        return _pattern(N, f, symmetric)
+    return Assembler(int(N))
 
 
-def assemble_(a, edof, Ke):
-    """assemble!(a, edof, Ke) for an Assembler, or assemble!(g, edof, ge) for a vector g."""
+def assemble_(a, edof, Ke, fe=None):
+    """assemble!(a, edof, Ke) for an Assembler, assemble!(A, dofs, Ke[, fe]) for a pattern
+    assembler, or assemble!(g, edof, ge) for a vector g."""
+    from .dofhandler import AssemblerSparsityPattern, assemble_ as _pattern_assemble
+    if isinstance(a, AssemblerSparsityPattern):
+        return _pattern_assemble(a, edof, Ke, fe)
     edof = np.ascontiguousarray(edof, dtype=np.int64)
     if isinstance(a, Assembler):
         K = np.asfortranarray(Ke, dtype=np.float64)

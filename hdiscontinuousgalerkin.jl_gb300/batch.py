@@ -104,7 +104,12 @@ class Bin:
         L.check(L.load().hdg_dirichlet(self.sp.h, b"boundary", C.byref(g), L.i32ptr(self.dofs), L.dptr(self.vals),
                                        C.byref(n)), self.ctx.handle)
 
-    def reassemble(self):
+    def reassemble(self, resident=False):
+        """Element blocks and trace system again; with resident=True from the coefficients already
+        on the device (no upload), else from the problems' host arrays."""
+        if resident:
+            L.check(L.load().hdg_system_reassemble_resident(self.h), self.ctx.handle)
+            return
         L.check(L.load().hdg_system_reassemble_batch(self.h, L.dptr(self.taus), self.farr, None, L.dptr(self.kc)),
                 self.ctx.handle)
 
@@ -114,6 +119,12 @@ class Bin:
 
     def recover(self):
         L.check(L.load().hdg_recover(self.h, None, None, None), self.ctx.handle)
+
+    def timings(self) -> dict:
+        """Per-phase device times of this bin's system recorded while profiling was on (ms)."""
+        t = L.hdg_timings()
+        L.check(L.load().hdg_system_timings(self.h, C.byref(t)), self.ctx.handle)
+        return {k: getattr(t, k) for k, _ in L.hdg_timings._fields_}
 
     def solution(self):
         """Per problem (uhat, q, u) on the host."""
@@ -149,10 +160,12 @@ class Batch:
         self.stats = None
 
     def solve(self, tol=1e-10, maxit=100000, chunk=32, reassemble=True):
-        """assemble + condense (all bins), apply!, interleaved CG over the bins, recovery."""
+        """assemble + condense (all bins), apply!, interleaved CG over the bins, recovery.
+        reassemble: True (upload the coefficients and assemble), "resident" (assemble from the
+        coefficients already on the device) or False (keep the assembled systems)."""
         for b in self.bins:
             if reassemble:
-                b.reassemble()
+                b.reassemble(resident=(reassemble == "resident"))
             b.apply()
         prec = self.bins[0].precision
         o = L.hdg_solver(float(tol), int(maxit), int(prec), int(chunk), 1e-5)

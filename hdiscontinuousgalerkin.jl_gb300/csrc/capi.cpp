@@ -473,6 +473,15 @@ int hdg_system_reassemble(hdg_system* s, double tau, const hdg_field* f, const h
   });
 }
 
+int hdg_system_reassemble_resident(hdg_system* s) {
+  if (!s) return HDG_ERR_ARG;
+  return guard(s->ctx, [&]() -> int {
+    set_device(s->ctx);
+    assemble_now(s);
+    return HDG_OK;
+  });
+}
+
 int hdg_system_sizes(const hdg_system* s, int* ndofs, int64_t* nnz, int* n, int* m) {
   if (!s) return HDG_ERR_ARG;
   if (ndofs) *ndofs = s->ndofs;
@@ -718,6 +727,8 @@ int hdg_system_timings(hdg_system* s, hdg_timings* out) {
     if (out->cg_samples) {
       out->cg_a_ms = ta / out->cg_samples;
       out->cg_b_ms = tb / out->cg_samples;
+      out->cg_a_bytes = s->prof_a_bytes / out->cg_samples;
+      out->cg_b_bytes = s->prof_b_bytes / out->cg_samples;
     }
     out->cg_iterations = s->cg_iterations;
     return HDG_OK;

@@ -47,7 +47,7 @@ struct CgState {
   int chunk64 = 0, chunk32 = 0;
   int32_t* h_st = nullptr;  // pinned mirrors
   double* h_sc = nullptr;
-  std::vector<double> rr_ref, rr_best;
+  std::vector<double> rr_best;
   std::vector<int> stagnant, outer;
   ~CgState() {
     if (graph64) cudaGraphExecDestroy(graph64);
@@ -97,7 +97,6 @@ __device__ __forceinline__ double row_dot(const int32_t* __restrict__ bcol5, int
 }
 
 template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_init(CgArgs<T> a) {
-  __shared__ double sh[32];
   const int P = a.g.seg_prob[blockIdx.x];
   double rz = 0.0, bb = 0.0;
   for (int row = a.g.seg_row0[blockIdx.x] + threadIdx.x; row < a.g.seg_row1[blockIdx.x]; row += CG_BLOCK) {
@@ -114,7 +113,7 @@ template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_i
     bb += bv * bv;
   }
   double s0, s1;
-  if (seg_finish<CG_BLOCK>(a.g, P, 0, rz, bb, sh, &s0, &s1) && threadIdx.x == 0) {
+  if (seg_finish<CG_BLOCK>(a.g, P, 0, rz, bb, &s0, &s1) && threadIdx.x == 0) {
     double* sc = a.sc + SC * P;
     sc[0] = s0;
     sc[1] = s0;
@@ -130,10 +129,12 @@ template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_i
 
 // FP64 product kernel with the q recurrence (p, q in place)
 template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_a(CgArgs<T> a) {
-  __shared__ double sh[32];
   const int P = a.g.seg_prob[blockIdx.x];
-  if (a.st[ST * P] != 0) return;
-  const double beta = a.sc[SC * P + 7];  // formed once by the reducing block of the update kernel
+  // status and beta are loaded together (one round trip); beta is formed once by the reducing
+  // block of the update kernel
+  const int status = a.st[ST * P];
+  const double beta = a.sc[SC * P + 7];
+  if (status != 0) return;
   const T bt = (T)beta;
   double pq = 0.0;
   const int r0 = a.g.seg_row0[blockIdx.x], r1 = a.g.seg_row1[blockIdx.x];
@@ -165,24 +166,27 @@ template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_a
       }
     }
   }
-  double s0, s1;
-  if (seg_finish<CG_BLOCK>(a.g, P, 0, pq, 0.0, sh, &s0, &s1) && threadIdx.x == 0) {
+  double s0;
+  if (seg_finish1<CG_BLOCK>(a.g, P, 0, pq, &s0) && threadIdx.x == 0) {
+    // alpha = rz / p.q; no step along a direction with p.q <= 0 (the update kernel then stops the
+    // problem, and the host restarts it or reports the breakdown)
     a.sc[SC * P + 2] = s0;
-    a.sc[SC * P + 6] = a.sc[SC * P] / s0;  // alpha = rz / p.q
+    a.sc[SC * P + 6] = (s0 > 0.0) ? a.sc[SC * P] / s0 : 0.0;
   }
 }
 
 // Low-precision product kernel: p_new = z + beta p_old formed on the fly for every column the row
-// touches, q = A p_new a fresh product; p_old / p_new alternate buffers (flip).
+// touches, q = A p_new a fresh product; p_old / p_new alternate buffers (flip).  p.q is summed
+// in float-float arithmetic (FP32 pipe); only each thread's total is converted to FP64.
 template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_a_fresh(CgArgs<T> a, int flip) {
-  __shared__ double sh[32];
   const int P = a.g.seg_prob[blockIdx.x];
-  if (a.st[ST * P] != 0) return;
+  const int status = a.st[ST * P];
   const T bt = (T)a.sc[SC * P + 7];
+  if (status != 0) return;
   const T* __restrict__ pin = flip ? a.p2 : a.p;
   T* __restrict__ pout = flip ? a.p : a.p2;
   const int64_t ndofs = (int64_t)a.nf * NT;
-  double pq = 0.0;
+  FF pq;
   for (int row = a.g.seg_row0[blockIdx.x] + threadIdx.x; row < a.g.seg_row1[blockIdx.x]; row += CG_BLOCK) {
     const int f = row / NT;
     T acc = T(0);
@@ -198,23 +202,25 @@ template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_a
     const T pn = a.z[row] + bt * pin[row];
     pout[row] = pn;
     a.q[row] = acc;
-    pq += (double)pn * (double)acc;
+    pq.add_prod((float)pn, (float)acc);
   }
-  double s0, s1;
-  if (seg_finish<CG_BLOCK>(a.g, P, 0, pq, 0.0, sh, &s0, &s1) && threadIdx.x == 0) {
+  double s0;
+  if (seg_finish1<CG_BLOCK>(a.g, P, 0, pq, &s0) && threadIdx.x == 0) {
     a.sc[SC * P + 2] = s0;
-    a.sc[SC * P + 6] = a.sc[SC * P] / s0;
+    a.sc[SC * P + 6] = (s0 > 0.0) ? a.sc[SC * P] / s0 : 0.0;
   }
 }
 
+// Update kernel.  In FP64 the dot products are FP64 FMAs; in the FP32 iteration they are summed
+// in float-float arithmetic (FP32 pipe) and only each thread's totals are converted to FP64.
 template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_b(CgArgs<T> a, int flip) {
-  __shared__ double sh[32];
   const int P = a.g.seg_prob[blockIdx.x];
-  if (a.st[ST * P] != 0) return;
+  const int status = a.st[ST * P];
   const double alpha = a.sc[SC * P + 6];
+  if (status != 0) return;
   const T at = (T)alpha;
   const T* __restrict__ pcur = flip ? a.p2 : a.p;  // the direction the product kernel just wrote
-  double rz = 0.0, rr = 0.0;
+  typename DotAcc<T>::type rz, rr;
   const int r0 = a.g.seg_row0[blockIdx.x], r1 = a.g.seg_row1[blockIdx.x];
   // the loads of four rows are issued before any store (stores may alias the loads, so the
   // compiler would not hoist the next row's loads above them by itself)
@@ -239,41 +245,47 @@ template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_b
         const T zn = dv[u] * rn;
         a.r[row] = rn;
         a.z[row] = zn;
-        rz += (double)rn * (double)zn;
-        rr += (double)rn * (double)rn;
+        rz.add_prod(rn, zn);
+        rr.add_prod(rn, rn);
       }
     }
   }
   double s0, s1;
-  if (seg_finish<CG_BLOCK>(a.g, P, 1, rz, rr, sh, &s0, &s1) && threadIdx.x == 0) {
+  if (seg_finish<CG_BLOCK>(a.g, P, 1, rz, rr, &s0, &s1) && threadIdx.x == 0) {
     double* sc = a.sc + SC * P;
     const double pq = sc[2], rr_prev = sc[3];
     sc[1] = sc[0];
     sc[0] = s0;
     sc[3] = s1;
     sc[7] = s0 / sc[1];  // beta for the next product kernel
+    sc[9] = (double)flip;  // 1: the latest direction is in p2 (FP32 iteration stopped mid-chunk)
     const int it = a.st[ST * P + 1] + 1;
     a.st[ST * P + 1] = it;
-    int status = 0;
+    int next = 0;
     if (!(pq > 0.0) || !isfinite(s1)) {
       // p'Ap <= 0 once the residual is at rounding level (tiny problems solved exactly in a few
       // steps) is convergence, not breakdown
-      status = (isfinite(s1) && rr_prev <= fmax(1e-24, 100.0 * sc[5]) * sc[4]) ? 1 : 3;
+      next = (isfinite(s1) && rr_prev <= fmax(1e-24, 100.0 * sc[5]) * sc[4]) ? 1 : 3;
     } else if (s1 <= sc[5] * sc[4]) {
-      status = 1;
+      next = 1;
+    } else if (it >= a.st[ST * P + 2]) {
+      next = 2;
     }
-    else if (it >= a.st[ST * P + 2]) status = 2;
-    a.st[ST * P] = status;
+    a.st[ST * P] = next;
   }
 }
 
 // True residual r = b - K x in FP64 (FP64 matrix) for the problems whose refine flag is set;
-// with `replace` it also replaces the Krylov residual: r = r_true, z = D^-1 r, rz, beta.
+// with `replace` it also replaces the Krylov residual: r = r_true, z = D^-1 r, rz and beta.
+// The search direction is kept (beta = rz_true / rz_old) unless the refine flag is 2 or the
+// true residual norm exceeds twice the recursive one, which then restarts the iteration (beta
+// 0, p = z).  In the FP32 iteration the latest direction is moved into p if it sits in p2, and
+// the next refinement is set to trigger once the recursive residual fell by DELTA.
 template <int NT, typename T>
 __global__ void __launch_bounds__(CG_BLOCK) k_cg_residual(CgArgs<T> a, const double* __restrict__ val64, int replace) {
-  __shared__ double sh[32];
   const int P = a.g.seg_prob[blockIdx.x];
   if (a.st[ST * P + 3] == 0) return;
+  const bool move_p = replace && a.p2 != a.p && a.sc[SC * P + 9] != 0.0;
   double rz = 0.0, rr = 0.0;
   for (int row = a.g.seg_row0[blockIdx.x] + threadIdx.x; row < a.g.seg_row1[blockIdx.x]; row += CG_BLOCK) {
     const double rv = a.b[row] - row_dot<NT>(a.bcol5, a.nf, val64, row, a.x);
@@ -284,16 +296,20 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_residual(CgArgs<T> a, const dou
       a.r[row] = rt;
       a.z[row] = zt;
       rz += (double)rt * (double)zt;
+      if (move_p) a.p[row] = a.p2[row];
     }
   }
   double s0, s1;
-  if (seg_finish<CG_BLOCK>(a.g, P, 2, rz, rr, sh, &s0, &s1) && threadIdx.x == 0) {
+  if (seg_finish<CG_BLOCK>(a.g, P, 2, rz, rr, &s0, &s1) && threadIdx.x == 0) {
     double* sc = a.sc + SC * P;
     sc[8] = s1;
     if (replace) {
+      const bool restart = a.st[ST * P + 1] == 0 || a.st[ST * P + 3] == 2 || s1 > 4.0 * sc[3];
       sc[0] = s0;
       sc[3] = s1;
-      sc[7] = (a.st[ST * P + 1] == 0) ? 0.0 : s0 / sc[1];
+      sc[7] = restart ? 0.0 : s0 / sc[1];
+      sc[9] = 0.0;
+      if (a.p2 != a.p) sc[5] = DELTA * DELTA * s1 / sc[4];
     }
   }
 }
@@ -325,6 +341,9 @@ template <int NT> struct SolverNT : CgSolver {
   // would only return.  The full tables are restored when the solve ends.
   std::vector<int32_t> full_prob, full_r0, full_r1, full_b0, full_nb;
   int nseg_full = 0;
+  // Byte accounting of sampled chunks: iteration counts at the launch of the sampled chunk.
+  std::vector<int32_t> sample_it0;
+  bool sample_pending = false;
 
   explicit SolverNT(hdg_system* s_) {
     s = s_;
@@ -341,7 +360,7 @@ template <int NT> struct SolverNT : CgSolver {
   }
 
   template <typename T> void launch_pair(const CgArgs<T>& a, cudaStream_t stream, int it) {
-    if (sizeof(T) == sizeof(double)) {
+    if constexpr (sizeof(T) == sizeof(double)) {
       k_cg_a<NT, T><<<s->nseg, CG_BLOCK, 0, stream>>>(a);
       k_cg_b<NT, T><<<s->nseg, CG_BLOCK, 0, stream>>>(a, 0);
     } else {
@@ -395,11 +414,13 @@ template <int NT> struct SolverNT : CgSolver {
     for (auto* e : s->ev_cg_b) delete e;
     s->ev_cg_a.clear();
     s->ev_cg_b.clear();
+    s->prof_a_bytes = s->prof_b_bytes = 0.0;
+    sample_pending = false;
     if (s->ctx->profiling) s->ev_cg.start(st);
-    // per-problem tolerance (mixed: recursive convergence only triggers a refinement) and cap
+    // per-problem tolerance (mixed: the recursive residual only triggers a refinement) and cap
     for (int P = 0; P < nprob; ++P) {
       std::memset(c->h_sc + SC * P, 0, sizeof(double) * SC);
-      c->h_sc[SC * P + 5] = mixed ? 0.0 : o.tol * o.tol;
+      c->h_sc[SC * P + 5] = mixed ? DELTA * DELTA : o.tol * o.tol;  // mixed: first refinement trigger
       c->h_st[ST * P + 0] = 0;
       c->h_st[ST * P + 1] = 0;
       c->h_st[ST * P + 2] = o.maxit;
@@ -430,7 +451,6 @@ template <int NT> struct SolverNT : CgSolver {
     }
     HDG_CUDA(cudaGetLastError());
     s->ctx->launches += 2;
-    c->rr_ref.assign(nprob, 0.0);
     c->rr_best.assign(nprob, 0.0);
     c->stagnant.assign(nprob, 0);
     c->outer.assign(nprob, 0);
@@ -438,11 +458,14 @@ template <int NT> struct SolverNT : CgSolver {
 
   template <typename T> void chunk_t(const CgArgs<T>& a, cudaGraphExec_t graph, int rep) {
     if (s->ctx->profiling && rep % SAMPLE_EVERY == SAMPLE_EVERY - 1) {
+      sample_it0.resize(nprob);
+      for (int P = 0; P < nprob; ++P) sample_it0[P] = c->h_st[ST * P + 1];
+      sample_pending = true;
       for (int it = 0; it < chunk; ++it) {
         EventPair* ea = new EventPair();
         EventPair* eb = new EventPair();
         ea->start(st);
-        if (sizeof(T) == sizeof(double)) k_cg_a<NT, T><<<s->nseg, CG_BLOCK, 0, st>>>(a);
+        if constexpr (sizeof(T) == sizeof(double)) k_cg_a<NT, T><<<s->nseg, CG_BLOCK, 0, st>>>(a);
         else k_cg_a_fresh<NT, T><<<s->nseg, CG_BLOCK, 0, st>>>(a, it & 1);
         ea->stop(st);
         eb->start(st);
@@ -512,27 +535,58 @@ template <int NT> struct SolverNT : CgSolver {
     if (active > 0 && s->nseg >= 16 && 2 * active <= s->nseg) set_segments(false);
   }
 
+  // Algorithmic bytes per row of the two iteration kernels: the matrix row (5 blocks of NT values),
+  // the block columns (5 per face), and each vector element read or written once; gathered
+  // neighbour values are counted once, at their own row.
+  double bytes_per_row_a() const { return mixed ? 20.0 * NT + 20.0 / NT + 16.0 : 40.0 * NT + 20.0 / NT + 40.0; }
+  double bytes_per_row_b() const { return mixed ? 40.0 : 64.0; }
+
+  void account_sample() {
+    if (!sample_pending) return;
+    sample_pending = false;
+    double rows_it = 0.0;
+    for (int P = 0; P < nprob; ++P) {
+      const double d = (double)(c->h_st[ST * P + 1] - sample_it0[P]);
+      rows_it += d * (double)(s->h_prob_row0[P + 1] - s->h_prob_row0[P]);
+    }
+    s->prof_a_bytes += rows_it * bytes_per_row_a();
+    s->prof_b_bytes += rows_it * bytes_per_row_b();
+  }
+
   bool process(const hdg_solver& o) override {
+    account_sample();
     bool done = process_impl(o);
     if (!done) maybe_compact();
     return done;
   }
 
+  // Host step between chunks.  A problem stopped by p.q <= 0 (status 3) with a finite residual is
+  // restarted from its true FP64 residual with p = z (refine flag 2), in both precisions.  In the
+  // mixed precision the update kernel also stops a problem once its recursive residual fell by
+  // DELTA since the last refinement (status 1); it is then refined here (flag 1).  Refining that
+  // early keeps the recursive and true residuals close, so the search direction stays valid.
+  // Convergence is declared on the true residual; five refinements in a row that do not reduce
+  // it 4x stop the problem.
   bool process_impl(const hdg_solver& o) {
-    if (!mixed) {
-      for (int P = 0; P < nprob; ++P)
-        if (c->h_st[ST * P] == 0) return false;
-      return true;
-    }
-    // mixed: pick the problems that need a refinement
     bool any = false, running = false;
     for (int P = 0; P < nprob; ++P) {
       int32_t* stp = c->h_st + ST * P;
       const double* scp = c->h_sc + SC * P;
-      if (c->rr_ref[P] == 0.0) c->rr_ref[P] = c->rr_best[P] = scp[4];
+      if (c->rr_best[P] == 0.0) c->rr_best[P] = scp[4];
       stp[3] = 0;
-      if (stp[0] >= 3) continue;  // breakdown or final
-      if (stp[0] != 0 || scp[3] <= DELTA * DELTA * c->rr_ref[P]) {
+      if (stp[0] == 3) {
+        if (std::isfinite(scp[3])) {
+          stp[3] = 2;
+          any = true;
+        }
+        continue;
+      }
+      if (!mixed) {
+        if (stp[0] == 0) running = true;
+        continue;
+      }
+      if (stp[0] >= 4) continue;  // final
+      if (stp[0] != 0) {
         stp[3] = 1;
         any = true;
       } else {
@@ -548,12 +602,14 @@ template <int NT> struct SolverNT : CgSolver {
       const double* scp = c->h_sc + SC * P;
       const double rr = scp[8], bb = scp[4];
       c->outer[P]++;
-      c->rr_ref[P] = rr;
-      if (rr <= tol2 * bb) { stp[0] = 4; continue; }     // converged on the true residual
-      if (stp[0] == 2) { stp[0] = 5; continue; }          // iteration cap reached
+      if (rr <= tol2 * bb) { stp[0] = mixed ? 4 : 1; continue; }  // converged on the true residual
+      if (stp[0] == 2) { stp[0] = mixed ? 5 : 2; continue; }      // iteration cap reached
       c->stagnant[P] = (rr > 0.25 * c->rr_best[P]) ? c->stagnant[P] + 1 : 0;
       c->rr_best[P] = std::min(c->rr_best[P], rr);
-      if (c->stagnant[P] >= 5) { stp[0] = 5; continue; }  // the FP32 operator limits the residual
+      if (c->stagnant[P] >= 5 || !std::isfinite(rr)) {
+        stp[0] = mixed ? 5 : 3;  // the FP32 operator limits the residual / repeated breakdown
+        continue;
+      }
       stp[0] = 0;
       running = true;
     }
@@ -579,7 +635,7 @@ template <int NT> struct SolverNT : CgSolver {
       const int status = c->h_st[ST * P];
       hdg_stats& r = (*out)[P];
       r.iterations = c->h_st[ST * P + 1];
-      r.outer = mixed ? c->outer[P] : 1;
+      r.outer = mixed ? c->outer[P] : 1 + c->outer[P];  // FP64: 1 + restarts
       const double bb = c->h_sc[SC * P + 4];
       r.rel_residual = bb > 0 ? std::sqrt(c->h_sc[SC * P + 8] / bb) : 0.0;
       r.converged = mixed ? (status == 4) : (status == 1);

@@ -250,6 +250,8 @@ struct hdg_system {
   // profiling
   EventPair ev_element, ev_gather, ev_apply, ev_cg, ev_recover;
   std::vector<EventPair*> ev_cg_a, ev_cg_b;
+  // algorithmic bytes moved by the sampled CG launches (rows of the problems that iterated)
+  double prof_a_bytes = 0.0, prof_b_bytes = 0.0;
   int cg_iterations = 0;
   double mdiag = 0.0;
   // solution and recovery

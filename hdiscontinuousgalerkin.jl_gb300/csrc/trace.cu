@@ -158,7 +158,6 @@ __global__ void k_gather_rhs(const int nf, const int32_t* __restrict__ fcell, co
 template <int NT>
 __global__ void k_meandiag(SegArgs g, const int32_t* __restrict__ prob_row0, const int nf,
                            const int8_t* __restrict__ kdiag, const double* __restrict__ val, double* __restrict__ mdiag) {
-  __shared__ double sh[32];
   const int P = g.seg_prob[blockIdx.x];
   const int ndofs = nf * NT;
   double acc = 0.0;
@@ -166,8 +165,8 @@ __global__ void k_meandiag(SegArgs g, const int32_t* __restrict__ prob_row0, con
     const int f = r / NT, i = r - f * NT;
     acc += fabs(val[(int64_t)(kdiag[f] * NT + i) * ndofs + r]);
   }
-  double s0, s1;
-  if (seg_finish<256>(g, P, 3, acc, 0.0, sh, &s0, &s1) && threadIdx.x == 0)
+  double s0;
+  if (seg_finish1<256>(g, P, 3, acc, &s0) && threadIdx.x == 0)
     mdiag[P] = s0 / (double)(prob_row0[P + 1] - prob_row0[P]);
 }
 

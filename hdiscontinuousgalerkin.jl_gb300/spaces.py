@@ -53,6 +53,43 @@ class GenericFiniteElement:
         return self.basis.getnbasefunctions()
 
 
+class ContinuousLagrange:
+    """ContinuousLagrange{dim,RefTetrahedron,order}: nodal P_order element with P1 geometry
+    (src/LagrangeFE.jl:5-61).  Nodes are ordered as get_nodal_points of src/shapes.jl:46-77:
+    the three vertices, then the order-1 interior points of each reference edge (1,0)->(0,1),
+    (0,1)->(0,0), (0,0)->(1,0), then the interior points.  topology[k] counts the dofs on
+    entities of dimension k."""
+
+    EDGES = (((1.0, 0.0), (0.0, 1.0)), ((0.0, 1.0), (0.0, 0.0)), ((0.0, 0.0), (1.0, 0.0)))
+
+    def __init__(self, dim: int = 2, shape=RefTetrahedron, order: int = 1):
+        if dim != 2 or order < 1:
+            raise ValueError("ContinuousLagrange is implemented for triangles (dim 2), order >= 1")
+        self.dim, self.shape, self.order = dim, shape, int(order)
+        k = self.order
+        self.topology = {0: 3, 1: 3 * (k - 1), 2: (k - 1) * (k - 2) // 2}
+
+    def getnbasefunctions(self):
+        return (self.order + 1) * (self.order + 2) // 2
+
+    def nodal_points(self):
+        k = self.order
+        pts = [(0.0, 0.0), (1.0, 0.0), (0.0, 1.0)]
+        for a, b in self.EDGES:
+            for i in range(1, k):
+                pts.append((a[0] + i * (b[0] - a[0]) / k, a[1] + i * (b[1] - a[1]) / k))
+        for i in range(1, k):            # interior grid, src/shapes.jl:_interior_points (m = 2):
+            for j in range(1, k - i):    # v1 + i (v3 - v1)/k + j (v2 - v1)/k
+                pts.append((j / k, i / k))
+        return np.array(pts)
+
+    def spatial_nodal_coordinate(self, i: int, coords):
+        """x of local node i (1-based) on a cell with vertex coordinates coords (3 x 2), P1 map."""
+        xi, eta = self.nodal_points()[i - 1]
+        c = np.asarray(coords, dtype=float)
+        return (1.0 - xi - eta) * c[0] + xi * c[1] + eta * c[2]
+
+
 _space_cache = {}
 
 
@@ -119,14 +156,16 @@ class ScalarFunctionSpace:
         self.mesh, self.fe = mesh, fe
         self.order = fe.order
         self.quad_degree = quad_degree if quad_degree is not None else fe.order + 1
-        self.sp = _handle(mesh, self.order, self.quad_degree)
+        # nodal (continuous Lagrange) spaces only carry dofs for a DofHandler; the HDG tables
+        # live in the device space handle of the modal (Dubiner) spaces
+        self.sp = None if isinstance(fe, ContinuousLagrange) else _handle(mesh, self.order, self.quad_degree)
         self.state = _CellState()
 
     def getnbasefunctions(self):
-        return self.sp.nw
+        return self.fe.getnbasefunctions() if self.sp is None else self.sp.nw
 
     def getnlocaldofs(self):
-        return self.sp.nw
+        return self.getnbasefunctions()
 
     def getnquadpoints(self):
         return self.sp.nq

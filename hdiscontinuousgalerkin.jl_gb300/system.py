@@ -78,7 +78,12 @@ class TraceSystem:
         except Exception:
             pass
 
-    def reassemble(self, tau=1.0, f=None, kappa=None, kappa_cell=None):
+    def reassemble(self, tau=1.0, f=None, kappa=None, kappa_cell=None, resident=False):
+        """Assemble and condense again with new coefficients; resident=True reuses the ones already
+        on the device (no host transfer)."""
+        if resident:
+            L.check(L.load().hdg_system_reassemble_resident(self._h), self.ctx)
+            return
         fc, kc, kcell = self._coef(f, kappa, kappa_cell)
         L.check(L.load().hdg_system_reassemble(self._h, float(tau), fc, kc, kcell), self.ctx)
 
@@ -176,9 +181,15 @@ def doassemble(Vh: VectorFunctionSpace, Wh: ScalarFunctionSpace, Mh: ScalarTrace
 
 
 class Dirichlet:
-    """Dirichlet(û_h, mesh, faceset, g) on the trace space (src/boundary.jl:212-247)."""
+    """Dirichlet(û_h, mesh, faceset, g) on the trace space (src/boundary.jl:212-247), or
+    Dirichlet(u, dh, faceset, g) on a nodal field of a DofHandler (src/boundary.jl:44-95)."""
 
     def __init__(self, u, mesh, faceset: str, g=None):
+        from .dofhandler import DofHandler, DirichletDH
+        if isinstance(mesh, DofHandler):
+            d = DirichletDH(u, mesh, faceset, g if g is not None else (lambda x: 0.0))
+            self.prescribed_dofs, self.values = d.prescribed_dofs, d.values
+            return
         fs = u.fs if isinstance(u, TrialFunction) else u
         if not isinstance(fs, ScalarTraceFunctionSpace):
             raise NotImplementedError("the HDG path prescribes trace dofs (ScalarTraceFunctionSpace)")

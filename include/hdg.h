@@ -56,8 +56,10 @@ typedef struct {
 /* Arithmetic of the element kernels and of the trace solve. */
 enum {
   HDG_PREC_FP64 = 0,  /* FP64 throughout (the plain path) */
-  HDG_PREC_MIXED = 1  /* FP32 quadrature/condensation + one FP64 refinement step per local solve;
-                         FP32 inner CG inside an FP64 iterative-refinement loop */
+  HDG_PREC_MIXED = 1  /* trace solve: FP32 matrix and Krylov vectors with FP64 x, dot products and
+                         scalars; FP64 true-residual refinement ("reliable updates") decides
+                         convergence.  Element condensation stays FP64 (local condition numbers
+                         reach 3e5, beyond what FP32 plus one refinement step recovers). */
 };
 
 typedef struct hdg_ctx hdg_ctx;
@@ -133,6 +135,9 @@ int hdg_assemble_condense(hdg_space* space, double tau, const hdg_field* f, cons
  * topology buffer (no reallocation). */
 int hdg_system_reassemble(hdg_system* sys, double tau, const hdg_field* f, const hdg_field* kappa,
                           const double* kappa_cell);
+/* Recompute the element blocks and the trace system with the coefficients already on the device
+ * (those of the last assemble or reassemble call): no host transfer.  No reference counterpart. */
+int hdg_system_reassemble_resident(hdg_system* sys);
 /* Trace dofs, stored entries of K, local system size n = 3 nw, trace dofs per cell m = 3 nt. */
 int hdg_system_sizes(const hdg_system* sys, int* ndofs, int64_t* nnz, int* n, int* m);
 /* K and b as the reference holds them (sign included) in CSC; base 0 or 1 (Julia). */
@@ -204,6 +209,8 @@ typedef struct {
   int cg_samples;      /* number of sampled iterations */
   int cg_iterations;   /* iterations of the last solve */
   double recover_ms;   /* last recovery */
+  double cg_a_bytes;   /* mean algorithmic bytes of a sampled product-kernel launch (rows that iterated) */
+  double cg_b_bytes;   /* mean algorithmic bytes of a sampled update-kernel launch */
 } hdg_timings;
 /* Per-phase device times recorded while profiling was on (0 where nothing was recorded). */
 int hdg_system_timings(hdg_system* sys, hdg_timings* out);
@@ -270,6 +277,39 @@ int hdg_assembler_add(hdg_assembler* a, int ndofs, const int64_t* edof, const do
 int hdg_assembler_finish(hdg_assembler* a, int64_t* nrows, int64_t* ncols, int64_t* nnz);
 int hdg_assembler_get_csc(const hdg_assembler* a, int base, int64_t* colptr, int64_t* rowval, double* nzval);
 int hdg_assembler_destroy(hdg_assembler* a);
+
+/* ---- DofHandler and the sparsity-pattern assembler (host) ------------------------------ */
+/* DofHandler(fields, mesh), src/dofhandler.jl:13-16 and _distribute_dofs :91-151, for nodal
+ * fields.  Field i carries vdofs[i] (0 or 1) dofs per vertex, fdofs[i] per face and cdofs[i] per
+ * cell, each times ncomp[i] components (gettopology of its element, src/LagrangeFE.jl:60).
+ * mesh must outlive the handler. */
+typedef struct hdg_dofhandler hdg_dofhandler;
+int hdg_dofhandler_create(const hdg_mesh* mesh, int nfields, const int* vdofs, const int* fdofs, const int* cdofs,
+                          const int* ncomp, hdg_dofhandler** out);
+/* ndofs(dh) and the length of cell_dofs. */
+int hdg_dofhandler_sizes(const hdg_dofhandler* dh, int* ndofs, int64_t* ncelldofs);
+/* dh.cell_dofs (1-based, concatenated per cell) and dh.cell_dofs_offset (ncells + 1, 1-based). */
+int hdg_dofhandler_cell_dofs(const hdg_dofhandler* dh, int32_t* cell_dofs, int32_t* offsets);
+/* dof_range(dh, field): first..last local dof of a field in a cell (1-based), src/dofhandler.jl:77-82. */
+int hdg_dofhandler_field_range(const hdg_dofhandler* dh, int field, int* first, int* last);
+/* create_sparsity_pattern / create_symmetric_sparsity_pattern (upper triangle),
+ * src/dofhandler.jl:171-229: CSC pattern with the diagonal; sizes first (colptr/rowval NULL). */
+int hdg_dofhandler_sparsity(const hdg_dofhandler* dh, int symmetric, int base, int64_t* colptr, int64_t* rowval,
+                            int64_t* nnz);
+/* Dirichlet(u, dh, faceset, f) dof selection, src/boundary.jl:44-95: sorted 1-based dofs of
+ * field `field` (0-based) on the face set, with the cell (1-based) and local node (1-based) that
+ * gives each one's nodal point for evaluating f.  Outputs may be NULL (count only). */
+int hdg_dofhandler_dirichlet(const hdg_dofhandler* dh, const char* faceset, int field, int32_t* dofs, int32_t* cells,
+                             int32_t* local, int* count);
+int hdg_dofhandler_destroy(hdg_dofhandler* dh);
+const char* hdg_dofhandler_last_error(void);
+/* assemble!(A::AssemblerSparsityPattern, dofs, Ke, fe), src/assembler.jl:97-137, for nel
+ * elements at once: K.nzval += Ke at the stored positions of a CSC pattern (colptr/rowval with
+ * base 0 or 1, rows sorted per column), f += fe.  dofs (nel x ndofs_e) are 1-based; Ke is
+ * column-major per element.  upper_only assembles the upper triangle (Symmetric pattern).  A
+ * pair that is not stored is an error ("some row indices were not found"). */
+int hdg_csc_assemble(int64_t n, const int64_t* colptr, const int64_t* rowval, int base, double* nzval, double* f,
+                     int upper_only, int nel, int ndofs_e, const int64_t* dofs, const double* Ke, const double* fe);
 
 #ifdef __cplusplus
 }

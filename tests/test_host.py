@@ -125,3 +125,73 @@ def test_mesh_concat_offsets(H, oracle):
     b = sorted(H.getfaceset(u, "boundary"))
     ref = sorted(int(v) + int(face0[k]) for k, n in enumerate((2, 3, 5)) for v in oracle.rectangle_mesh(n, n).faceset("boundary"))
     assert b == ref
+
+
+# ---- DofHandler (test/test_handlers.jl) and the sparsity-pattern assembler ------------------
+def test_dofhandler_matches_reference_test(H):
+    """The 2x2 P1 numbering, offsets, dof_range and boundary dofs of test/test_handlers.jl:6-18."""
+    mesh = H.rectangle_mesh(H.TriangleCell, (2, 2), (0.0, 0.0), (1.0, 1.0), ctx=None)
+    Wh = H.ScalarFunctionSpace(mesh, H.ContinuousLagrange(2, H.RefTetrahedron, 1), update_face_data=False)
+    u_h = H.TrialFunction(Wh)
+    dh = H.DofHandler([u_h], mesh)
+    assert dh.cell_dofs.tolist() == [1, 2, 3, 2, 4, 3, 2, 5, 4, 5, 6, 4, 3, 4, 7, 4, 8, 7, 4, 6, 8, 6, 9, 8]
+    assert dh.cell_dofs_offset.tolist() == [1, 4, 7, 10, 13, 16, 19, 22, 25]
+    assert list(H.dof_range(dh, u_h)) == [1, 2, 3]
+    dbc = H.Dirichlet(u_h, dh, "boundary", lambda x: 0.0)
+    assert dbc.prescribed_dofs.tolist() == [1, 2, 3, 5, 6, 7, 8, 9]
+    assert np.all(dbc.values == 0.0)
+
+
+def test_dofhandler_p2_and_two_fields(H):
+    """P2 adds one dof per face at its first visit; a second field is numbered after the first
+    within each cell; the sparsity pattern holds every pair of dofs that share a cell."""
+    mesh = H.rectangle_mesh(H.TriangleCell, (3, 2), (0.0, 0.0), (1.0, 1.0), ctx=None)
+    nn, nf = mesh.nnodes, mesh.nfaces
+    u = H.TrialFunction(H.ScalarFunctionSpace(mesh, H.ContinuousLagrange(2, H.RefTetrahedron, 2)))
+    p = H.TrialFunction(H.ScalarFunctionSpace(mesh, H.ContinuousLagrange(2, H.RefTetrahedron, 1)))
+    dh = H.DofHandler([u, p], mesh)
+    assert H.ndofs(dh) == (nn + nf) + nn
+    assert H.ndofs_per_cell(dh) == 9
+    assert list(H.dof_range(dh, u)) == list(range(1, 7)) and list(H.dof_range(dh, p)) == [7, 8, 9]
+    # first cell: vertices 1..3, faces 4..6, then the second field's vertices 7..9
+    assert dh.cell_dofs[:9].tolist() == list(range(1, 10))
+    K = H.create_sparsity_pattern(dh)
+    dense = np.zeros(K.shape, bool)
+    for c in range(mesh.ncells):
+        g = dh.cell_dofs[dh.cell_dofs_offset[c] - 1: dh.cell_dofs_offset[c + 1] - 1] - 1
+        dense[np.ix_(g, g)] = True
+    dense |= np.eye(K.shape[0], dtype=bool)
+    stored = np.zeros(K.shape, bool)
+    for j in range(K.shape[1]):
+        stored[K.indices[K.indptr[j]:K.indptr[j + 1]], j] = True
+    assert np.array_equal(stored, dense) and K.nnz == dense.sum() and not K.data.any()
+    Ks = H.create_symmetric_sparsity_pattern(dh)
+    assert Ks.nnz == np.triu(dense).sum()
+
+
+def test_pattern_assembler_matches_triplets(H):
+    """start_assemble(K, f) + assemble! into a stored pattern equals the triplet assembler's
+    sparse(I, J, V) on the same element matrices (src/assembler.jl:31-60 vs 97-137)."""
+    rng = np.random.default_rng(5)
+    mesh = H.rectangle_mesh(H.TriangleCell, (4, 3), (0.0, 0.0), (2.0, 1.0), ctx=None)
+    u = H.TrialFunction(H.ScalarFunctionSpace(mesh, H.ContinuousLagrange(2, H.RefTetrahedron, 2)))
+    dh = H.DofHandler([u], mesh)
+    K = H.create_sparsity_pattern(dh)
+    f = np.zeros(H.ndofs(dh))
+    A = H.start_assemble(K, f)
+    T = H.start_assemble(H.ndofs(dh))
+    g = np.zeros(H.ndofs(dh))
+    n = H.ndofs_per_cell(dh)
+    dofs = np.zeros(n, np.int64)
+    for c in range(1, mesh.ncells + 1):
+        Ke = rng.standard_normal((n, n))
+        fe = rng.standard_normal(n)
+        H.celldofs_(dofs, dh, c)
+        H.assemble_(A, dofs, Ke, fe)
+        H.assemble_(T, dofs, Ke)
+        H.assemble_(g, dofs, fe)
+    ref = H.end_assemble(T).to_scipy().toarray()
+    assert np.allclose(K.toarray(), ref, rtol=0, atol=1e-13)
+    assert np.allclose(f, g, rtol=0, atol=1e-13)
+    with pytest.raises(H.HDGError):
+        H.assemble_(A, np.array([1, H.ndofs(dh)]), np.ones((2, 2)))
