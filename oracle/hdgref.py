@@ -289,12 +289,14 @@ class System:
         lib().hr_apply(self.h, len(dofs), _ip(dofs), _dp(vals))
 
     def solve(self):
-        """û = K \\ b with SuperLU (examples/poisson2D_HDG.jl:195).  The column ordering is minimum
-        degree on A'+A, the analogue of UMFPACK's symmetric strategy for a matrix with a symmetric
-        pattern (Julia's `\\` on a non-Hermitian SparseMatrixCSC calls UMFPACK)."""
+        """û = K \\ b with SuperLU (examples/poisson2D_HDG.jl:195).  Julia's `\\` on a
+        non-Hermitian SparseMatrixCSC calls UMFPACK, whose symmetric strategy (chosen for a matrix
+        with a symmetric pattern and a zero-free diagonal, as K is) orders A'+A by minimum degree
+        and prefers diagonal pivots with a relative tolerance of 0.001.  SuperLU is set up the
+        same way: minimum degree on A'+A and diag_pivot_thresh = 0.001."""
         import scipy.sparse.linalg as spla
         K, b = self.csc()
-        return spla.splu(K.tocsc(), permc_spec="MMD_AT_PLUS_A").solve(b)
+        return spla.splu(K.tocsc(), permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=0.001).solve(b)
 
     def recover(self, uhat):
         nc = self.mesh.ncells
