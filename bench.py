@@ -1,18 +1,20 @@
 #!/usr/bin/env python
 """Benchmark of the HDG Poisson path on one GB300 (or N replicas, one per GPU).
 
-Default workload (the plain-method scaled case): -Δu = f on the unit square, f = 2π² sin(πx)
-sin(πy), homogeneous Dirichlet, structured right-diagonal mesh 2·256·256 = 131072 triangles,
-p = 2, τ = 1, FP64: element assembly + condensation, trace-matrix gather, apply!, Jacobi-PCG to
-1e-12 relative residual, recovery of u and q.  One step = one complete solve.
+Default workload (c4, the batching configuration the served-vs-plain metric is stated on): 256
+independent Poisson problems, n log-uniform in [8, 128], p uniform in {1..4}, jittered meshes,
+per-cell kappa log-uniform in [1e-2, 1e2], Gaussian-bump sources.  One step solves all 256 as
+degree-binned batches (assemble + condense, apply!, multigrid-preconditioned CG to 1e-9 with an
+FP32 V-cycle, recovery); the plain FP64 path that solves them one at a time with the same
+preconditioner is timed beside it.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload c1|c2] [--precision fp64|mixed] [--no-cpu-baseline]
+                  [--workload c1|c2|c3|c4|c5] [--precision fp64|mixed] [--no-cpu-baseline]
 
 Prints one JSON line (rank 0).  `value` is solves/s with inputs resident on the device; `e2e`
-is the same metric through the public API with host buffers (coordinates and source uploaded,
-û, q, u downloaded every step).  With --impl reference the CPU oracle (a C++ restatement of the
-reference's flow with a sparse direct solve) is timed on the host cores instead.
+is the same metric through the public API with host buffers.  With --impl reference the CPU
+oracle (a C++ restatement of the reference's flow with a sparse direct solve) is timed on the
+host cores instead.
 """
 from __future__ import annotations
 
@@ -106,6 +108,7 @@ def run_c4(args, ws, rank, local):
     ctx.set_stream(stream.cuda_stream)
     probs = c4_problems(H)
     prec = H.PREC_FP64 if args.precision == "fp64" else H.PREC_MIXED
+    pc = H.PRECOND_AMG if args.preconditioner == "amg" else H.PRECOND_JACOBI
     tol = args.tol if args.tol != 1e-12 else 1e-9
     ncells = sum(2 * pr.n * pr.n for pr in probs)
 
@@ -123,12 +126,12 @@ def run_c4(args, ws, rank, local):
         dbc = H.Dirichlet(H.TrialFunction(Mh), dm, "boundary")
         plain.append((dm, K, dbc, pr))
 
-    def plain_step(keep=False, tol_=tol):
+    def plain_step(keep=False, tol_=tol, pc_=None):
         out = []
         for dm, K, dbc, pr in plain:
             K.reassemble(resident=True)
             K.apply_dirichlet(dbc.prescribed_dofs, dbc.values)
-            uh = K.solve(tol=tol_, precision=H.PREC_FP64, to_host=keep)
+            uh = K.solve(tol=tol_, precision=H.PREC_FP64, to_host=keep, preconditioner=pc if pc_ is None else pc_)
             r = K.recover(to_host=keep)
             if keep:
                 out.append((uh, r[0], r[1]))
@@ -136,7 +139,7 @@ def run_c4(args, ws, rank, local):
 
     B = H.Batch(ctx, probs, precision=prec)
     for _ in range(max(args.warmup, 3)):
-        B.solve(tol=tol, reassemble="resident")
+        B.solve(tol=tol, reassemble="resident", preconditioner=pc)
     plain_step()
     torch.cuda.synchronize()
 
@@ -153,7 +156,7 @@ def run_c4(args, ws, rank, local):
     for _ in range(args.steps):
         s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s0.record(stream)
-        B.solve(tol=tol, reassemble="resident")
+        B.solve(tol=tol, reassemble="resident", preconditioner=pc)
         s1.record(stream)
         s1.synchronize()
         steps_ms.append(s0.elapsed_time(s1))
@@ -167,34 +170,35 @@ def run_c4(args, ws, rank, local):
     value = ws * len(probs) / (batch_ms / 1e3)
     iters = [s.iterations for s in B.stats]
 
-    # ---- roofline of the dominant kernel (last timed step, sampled CG launches of every bin) ----
+    # ---- roofline of the dominant phase (last timed step) ----
+    # The degree bins iterate concurrently on their own streams, so the CG kernels of one bin
+    # overlap those of the others and a single launch's duration is not its own.  The CG phase is
+    # therefore measured as a whole: the algorithmic bytes of every iteration launch of every bin
+    # (rows of the problems that iterated x the per-row bytes of the two kernels) over the
+    # phase's wall time (the longest bin, all bins starting together).
     peaks, peak_kind = measured_peaks()
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     tims = [bn.timings() for bn in B.bins]
-    chunk = 32
-    cg_launches = [chunk * math.ceil(t["cg_iterations"] / chunk) for t in tims]
-    tot = {
-        "cg_a": sum(t["cg_a_ms"] * n for t, n in zip(tims, cg_launches)),
-        "cg_b": sum(t["cg_b_ms"] * n for t, n in zip(tims, cg_launches)),
-        "element": sum(t["element_ms"] for t in tims),
-    }
-    dom = max(tot, key=tot.get)
-    names = {"cg_a": ("k_cg_a_fresh" if prec == H.PREC_MIXED else "k_cg_a") + " (all degree bins)",
-             "cg_b": "k_cg_b (all degree bins)", "element": "k_element_condense (all degree bins)"}
-    if dom in ("cg_a", "cg_b"):
-        ms = sum(t[dom + "_ms"] * t["cg_samples"] for t in tims)
-        by = sum(t[dom + "_bytes"] * t["cg_samples"] for t in tims)
-        nsamp = sum(t["cg_samples"] for t in tims)
-        dur, alg = (ms / nsamp, by / nsamp) if nsamp else (0.0, 0.0)
+    cg_ms = max(t["cg_ms"] for t in tims)
+    cg_bytes = sum(t["cg_bytes"] for t in tims)
+    el_ms = sum(t["element_ms"] for t in tims)
+    nw_ = lambda p: (p + 1) * (p + 2) // 2
+    el_bytes = sum(2 * pr.n * pr.n * (12 + 48 + 1 + 8 * ((3 * pr.p + 3) * (3 * pr.p + 4) +
+                                                       3 * nw_(pr.p) * (3 * pr.p + 4))) for pr in probs)
+    if cg_ms >= el_ms:
+        if pc == H.PRECOND_AMG:
+            kname = "k_cg_a"
+            dom = ("CG iteration kernels (k_cg_a + k_cg_b_mg + multigrid V-cycle + k_cg_c) of all degree bins, "
+                   "on concurrent streams")
+        else:
+            kname = "k_cg_a_fresh" if prec == H.PREC_MIXED else "k_cg_a"
+            dom = f"CG iteration kernels ({kname} + k_cg_b) of all degree bins, on concurrent streams"
+        alg, dur = cg_bytes, cg_ms
     else:
-        nw_ = lambda p: (p + 1) * (p + 2) // 2
-        alg = sum(2 * pr.n * pr.n * (12 + 48 + 1 + 8 * ((3 * pr.p + 3) * (3 * pr.p + 4) +
-                                                      3 * nw_(pr.p) * (3 * pr.p + 4))) for pr in probs)
-        dur = tot["element"]
+        kname = "k_element_condense"
+        dom = "k_element_condense (all degree bins)"
+        alg, dur = el_bytes, el_ms
     achieved = alg / (dur / 1e3) / 1e9 if dur > 0 else None
-    kname = "k_cg_a_fresh" if (dom == "cg_a" and prec == H.PREC_MIXED) else ("k_cg_a" if dom == "cg_a" else
-                                                                            "k_cg_b" if dom == "cg_b" else
-                                                                            "k_element_condense")
     traffic = profile_traffic("c4_" + args.precision + ":" + kname)
 
     # ---- plain path, one timed pass over the batch ----
@@ -206,19 +210,19 @@ def run_c4(args, ws, rank, local):
     plain_ms = p0.elapsed_time(p1)
 
     # ---- accuracy against the plain FP64 path at tolerance 1e-12 ----
-    ref = plain_step(keep=True, tol_=1e-12)
+    ref = plain_step(keep=True, tol_=1e-12, pc_=H.PRECOND_JACOBI)
     sols = B.solutions()
     err = max(max(rel_l2(a[0], b[0]), rel_l2(a[1], b[1]), rel_l2(a[2], b[2])) for a, b in zip(sols, ref))
 
     # ---- end to end through the public API with host buffers ----
     def e2e_step():
-        res = B.solve(tol=tol, reassemble=True)   # H2D: kappa per cell, sources, tau, Dirichlet data
+        res = B.solve(tol=tol, reassemble=True, preconditioner=pc)  # H2D: kappa, sources, tau, Dirichlet data
         return res, B.solutions()                 # D2H: uhat, q, u of every problem
     e2e_step()
     torch.cuda.synchronize()
     barrier(ws)
     t0 = time.perf_counter()
-    e2e_n = max(2, args.steps)
+    e2e_n = max(2, args.steps // 3)
     for _ in range(e2e_n):
         e2e_step()
     torch.cuda.synchronize()
@@ -231,7 +235,8 @@ def run_c4(args, ws, rank, local):
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": batch_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64" if prec == H.PREC_MIXED else "f64", "data": "synthetic",
-        "config": {"workload": C4_DESC + f"; degree-binned batch, {args.precision}, CG tol {tol:g}",
+        "config": {"workload": C4_DESC + f"; degree-binned batch, {args.precision}, {args.preconditioner}-preconditioned "
+                               f"CG tol {tol:g}",
                    "problems": len(probs), "cells": ncells, "tol": tol,
                    "quadrature": "Strang(p+1) for p<=2, Strang(6) for p=3, Grundmann-Moeller(9) for p=4",
                    "step": "assemble+condense (coefficients resident) -> apply! -> CG -> recovery of all 256 problems",
@@ -239,16 +244,18 @@ def run_c4(args, ws, rank, local):
                    "parallelism": f"{ws} independent replica(s), one per GPU"},
         "p50_ms": statistics.median(steps_ms), "p99_ms": max(steps_ms),
         "plain_fp64_solves_per_s": len(probs) / (plain_ms / 1e3),
+        "plain_path": f"one problem at a time: reassemble, apply!, FP64 {args.preconditioner}-preconditioned CG, recovery",
         "speedup_vs_plain": (len(probs) / (batch_ms / 1e3)) / (len(probs) / (plain_ms / 1e3)),
         "max_rel_l2_err_vs_fp64": err,
         "converged_fraction": float(np.mean([s.converged for s in B.stats])),
         "max_rel_residual": float(max(s.rel_residual for s in B.stats)),
         "cg_iterations_max": max(iters), "cg_iterations_mean": float(np.mean(iters)),
-        "phase_ms": {"element_ms": tot["element"], "cg_a_ms_total": tot["cg_a"], "cg_b_ms_total": tot["cg_b"]},
+        "phase_ms": {"element_ms_sum_of_bins": el_ms, "cg_ms_longest_bin": cg_ms},
         "gpu_launches": launches,
-        "roofline": {"kernel": names[dom], "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+        "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
-                     "algorithmic_bytes_per_launch": alg, "avg_launch_ms": dur,
+                     "algorithmic_bytes": alg, "duration_ms": dur,
+                     "note": "whole-phase figure: algorithmic bytes of all launches of the phase / its wall time",
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
                      "fallback 6.8 TB/s"},
         "e2e": {"value": ws * len(probs) * e2e_n / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
@@ -525,15 +532,24 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c3", "c4", "c5"])
+    ap.add_argument("--workload", default="c4", choices=sorted(WORKLOADS) + ["c3", "c4", "c5"])
     ap.add_argument("--requests", type=int, default=2000)
     ap.add_argument("--hbm-budget-gb", type=float, default=64.0)
     ap.add_argument("--max-batch", type=int, default=64)
     ap.add_argument("--max-flights", type=int, default=8)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default=None, choices=["fp64", "mixed"],
+                    help="default: mixed for the batched and served workloads (c3, c4, c5), fp64 for c1, c2")
     ap.add_argument("--tol", type=float, default=1e-12)
+    ap.add_argument("--preconditioner", default=None, choices=["jacobi", "amg"],
+                    help="trace CG preconditioner (default: amg for the batch c4, jacobi otherwise); the plain "
+                         "FP64 path of c4 uses the same one")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.precision is None:
+        args.precision = "mixed" if args.workload in ("c3", "c4", "c5") else "fp64"
+    if args.preconditioner is None:
+        args.preconditioner = "amg" if args.workload == "c4" else "jacobi"
+    return args
 
 
 # ---------------------------------------------------------------- distributed helpers
@@ -716,6 +732,7 @@ def run_ours(args, ws, rank, local):
     H = g.import_package()
     w = WORKLOADS[args.workload]
     prec = H.PREC_FP64 if args.precision == "fp64" else H.PREC_MIXED
+    pc = H.PRECOND_AMG if args.preconditioner == "amg" else H.PRECOND_JACOBI
     torch.cuda.set_device(local)
     ctx = H.Context(local)
     stream = torch.cuda.current_stream()
@@ -735,7 +752,7 @@ def run_ours(args, ws, rank, local):
     def step():
         K.reassemble(1.0, f)
         K.apply_dirichlet(dbc.prescribed_dofs, dbc.values)
-        K.solve(tol=args.tol, precision=prec, to_host=False)
+        K.solve(tol=args.tol, precision=prec, to_host=False, preconditioner=pc)
         K.recover(to_host=False)
 
     for _ in range(max(args.warmup, 3)):
@@ -807,7 +824,7 @@ def run_ours(args, ws, rank, local):
         mesh.set_coordinates(xy_pinned)                       # H2D: node coordinates
         K.reassemble(1.0, f)                                  # H2D: source parameters
         K.apply_dirichlet(dbc.prescribed_dofs, dbc.values)    # H2D: prescribed dofs and values
-        uh = K.solve(tol=args.tol, precision=prec, to_host=True)   # D2H: û
+        uh = K.solve(tol=args.tol, precision=prec, to_host=True, preconditioner=pc)   # D2H: û
         return uh, K.recover(to_host=True)                    # D2H: q, u, û per cell
 
     for _ in range(2):

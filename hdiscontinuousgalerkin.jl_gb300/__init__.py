@@ -6,7 +6,7 @@ ScalarFunctionSpace, VectorFunctionSpace, ScalarTraceFunctionSpace, TrialFunctio
 CellIterator, start_assemble / assemble_ / end_assemble, doassemble, apply_, solve,
 get_usigma_, errornorm.  Everything numerical runs in libhdg.so (CUDA, built in-tree)."""
 from . import _lib
-from ._lib import HDGError, PREC_FP64, PREC_MIXED
+from ._lib import HDGError, PREC_FP64, PREC_MIXED, PRECOND_AMG, PRECOND_JACOBI
 from .batch import Batch, Problem, concat_meshes, problem_offsets
 from .serve import Engine
 from .assembler import Assembler, SparseMatrixCSC, assemble_, end_assemble, start_assemble

@@ -21,6 +21,7 @@ ERRORS = {
     -9: "HDG_ERR_BREAKDOWN", -10: "HDG_ERR_UNKNOWN_SET", -11: "HDG_ERR_TIMEOUT", -12: "HDG_ERR_CAPACITY",
 }
 PREC_FP64, PREC_MIXED = 0, 1
+PRECOND_JACOBI, PRECOND_AMG = 0, 1
 FIELD_CONST, FIELD_SINSIN, FIELD_BUMPS, FIELD_FOURIER, FIELD_EXP_FOURIER = 0, 1, 2, 3, 4
 
 
@@ -36,14 +37,14 @@ class hdg_field(C.Structure):
 
 class hdg_solver(C.Structure):
     _fields_ = [("tol", C.c_double), ("maxit", C.c_int), ("precision", C.c_int), ("chunk", C.c_int),
-                ("inner_tol", C.c_double)]
+                ("inner_tol", C.c_double), ("preconditioner", C.c_int)]
 
 
 class hdg_timings(C.Structure):
     _fields_ = [("element_ms", C.c_double), ("gather_ms", C.c_double), ("apply_ms", C.c_double),
                 ("cg_ms", C.c_double), ("cg_a_ms", C.c_double), ("cg_b_ms", C.c_double), ("cg_samples", C.c_int),
                 ("cg_iterations", C.c_int), ("recover_ms", C.c_double), ("cg_a_bytes", C.c_double),
-                ("cg_b_bytes", C.c_double)]
+                ("cg_b_bytes", C.c_double), ("cg_bytes", C.c_double)]
 
 
 class hdg_stats(C.Structure):

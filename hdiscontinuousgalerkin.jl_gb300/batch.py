@@ -159,7 +159,7 @@ class Batch:
             self.bins.append(Bin(ctx, [self.problems[i] for i in idx], idx, precision))
         self.stats = None
 
-    def solve(self, tol=1e-10, maxit=100000, chunk=32, reassemble=True):
+    def solve(self, tol=1e-10, maxit=100000, chunk=32, reassemble=True, preconditioner=L.PRECOND_JACOBI):
         """assemble + condense (all bins), apply!, interleaved CG over the bins, recovery.
         reassemble: True (upload the coefficients and assemble), "resident" (assemble from the
         coefficients already on the device) or False (keep the assembled systems)."""
@@ -168,7 +168,7 @@ class Batch:
                 b.reassemble(resident=(reassemble == "resident"))
             b.apply()
         prec = self.bins[0].precision
-        o = L.hdg_solver(float(tol), int(maxit), int(prec), int(chunk), 1e-5)
+        o = L.hdg_solver(float(tol), int(maxit), int(prec), int(chunk), 1e-5, int(preconditioner))
         n = len(self.problems)
         st = (L.hdg_stats * n)()
         arr = (C.c_void_p * len(self.bins))(*[b.h for b in self.bins])

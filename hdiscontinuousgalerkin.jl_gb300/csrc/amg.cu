@@ -1,0 +1,1055 @@
+// Smoothed-aggregation algebraic multigrid (SA-AMG) V-cycle used as the preconditioner of the
+// trace CG (an alternative to Jacobi).  It has no reference counterpart: the reference solves
+// K \ b with a sparse direct solver (examples/poisson2D_HDG.jl:195).
+//
+// Method (Vanek, Mandel & Brezina 1996; Vanek, Brezina & Mandel 2001).
+//  * Level 0 is the trace matrix itself: faces with nt dofs each, in the block-ELL layout.  The
+//    near-null space is the constant trace (Legendre mode 0 = 1 on every face).  Faces are
+//    aggregated greedily on the face graph (faces of a common cell are neighbours); Dirichlet
+//    faces (decoupled after apply!) belong to no aggregate.  The tentative prolongator puts
+//    1/sqrt(|J|) on the mode-0 row of every face of aggregate J.
+//  * Level l >= 1 is a scalar CSR matrix.  Its nodes are aggregated on the quotient of the level
+//    below's graph; the tentative prolongator normalises the near-null vector carried down
+//    (B_{l+1}[J] = |B_l restricted to J|).
+//  * Smoothed prolongator P = (I - w D^-1 A) P_tent: D is the face-block diagonal (nt x nt) on
+//    level 0 with w = 4/(3 lambda), lambda a Gershgorin bound of D^-1 A per problem, and the
+//    l1 row sums on the coarse levels with w = 4/3 (their spectrum lies in (0, 1]).
+//  * Coarse operator A_{l+1} = P' A P.  Coarsening stops once every problem has at most 96
+//    coarse rows; the coarsest systems are inverted densely, one per problem.
+//  * V(2,2) cycle: damped block Jacobi on level 0 (x += D^-1 (b - A x) / lambda), l1-Jacobi on
+//    the coarse levels, exact coarsest solve.  Pre- and post-smoothing are the same symmetric
+//    iteration, so the cycle is a symmetric positive definite preconditioner.
+//
+// Aggregates depend only on the mesh and the Dirichlet faces, never on matrix values.  The
+// symbolic setup (aggregates, every sparsity pattern, the P' lists) therefore runs once per
+// system on the host and is reused when the system is reassembled with new coefficients; the
+// numeric setup (block inverses, bounds, P, A P, P' A P, coarsest inverses) runs on the device
+// after every assembly.  Batched systems are block diagonal: aggregates never cross problems,
+// so each problem gets its own hierarchy inside the shared arrays.
+//
+// Everything in the hierarchy and the cycle is FP32: the preconditioner only has to be a fixed
+// SPD approximation.  All sums run in a fixed order, so the cycle is deterministic.
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
+#include "hdg_device.cuh"
+
+namespace {
+
+constexpr int AMG_MAX_COARSE = 96;  // per problem, dense inverse on the coarsest level
+constexpr int AMG_MAX_LEVELS = 12;
+constexpr int AMG_CINV_MAX = 150;   // largest dense coarsest block: (2 m^2 + m) floats of shared memory
+constexpr int PW = 5;               // level-0 prolongator row width (a face and its 4 neighbours)
+
+// Greedy aggregation on an adjacency graph (CSR, symmetric, no self loops needed):
+// 1. a node whose active neighbours are all free becomes a root with all of them;
+// 2. a free node joins the aggregate of its first aggregated neighbour;
+// 3. the rest become roots with their free neighbours.
+// Aggregates are renumbered by their smallest member, so aggregates of one problem (whose nodes
+// are contiguous) are contiguous too.
+int aggregate(int n, const std::vector<int32_t>& ptr, const std::vector<int32_t>& adj, const std::vector<char>& active,
+              std::vector<int32_t>* agg_out) {
+  std::vector<int32_t>& agg = *agg_out;
+  agg.assign(n, -1);
+  int na = 0;
+  for (int i = 0; i < n; ++i) {
+    if (!active[i] || agg[i] >= 0) continue;
+    bool free_all = true;
+    for (int e = ptr[i]; e < ptr[i + 1]; ++e) {
+      const int j = adj[e];
+      if (j != i && active[j] && agg[j] >= 0) {
+        free_all = false;
+        break;
+      }
+    }
+    if (!free_all) continue;
+    agg[i] = na;
+    for (int e = ptr[i]; e < ptr[i + 1]; ++e)
+      if (active[adj[e]]) agg[adj[e]] = na;
+    ++na;
+  }
+  for (int i = 0; i < n; ++i) {
+    if (!active[i] || agg[i] >= 0) continue;
+    for (int e = ptr[i]; e < ptr[i + 1]; ++e) {
+      const int j = adj[e];
+      if (j != i && active[j] && agg[j] >= 0) {
+        agg[i] = agg[j];
+        break;
+      }
+    }
+  }
+  for (int i = 0; i < n; ++i) {
+    if (!active[i] || agg[i] >= 0) continue;
+    agg[i] = na;
+    for (int e = ptr[i]; e < ptr[i + 1]; ++e)
+      if (active[adj[e]] && agg[adj[e]] < 0) agg[adj[e]] = na;
+    ++na;
+  }
+  // renumber by smallest member
+  std::vector<int32_t> first(na, INT32_MAX);
+  for (int i = 0; i < n; ++i)
+    if (agg[i] >= 0) first[agg[i]] = std::min(first[agg[i]], (int32_t)i);
+  std::vector<int32_t> order(na);
+  std::iota(order.begin(), order.end(), 0);
+  std::sort(order.begin(), order.end(), [&](int a, int b) { return first[a] < first[b]; });
+  std::vector<int32_t> rank(na);
+  for (int k = 0; k < na; ++k) rank[order[k]] = k;
+  for (int i = 0; i < n; ++i)
+    if (agg[i] >= 0) agg[i] = rank[agg[i]];
+  return na;
+}
+
+// Quotient graph of (ptr, adj) by agg: J ~ K when some member of J neighbours some member of K.
+void quotient(int n, const std::vector<int32_t>& ptr, const std::vector<int32_t>& adj, const std::vector<int32_t>& agg,
+              int na, std::vector<int32_t>* qptr, std::vector<int32_t>* qadj) {
+  std::vector<std::vector<int32_t>> nb(na);
+  for (int i = 0; i < n; ++i) {
+    if (agg[i] < 0) continue;
+    for (int e = ptr[i]; e < ptr[i + 1]; ++e) {
+      const int j = adj[e];
+      if (agg[j] >= 0 && agg[j] != agg[i]) nb[agg[i]].push_back(agg[j]);
+    }
+  }
+  qptr->assign(na + 1, 0);
+  qadj->clear();
+  for (int J = 0; J < na; ++J) {
+    auto& v = nb[J];
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+    qadj->insert(qadj->end(), v.begin(), v.end());
+    (*qptr)[J + 1] = (int32_t)qadj->size();
+  }
+}
+
+// Device copy of a host array that may be empty (a one-element buffer is kept so that kernels get
+// a valid pointer; nothing reads it when the array is empty).
+template <class T> void upload_min1(DevBuf<T>& d, const std::vector<T>& v, cudaStream_t st) {
+  if (v.empty()) d.alloc(1);
+  else d.upload(v.data(), v.size(), st);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------
+// Host-side structure
+struct AmgLevel {  // a scalar level l >= 1 (rows = aggregates of level l-1)
+  int n = 0;
+  std::vector<int32_t> h_ptr, h_col;  // pattern of A_l (sorted columns, diagonal included)
+  std::vector<int32_t> h_prob;        // problem of each row
+  std::vector<double> h_B;            // near-null vector on this level
+  DevBuf<int32_t> ptr, col;
+  DevBuf<float> val, dl1inv;
+  DevBuf<float> b, x, t, r;           // cycle vectors: rhs, iterate, sweep target, residual
+  // transfer to the next level (all empty on the coarsest)
+  int nc = 0;
+  DevBuf<int32_t> agg;                // aggregate of each row
+  DevBuf<float> tent;                 // tentative weight of each row
+  DevBuf<int32_t> pptr, pcol;         // P (CSR, sorted columns)
+  DevBuf<float> pval;
+  DevBuf<int32_t> apptr, apcol;       // A P pattern
+  DevBuf<float> apval;
+  DevBuf<int32_t> rptr, rent, rrow;   // P': per coarse row the P entries (index, fine row)
+};
+
+struct AmgHierarchy {
+  int nf = 0, nt = 0, nprob = 0;
+  // level 0 (faces)
+  DevBuf<int32_t> agg0;      // [nf] aggregate (-1: Dirichlet face)
+  DevBuf<float> tent0;       // [nf]
+  DevBuf<int32_t> pcol0;     // [nf][PW] prolongator columns (-1 pad), shared by the face's nt rows
+  DevBuf<float> pval0;       // [nf*nt][PW]
+  int wap = 0;               // width of an A0 P0 row
+  DevBuf<int32_t> apcol0;    // [nf][wap]
+  DevBuf<int8_t> apmap0;     // [nf][5 slots][PW]: position of pcol0[g_k][c] in apcol0[f]
+  DevBuf<float> apval0;      // [nf*nt][wap]
+  DevBuf<int32_t> rptr0, rent0;  // P0': per coarse row J the (face*PW + c) entries with pcol0 == J
+  DevBuf<float> dinv0;       // [nf][nt][nt]
+  DevBuf<float> lam0;        // [nprob] Gershgorin bound of D^-1 A0
+  DevBuf<int32_t> face_prob; // [nf]
+  DevBuf<float> val0f;       // FP32 trace matrix (when the system has none)
+  DevBuf<float> x0, r0;      // level-0 cycle vectors
+  std::vector<AmgLevel> lev; // lev[0] is level 1
+  // coarsest (last level): per-problem dense inverses
+  std::vector<int32_t> h_crow0;  // [nprob+1] first coarsest row of each problem
+  DevBuf<int32_t> crow0, coff;   // coff: offset of each problem's dense block
+  DevBuf<float> cinv;
+  int cmax = 0;
+  bool built = false;
+};
+
+void destroy_amg(AmgHierarchy* h) { delete h; }
+
+// ------------------------------------------------------------------------------------------
+// Symbolic setup
+void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) {
+  if (s->amg) destroy_amg(s->amg);
+  s->amg = new AmgHierarchy();
+  AmgHierarchy* H = s->amg;
+  const int nf = s->nf, nt = s->nt;
+  H->nf = nf;
+  H->nt = nt;
+  H->nprob = s->nprob;
+  const hdg_mesh* m = s->space->mesh;
+  cudaStream_t st = s->ctx->stream;
+  // face graph and problem of each face
+  std::vector<int32_t> fptr(nf + 1, 0), fadj;
+  std::vector<int32_t> fprob(nf, 0);
+  for (int P = 0; P < s->nprob; ++P)
+    for (int f = m->prob_face0[P]; f < m->prob_face0[P + 1]; ++f) fprob[f] = P;
+  for (int f = 0; f < nf; ++f) {
+    for (int e = s->h_browptr[f]; e < s->h_browptr[f + 1]; ++e)
+      if (s->h_bcol[e] != f) fadj.push_back(s->h_bcol[e]);
+    fptr[f + 1] = (int32_t)fadj.size();
+  }
+  std::vector<char> active(nf);
+  for (int f = 0; f < nf; ++f) active[f] = !dirichlet_face[f];
+  std::vector<int32_t> agg0;
+  const int na0 = aggregate(nf, fptr, fadj, active, &agg0);
+  std::vector<int> size0(na0, 0);
+  for (int f = 0; f < nf; ++f)
+    if (agg0[f] >= 0) ++size0[agg0[f]];
+  std::vector<float> tent0(nf, 0.f);
+  for (int f = 0; f < nf; ++f)
+    if (agg0[f] >= 0) tent0[f] = (float)(1.0 / std::sqrt((double)size0[agg0[f]]));
+  // P0 pattern per face: aggregates of the face and its neighbours (active only)
+  std::vector<int32_t> pcol0((size_t)nf * PW, -1);
+  for (int f = 0; f < nf; ++f) {
+    if (!active[f]) continue;
+    int cols[8], nc = 0;
+    cols[nc++] = agg0[f];
+    for (int e = fptr[f]; e < fptr[f + 1]; ++e)
+      if (agg0[fadj[e]] >= 0) cols[nc++] = agg0[fadj[e]];
+    std::sort(cols, cols + nc);
+    nc = (int)(std::unique(cols, cols + nc) - cols);
+    for (int c = 0; c < nc && c < PW; ++c) pcol0[(size_t)f * PW + c] = cols[c];
+  }
+  // A0 P0 pattern per face: union over the 5 slot faces of their P0 columns
+  std::vector<int32_t> bcol5((size_t)5 * nf);
+  s->d_bcol5.download(bcol5.data(), bcol5.size(), st);
+  HDG_CUDA(cudaStreamSynchronize(st));
+  std::vector<std::vector<int32_t>> apc(nf);
+  int wap = 1;
+  for (int f = 0; f < nf; ++f) {
+    auto& v = apc[f];
+    for (int k = 0; k < 5; ++k) {
+      const int g = bcol5[(size_t)k * nf + f];
+      for (int c = 0; c < PW; ++c)
+        if (pcol0[(size_t)g * PW + c] >= 0) v.push_back(pcol0[(size_t)g * PW + c]);
+    }
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+    wap = std::max(wap, (int)v.size());
+  }
+  if (wap > 32) throw HdgError{HDG_ERR_ARG, "AMG: prolongator pattern wider than 32 (invalid trace mesh)"};
+  std::vector<int32_t> apcol0((size_t)nf * wap, -1);
+  std::vector<int8_t> apmap0((size_t)nf * 5 * PW, -1);
+  for (int f = 0; f < nf; ++f) {
+    const auto& v = apc[f];
+    std::copy(v.begin(), v.end(), apcol0.begin() + (size_t)f * wap);
+    for (int k = 0; k < 5; ++k) {
+      const int g = bcol5[(size_t)k * nf + f];
+      for (int c = 0; c < PW; ++c) {
+        const int J = pcol0[(size_t)g * PW + c];
+        if (J < 0) continue;
+        apmap0[((size_t)f * 5 + k) * PW + c] = (int8_t)(std::lower_bound(v.begin(), v.end(), J) - v.begin());
+      }
+    }
+  }
+  // P0' lists and the level-1 pattern (rows = aggregates)
+  std::vector<std::vector<int32_t>> rl(na0);
+  for (int f = 0; f < nf; ++f)
+    for (int c = 0; c < PW; ++c)
+      if (pcol0[(size_t)f * PW + c] >= 0) rl[pcol0[(size_t)f * PW + c]].push_back(f * PW + c);
+  std::vector<int32_t> rptr0(na0 + 1, 0), rent0;
+  AmgLevel L1;
+  L1.n = na0;
+  L1.h_ptr.assign(na0 + 1, 0);
+  L1.h_prob.assign(na0, 0);
+  L1.h_B.assign(na0, 0.0);
+  for (int J = 0; J < na0; ++J) {
+    rent0.insert(rent0.end(), rl[J].begin(), rl[J].end());
+    rptr0[J + 1] = (int32_t)rent0.size();
+    std::vector<int32_t> cols;
+    for (int e : rl[J]) {
+      const auto& v = apc[e / PW];
+      cols.insert(cols.end(), v.begin(), v.end());
+    }
+    std::sort(cols.begin(), cols.end());
+    cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
+    L1.h_col.insert(L1.h_col.end(), cols.begin(), cols.end());
+    L1.h_ptr[J + 1] = (int32_t)L1.h_col.size();
+    L1.h_B[J] = std::sqrt((double)size0[J]);
+  }
+  for (int f = 0; f < nf; ++f)
+    if (agg0[f] >= 0) L1.h_prob[agg0[f]] = fprob[f];
+  // quotient graph of the face graph for level 1's aggregation
+  std::vector<int32_t> gptr, gadj;
+  quotient(nf, fptr, fadj, agg0, na0, &gptr, &gadj);
+  // upload level 0
+  H->agg0.upload(agg0.data(), agg0.size(), st);
+  H->tent0.upload(tent0.data(), tent0.size(), st);
+  H->pcol0.upload(pcol0.data(), pcol0.size(), st);
+  H->pval0.alloc((size_t)nf * nt * PW);
+  H->wap = wap;
+  H->apcol0.upload(apcol0.data(), apcol0.size(), st);
+  H->apmap0.upload(apmap0.data(), apmap0.size(), st);
+  H->apval0.alloc((size_t)nf * nt * wap);
+  H->rptr0.upload(rptr0.data(), rptr0.size(), st);
+  upload_min1(H->rent0, rent0, st);
+  H->dinv0.alloc((size_t)nf * nt * nt);
+  H->lam0.alloc(std::max(s->nprob, 1));
+  H->face_prob.upload(fprob.data(), fprob.size(), st);
+  H->x0.alloc((size_t)nf * nt);
+  H->r0.alloc((size_t)nf * nt);
+  H->lev.clear();
+  H->lev.push_back(std::move(L1));
+  // coarser levels
+  auto max_per_problem = [&](const AmgLevel& L) {
+    std::vector<int> cnt(s->nprob, 0);
+    for (int i = 0; i < L.n; ++i) ++cnt[L.h_prob[i]];
+    return cnt.empty() ? 0 : *std::max_element(cnt.begin(), cnt.end());
+  };
+  while ((int)H->lev.size() < AMG_MAX_LEVELS && max_per_problem(H->lev.back()) > AMG_MAX_COARSE) {
+    AmgLevel& F = H->lev.back();
+    const int n = F.n;
+    std::vector<char> act(n, 1);
+    std::vector<int32_t> agg;
+    const int na = aggregate(n, gptr, gadj, act, &agg);
+    if (na > (int)(0.85 * n)) break;  // no longer coarsening
+    std::vector<double> nrm(na, 0.0);
+    for (int i = 0; i < n; ++i) nrm[agg[i]] += F.h_B[i] * F.h_B[i];
+    for (int J = 0; J < na; ++J) nrm[J] = std::sqrt(nrm[J]);
+    std::vector<float> tent(n);
+    for (int i = 0; i < n; ++i) tent[i] = nrm[agg[i]] > 0 ? (float)(F.h_B[i] / nrm[agg[i]]) : 0.f;
+    // P pattern row i: aggregates of the columns of A row i
+    std::vector<int32_t> pptr(n + 1, 0), pcol;
+    for (int i = 0; i < n; ++i) {
+      std::vector<int32_t> v;
+      for (int e = F.h_ptr[i]; e < F.h_ptr[i + 1]; ++e) v.push_back(agg[F.h_col[e]]);
+      std::sort(v.begin(), v.end());
+      v.erase(std::unique(v.begin(), v.end()), v.end());
+      pcol.insert(pcol.end(), v.begin(), v.end());
+      pptr[i + 1] = (int32_t)pcol.size();
+    }
+    // A P pattern row i: union of the P rows of A row i's columns
+    std::vector<int32_t> apptr(n + 1, 0), apcol;
+    for (int i = 0; i < n; ++i) {
+      std::vector<int32_t> v;
+      for (int e = F.h_ptr[i]; e < F.h_ptr[i + 1]; ++e) {
+        const int k = F.h_col[e];
+        v.insert(v.end(), pcol.begin() + pptr[k], pcol.begin() + pptr[k + 1]);
+      }
+      std::sort(v.begin(), v.end());
+      v.erase(std::unique(v.begin(), v.end()), v.end());
+      apcol.insert(apcol.end(), v.begin(), v.end());
+      apptr[i + 1] = (int32_t)apcol.size();
+    }
+    // P' lists and the next level's pattern
+    std::vector<std::vector<int32_t>> r(na);
+    for (int i = 0; i < n; ++i)
+      for (int e = pptr[i]; e < pptr[i + 1]; ++e) r[pcol[e]].push_back(e);
+    std::vector<int32_t> prow_of(pcol.size());
+    for (int i = 0; i < n; ++i)
+      for (int e = pptr[i]; e < pptr[i + 1]; ++e) prow_of[e] = i;
+    std::vector<int32_t> rptr(na + 1, 0), rent, rrow;
+    AmgLevel C;
+    C.n = na;
+    C.h_ptr.assign(na + 1, 0);
+    C.h_prob.assign(na, 0);
+    C.h_B = nrm;
+    for (int J = 0; J < na; ++J) {
+      std::vector<int32_t> cols;
+      for (int e : r[J]) {
+        rent.push_back(e);
+        rrow.push_back(prow_of[e]);
+        const int i = prow_of[e];
+        cols.insert(cols.end(), apcol.begin() + apptr[i], apcol.begin() + apptr[i + 1]);
+      }
+      rptr[J + 1] = (int32_t)rent.size();
+      std::sort(cols.begin(), cols.end());
+      cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
+      C.h_col.insert(C.h_col.end(), cols.begin(), cols.end());
+      C.h_ptr[J + 1] = (int32_t)C.h_col.size();
+    }
+    for (int i = 0; i < n; ++i) C.h_prob[agg[i]] = F.h_prob[i];
+    F.nc = na;
+    F.agg.upload(agg.data(), agg.size(), st);
+    F.tent.upload(tent.data(), tent.size(), st);
+    F.pptr.upload(pptr.data(), pptr.size(), st);
+    F.pcol.upload(pcol.data(), pcol.size(), st);
+    F.pval.alloc(pcol.size());
+    F.apptr.upload(apptr.data(), apptr.size(), st);
+    F.apcol.upload(apcol.data(), apcol.size(), st);
+    F.apval.alloc(apcol.size());
+    F.rptr.upload(rptr.data(), rptr.size(), st);
+    upload_min1(F.rent, rent, st);
+    upload_min1(F.rrow, rrow, st);
+    std::vector<int32_t> qptr, qadj;
+    quotient(n, gptr, gadj, agg, na, &qptr, &qadj);
+    gptr.swap(qptr);
+    gadj.swap(qadj);
+    H->lev.push_back(std::move(C));
+  }
+  // device copies of every level's matrix pattern and vectors
+  for (auto& L : H->lev) {
+    L.ptr.upload(L.h_ptr.data(), L.h_ptr.size(), st);
+    upload_min1(L.col, L.h_col, st);
+    L.val.alloc(std::max<size_t>(L.h_col.size(), 1));
+    L.dl1inv.alloc(std::max(L.n, 1));
+    L.b.alloc(std::max(L.n, 1));
+    L.x.alloc(std::max(L.n, 1));
+    L.t.alloc(std::max(L.n, 1));
+    L.r.alloc(std::max(L.n, 1));
+  }
+  // coarsest: per-problem dense blocks
+  const AmgLevel& C = H->lev.back();
+  H->h_crow0.assign(s->nprob + 1, 0);
+  for (int i = 0; i < C.n; ++i) ++H->h_crow0[C.h_prob[i] + 1];
+  for (int P = 0; P < s->nprob; ++P) H->h_crow0[P + 1] += H->h_crow0[P];
+  std::vector<int32_t> coff(s->nprob + 1, 0);
+  H->cmax = 0;
+  for (int P = 0; P < s->nprob; ++P) {
+    const int mP = H->h_crow0[P + 1] - H->h_crow0[P];
+    H->cmax = std::max(H->cmax, mP);
+    coff[P + 1] = coff[P] + mP * mP;
+  }
+  if (H->cmax > AMG_CINV_MAX)
+    throw HdgError{HDG_ERR_ARG, "AMG: coarsening stalled above the dense coarsest size"};
+  H->crow0.upload(H->h_crow0.data(), H->h_crow0.size(), st);
+  H->coff.upload(coff.data(), coff.size(), st);
+  H->cinv.alloc(std::max(coff[s->nprob], 1));
+  H->built = true;
+  HDG_CUDA(cudaStreamSynchronize(st));
+}
+
+// ------------------------------------------------------------------------------------------
+// Numeric setup kernels
+namespace {
+
+__device__ __forceinline__ void atomic_max_pos(float* a, float v) {  // v >= 0: int order = float order
+  atomicMax(reinterpret_cast<int*>(a), __float_as_int(v));
+}
+
+// Inverse of each face's diagonal block (Gauss-Jordan, partial pivoting) and the per-problem
+// Gershgorin bound of D^-1 A0: max over rows of sum_j |(D^-1 A0)_ij|.
+template <int NT>
+__global__ void k_amg_block_inv(int nf, const int32_t* __restrict__ bcol5, const int8_t* __restrict__ kdiag,
+                                const float* __restrict__ val, const int32_t* __restrict__ face_prob,
+                                float* __restrict__ dinv, float* __restrict__ lam) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const int64_t nd = (int64_t)nf * NT;
+  float a[NT][2 * NT];
+  const int kd = kdiag[f];
+  for (int i = 0; i < NT; ++i)
+    for (int j = 0; j < NT; ++j) {
+      a[i][j] = val[(kd * NT + j) * nd + (int64_t)f * NT + i];
+      a[i][NT + j] = (i == j) ? 1.f : 0.f;
+    }
+  for (int c = 0; c < NT; ++c) {
+    int piv = c;
+    for (int i = c + 1; i < NT; ++i)
+      if (fabsf(a[i][c]) > fabsf(a[piv][c])) piv = i;
+    if (piv != c)
+      for (int j = 0; j < 2 * NT; ++j) {
+        const float t = a[c][j];
+        a[c][j] = a[piv][j];
+        a[piv][j] = t;
+      }
+    const float inv = (a[c][c] != 0.f) ? 1.f / a[c][c] : 0.f;
+    for (int j = 0; j < 2 * NT; ++j) a[c][j] *= inv;
+    for (int i = 0; i < NT; ++i) {
+      if (i == c) continue;
+      const float m = a[i][c];
+      for (int j = 0; j < 2 * NT; ++j) a[i][j] -= m * a[c][j];
+    }
+  }
+  for (int i = 0; i < NT; ++i)
+    for (int j = 0; j < NT; ++j) dinv[((int64_t)f * NT + i) * NT + j] = a[i][NT + j];
+  // row sums of |D^-1 A0| over the face's rows
+  float rs[NT];
+  for (int i = 0; i < NT; ++i) rs[i] = 0.f;
+  for (int k = 0; k < 5; ++k) {
+    const int g = bcol5[k * nf + f];
+    if (k > 0 && g == f && k != kd) continue;  // padding slot (zero block)
+    for (int j = 0; j < NT; ++j) {
+      float col[NT];
+      for (int i = 0; i < NT; ++i) col[i] = val[(k * NT + j) * nd + (int64_t)f * NT + i];
+      for (int i = 0; i < NT; ++i) {
+        float t = 0.f;
+        for (int l = 0; l < NT; ++l) t += a[i][NT + l] * col[l];
+        rs[i] += fabsf(t);
+      }
+    }
+  }
+  float mx = 0.f;
+  for (int i = 0; i < NT; ++i) mx = fmaxf(mx, rs[i]);
+  atomic_max_pos(lam + face_prob[f], mx);
+}
+
+// P0 = (I - w D^-1 A0) P_tent, w = 4/(3 lambda); one thread per face (all its nt rows).
+template <int NT>
+__global__ void k_amg_p0(int nf, const int32_t* __restrict__ bcol5, const float* __restrict__ val,
+                         const float* __restrict__ dinv, const float* __restrict__ lam,
+                         const int32_t* __restrict__ face_prob, const int32_t* __restrict__ agg0,
+                         const float* __restrict__ tent0, const int32_t* __restrict__ pcol0,
+                         float* __restrict__ pval0) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const int64_t nd = (int64_t)nf * NT;
+  float out[NT][PW];
+  for (int i = 0; i < NT; ++i)
+    for (int c = 0; c < PW; ++c) out[i][c] = 0.f;
+  if (pcol0[f * PW] < 0) {  // Dirichlet face: no prolongator rows
+    for (int i = 0; i < NT; ++i)
+      for (int c = 0; c < PW; ++c) pval0[((int64_t)f * NT + i) * PW + c] = 0.f;
+    return;
+  }
+  const float w = (4.f / 3.f) / fmaxf(lam[face_prob[f]], 1e-30f);
+  int done[5];
+  int nd_ = 0;
+  for (int k = 0; k < 5; ++k) {
+    const int g = bcol5[k * nf + f];
+    bool dup = false;
+    for (int t = 0; t < nd_; ++t) dup |= (done[t] == g);
+    if (dup) continue;  // padding slots repeat the face itself; its block is counted once (real slot)
+    done[nd_++] = g;
+    const int J = agg0[g];
+    if (J < 0) continue;
+    int c = 0;
+    while (c < PW && pcol0[f * PW + c] != J) ++c;
+    if (c == PW) continue;  // not in the pattern (cannot happen for a valid setup)
+    // column (g, mode 0) of A0's block row f, for the real slot holding g
+    int ks = k;
+    for (int kk = 0; kk < 5; ++kk)
+      if (bcol5[kk * nf + f] == g) { ks = kk; break; }
+    float col[NT];
+    for (int i = 0; i < NT; ++i) col[i] = val[(ks * NT + 0) * nd + (int64_t)f * NT + i];
+    for (int i = 0; i < NT; ++i) {
+      float t = 0.f;
+      for (int l = 0; l < NT; ++l) t += dinv[((int64_t)f * NT + i) * NT + l] * col[l];
+      out[i][c] -= w * t * tent0[g];
+    }
+  }
+  {
+    const int J = agg0[f];
+    int c = 0;
+    while (c < PW && pcol0[f * PW + c] != J) ++c;
+    if (c < PW) out[0][c] += tent0[f];
+  }
+  for (int i = 0; i < NT; ++i)
+    for (int c = 0; c < PW; ++c) pval0[((int64_t)f * NT + i) * PW + c] = out[i][c];
+}
+
+// A0 P0, one thread per fine row.
+template <int NT>
+__global__ void k_amg_ap0(int nf, int wap, const int32_t* __restrict__ bcol5, const float* __restrict__ val,
+                          const int32_t* __restrict__ pcol0, const float* __restrict__ pval0,
+                          const int8_t* __restrict__ apmap0, float* __restrict__ apval0) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t nd = (int64_t)nf * NT;
+  if (r >= nd) return;
+  const int f = (int)(r / NT);
+  float acc[32];
+  for (int q = 0; q < wap && q < 32; ++q) acc[q] = 0.f;
+  int seen[5];
+  int ns = 0;
+  for (int k = 0; k < 5; ++k) {
+    const int g = bcol5[k * nf + f];
+    bool dup = false;
+    for (int t = 0; t < ns; ++t) dup |= (seen[t] == g);
+    if (dup) continue;
+    seen[ns++] = g;
+    for (int j = 0; j < NT; ++j) {
+      const float a = val[(k * NT + j) * nd + r];
+      if (a == 0.f) continue;
+      for (int c = 0; c < PW; ++c) {
+        if (pcol0[g * PW + c] < 0) break;
+        const int q = apmap0[((int64_t)f * 5 + k) * PW + c];
+        if (q >= 0 && q < wap) acc[q] += a * pval0[((int64_t)g * NT + j) * PW + c];
+      }
+    }
+  }
+  for (int q = 0; q < wap; ++q) apval0[r * wap + q] = acc[q];
+}
+
+__device__ __forceinline__ int find_col(const int32_t* __restrict__ col, int a, int b, int key) {
+  while (a < b) {  // lower bound in the sorted columns [a, b)
+    const int m = (a + b) >> 1;
+    if (col[m] < key) a = m + 1;
+    else b = m;
+  }
+  return a;
+}
+
+// val[position of key in the sorted columns [a, b)] += v; a key outside the pattern is ignored
+// (the symbolic setup puts every product's column in the pattern, so this never drops anything)
+__device__ __forceinline__ void add_at(const int32_t* __restrict__ col, float* __restrict__ val, int a, int b, int key,
+                                       float v) {
+  const int e = find_col(col, a, b, key);
+  if (e < b && col[e] == key) val[e] += v;
+}
+
+// A1 = P0' (A0 P0), one thread per coarse row.
+template <int NT>
+__global__ void k_amg_rap0(int na, int wap, const int32_t* __restrict__ rptr0, const int32_t* __restrict__ rent0,
+                           const float* __restrict__ pval0, const int32_t* __restrict__ apcol0,
+                           const float* __restrict__ apval0, const int32_t* __restrict__ ptr1,
+                           const int32_t* __restrict__ col1, float* __restrict__ val1) {
+  const int J = blockIdx.x * blockDim.x + threadIdx.x;
+  if (J >= na) return;
+  const int a0 = ptr1[J], a1 = ptr1[J + 1];
+  for (int e = a0; e < a1; ++e) val1[e] = 0.f;
+  for (int t = rptr0[J]; t < rptr0[J + 1]; ++t) {
+    const int f = rent0[t] / PW, c = rent0[t] - f * PW;
+    for (int i = 0; i < NT; ++i) {
+      const float p = pval0[((int64_t)f * NT + i) * PW + c];
+      if (p == 0.f) continue;
+      const float* apr = apval0 + ((int64_t)f * NT + i) * wap;
+      for (int q = 0; q < wap; ++q) {
+        const int K = apcol0[(int64_t)f * wap + q];
+        if (K < 0) break;
+        add_at(col1, val1, a0, a1, K, p * apr[q]);
+      }
+    }
+  }
+}
+
+// 1 / l1 row sums of a CSR level
+__global__ void k_amg_dl1(int n, const int32_t* __restrict__ ptr, const float* __restrict__ val,
+                          float* __restrict__ dl1inv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float s = 0.f;
+  for (int e = ptr[i]; e < ptr[i + 1]; ++e) s += fabsf(val[e]);
+  dl1inv[i] = s > 0.f ? 1.f / s : 0.f;
+}
+
+// P = (I - 4/3 D_l1^-1 A) P_tent on a CSR level, one thread per row
+__global__ void k_amg_p(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                        const float* __restrict__ val, const float* __restrict__ dl1inv, const int32_t* __restrict__ agg,
+                        const float* __restrict__ tent, const int32_t* __restrict__ pptr,
+                        const int32_t* __restrict__ pcol, float* __restrict__ pval) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int p0 = pptr[i], p1 = pptr[i + 1];
+  for (int e = p0; e < p1; ++e) pval[e] = 0.f;
+  const float w = (4.f / 3.f) * dl1inv[i];
+  for (int e = ptr[i]; e < ptr[i + 1]; ++e) {
+    const int k = col[e];
+    add_at(pcol, pval, p0, p1, agg[k], -w * val[e] * tent[k]);
+  }
+  add_at(pcol, pval, p0, p1, agg[i], tent[i]);
+}
+
+// A P on a CSR level, one thread per row
+__global__ void k_amg_ap(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                         const float* __restrict__ val, const int32_t* __restrict__ pptr,
+                         const int32_t* __restrict__ pcol, const float* __restrict__ pval,
+                         const int32_t* __restrict__ apptr, const int32_t* __restrict__ apcol,
+                         float* __restrict__ apval) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int a0 = apptr[i], a1 = apptr[i + 1];
+  for (int e = a0; e < a1; ++e) apval[e] = 0.f;
+  for (int e = ptr[i]; e < ptr[i + 1]; ++e) {
+    const int k = col[e];
+    const float a = val[e];
+    for (int t = pptr[k]; t < pptr[k + 1]; ++t) add_at(apcol, apval, a0, a1, pcol[t], a * pval[t]);
+  }
+}
+
+// A_{l+1} = P' (A P), one thread per coarse row
+__global__ void k_amg_rap(int nc, const int32_t* __restrict__ rptr, const int32_t* __restrict__ rent,
+                          const int32_t* __restrict__ rrow, const float* __restrict__ pval,
+                          const int32_t* __restrict__ apptr, const int32_t* __restrict__ apcol,
+                          const float* __restrict__ apval, const int32_t* __restrict__ cptr,
+                          const int32_t* __restrict__ ccol, float* __restrict__ cval) {
+  const int J = blockIdx.x * blockDim.x + threadIdx.x;
+  if (J >= nc) return;
+  const int a0 = cptr[J], a1 = cptr[J + 1];
+  for (int e = a0; e < a1; ++e) cval[e] = 0.f;
+  for (int t = rptr[J]; t < rptr[J + 1]; ++t) {
+    const float p = pval[rent[t]];
+    const int i = rrow[t];
+    for (int q = apptr[i]; q < apptr[i + 1]; ++q) add_at(ccol, cval, a0, a1, apcol[q], p * apval[q]);
+  }
+}
+
+// Dense inverse of each problem's coarsest matrix (Gauss-Jordan with partial pivoting in shared
+// memory, one CTA per problem).  Sizes are at most AMG_CINV_MAX (the symbolic setup checks).
+__global__ void k_amg_coarse_inv(const int32_t* __restrict__ crow0, const int32_t* __restrict__ coff,
+                                 const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                                 const float* __restrict__ val, float* __restrict__ cinv) {
+  extern __shared__ float sm[];
+  const int P = blockIdx.x;
+  const int r0 = crow0[P], m = crow0[P + 1] - r0;
+  if (m == 0) return;
+  const int w = 2 * m;
+  float* a = sm;          // m x 2m augmented matrix
+  float* mult = sm + m * w;  // m multipliers of the current column
+  __shared__ int piv;
+  for (int t = threadIdx.x; t < m * w; t += blockDim.x) a[t] = 0.f;
+  __syncthreads();
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    for (int e = ptr[r0 + i]; e < ptr[r0 + i + 1]; ++e) {
+      const int c = col[e] - r0;
+      if (c >= 0 && c < m) a[i * w + c] = val[e];
+    }
+    a[i * w + m + i] = 1.f;
+  }
+  __syncthreads();
+  for (int c = 0; c < m; ++c) {
+    if (threadIdx.x == 0) {
+      int p = c;
+      for (int i = c + 1; i < m; ++i)
+        if (fabsf(a[i * w + c]) > fabsf(a[p * w + c])) p = i;
+      piv = p;
+    }
+    __syncthreads();
+    const int pr = piv;
+    if (pr != c)
+      for (int j = threadIdx.x; j < w; j += blockDim.x) {
+        const float t = a[c * w + j];
+        a[c * w + j] = a[pr * w + j];
+        a[pr * w + j] = t;
+      }
+    __syncthreads();
+    const float d = a[c * w + c];
+    const float inv = d != 0.f ? 1.f / d : 0.f;
+    __syncthreads();
+    for (int j = threadIdx.x; j < w; j += blockDim.x) a[c * w + j] *= inv;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) mult[i] = (i == c) ? 0.f : a[i * w + c];
+    __syncthreads();
+    for (int t = threadIdx.x; t < m * w; t += blockDim.x) {
+      const int i = t / w, j = t - i * w;
+      if (i != c) a[t] -= mult[i] * a[c * w + j];
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
+    const int i = t / m, j = t - i * m;
+    cinv[coff[P] + t] = a[i * w + m + j];
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Cycle kernels
+template <int NT>
+__global__ void k_amg_face_smooth(int nf, const int32_t* __restrict__ bcol5, const float* __restrict__ val,
+                                  const float* __restrict__ dinv, const float* __restrict__ lam,
+                                  const int32_t* __restrict__ face_prob, const float* __restrict__ b,
+                                  const float* __restrict__ xin, float* __restrict__ xout, int first) {
+  // first: x = D^-1 b / lambda;  else x = xin + D^-1 (b - A xin) / lambda  (xout != xin)
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const int64_t nd = (int64_t)nf * NT;
+  float res[NT];
+  for (int i = 0; i < NT; ++i) res[i] = b[(int64_t)f * NT + i];
+  if (!first) {
+    int seen[5];
+    int ns = 0;
+    for (int k = 0; k < 5; ++k) {
+      const int g = bcol5[k * nf + f];
+      bool dup = false;
+      for (int t = 0; t < ns; ++t) dup |= (seen[t] == g);
+      if (dup) continue;
+      seen[ns++] = g;
+      for (int j = 0; j < NT; ++j) {
+        const float xv = xin[(int64_t)g * NT + j];
+        for (int i = 0; i < NT; ++i) res[i] -= val[(k * NT + j) * nd + (int64_t)f * NT + i] * xv;
+      }
+    }
+  }
+  const float sc = 1.f / fmaxf(lam[face_prob[f]], 1e-30f);
+  for (int i = 0; i < NT; ++i) {
+    float t = 0.f;
+    for (int l = 0; l < NT; ++l) t += dinv[((int64_t)f * NT + i) * NT + l] * res[l];
+    xout[(int64_t)f * NT + i] = (first ? 0.f : xin[(int64_t)f * NT + i]) + sc * t;
+  }
+}
+
+// r = b - A0 x (level 0)
+template <int NT>
+__global__ void k_amg_face_residual(int nf, const int32_t* __restrict__ bcol5, const float* __restrict__ val,
+                                    const float* __restrict__ b, const float* __restrict__ x, float* __restrict__ r) {
+  const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t nd = (int64_t)nf * NT;
+  if (row >= nd) return;
+  const int f = (int)(row / NT);
+  float s = b[row];
+  int seen[5];
+  int ns = 0;
+  for (int k = 0; k < 5; ++k) {
+    const int g = bcol5[k * nf + f];
+    bool dup = false;
+    for (int t = 0; t < ns; ++t) dup |= (seen[t] == g);
+    if (dup) continue;
+    seen[ns++] = g;
+    for (int j = 0; j < NT; ++j) s -= val[(k * NT + j) * nd + row] * x[(int64_t)g * NT + j];
+  }
+  r[row] = s;
+}
+
+// b1 = P0' r0 and the first l1-Jacobi sweep of level 1: x1 = b1 / dl1
+template <int NT>
+__global__ void k_amg_restrict0(int na, const int32_t* __restrict__ rptr0, const int32_t* __restrict__ rent0,
+                                const float* __restrict__ pval0, const float* __restrict__ r0,
+                                const float* __restrict__ dl1inv, float* __restrict__ b1, float* __restrict__ x1) {
+  const int J = blockIdx.x * blockDim.x + threadIdx.x;
+  if (J >= na) return;
+  float s = 0.f;
+  for (int t = rptr0[J]; t < rptr0[J + 1]; ++t) {
+    const int f = rent0[t] / PW, c = rent0[t] - f * PW;
+    for (int i = 0; i < NT; ++i) s += pval0[((int64_t)f * NT + i) * PW + c] * r0[(int64_t)f * NT + i];
+  }
+  b1[J] = s;
+  x1[J] = s * dl1inv[J];
+}
+
+// x0 += P0 x1
+template <int NT>
+__global__ void k_amg_prolong0(int nf, const int32_t* __restrict__ pcol0, const float* __restrict__ pval0,
+                               const float* __restrict__ x1, float* __restrict__ x0) {
+  const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (row >= (int64_t)nf * NT) return;
+  const int f = (int)(row / NT);
+  float s = 0.f;
+  for (int c = 0; c < PW; ++c) {
+    const int J = pcol0[f * PW + c];
+    if (J < 0) break;
+    s += pval0[row * PW + c] * x1[J];
+  }
+  x0[row] += s;
+}
+
+// CSR level: x_out = x_in + (b - A x_in) / dl1
+__global__ void k_amg_l1_sweep(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                               const float* __restrict__ val, const float* __restrict__ dl1inv,
+                               const float* __restrict__ b, const float* __restrict__ xin, float* __restrict__ xout) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float s = b[i];
+  for (int e = ptr[i]; e < ptr[i + 1]; ++e) s -= val[e] * xin[col[e]];
+  xout[i] = xin[i] + s * dl1inv[i];
+}
+
+// CSR level: r = b - A x
+__global__ void k_amg_residual(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                               const float* __restrict__ val, const float* __restrict__ b, const float* __restrict__ x,
+                               float* __restrict__ r) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float s = b[i];
+  for (int e = ptr[i]; e < ptr[i + 1]; ++e) s -= val[e] * x[col[e]];
+  r[i] = s;
+}
+
+// b_c = P' r and x_c = b_c / dl1_c (first sweep of the coarse level; dl1 NULL on the coarsest)
+__global__ void k_amg_restrict(int nc, const int32_t* __restrict__ rptr, const int32_t* __restrict__ rent,
+                               const int32_t* __restrict__ rrow, const float* __restrict__ pval,
+                               const float* __restrict__ r, const float* __restrict__ dl1inv, float* __restrict__ bc,
+                               float* __restrict__ xc) {
+  const int J = blockIdx.x * blockDim.x + threadIdx.x;
+  if (J >= nc) return;
+  float s = 0.f;
+  for (int t = rptr[J]; t < rptr[J + 1]; ++t) s += pval[rent[t]] * r[rrow[t]];
+  bc[J] = s;
+  if (dl1inv) xc[J] = s * dl1inv[J];
+}
+
+// x += P x_c
+__global__ void k_amg_prolong(int n, const int32_t* __restrict__ pptr, const int32_t* __restrict__ pcol,
+                              const float* __restrict__ pval, const float* __restrict__ xc, float* __restrict__ x) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float s = 0.f;
+  for (int e = pptr[i]; e < pptr[i + 1]; ++e) s += pval[e] * xc[pcol[e]];
+  x[i] += s;
+}
+
+// coarsest: x = A^-1 b per problem (one CTA per problem)
+__global__ void k_amg_coarse_solve(const int32_t* __restrict__ crow0, const int32_t* __restrict__ coff,
+                                   const float* __restrict__ cinv, const float* __restrict__ b, float* __restrict__ x) {
+  const int P = blockIdx.x;
+  const int r0 = crow0[P], m = crow0[P + 1] - r0;
+  const float* A = cinv + coff[P];
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    float s = 0.f;
+    for (int j = 0; j < m; ++j) s += A[i * m + j] * b[r0 + j];
+    x[r0 + i] = s;
+  }
+}
+
+inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)std::max<int64_t>(1, (n + t - 1) / t); }
+
+template <int NT> void numeric_nt(hdg_system* s, const float* val0, cudaStream_t st) {
+  AmgHierarchy* H = s->amg;
+  const int nf = H->nf;
+  HDG_CUDA(cudaMemsetAsync(H->lam0.p, 0, sizeof(float) * std::max(s->nprob, 1), st));
+  k_amg_block_inv<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, s->d_kdiag.p, val0, H->face_prob.p, H->dinv0.p,
+                                                H->lam0.p);
+  k_amg_p0<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, H->agg0.p,
+                                         H->tent0.p, H->pcol0.p, H->pval0.p);
+  k_amg_ap0<NT><<<nblk((int64_t)nf * NT), 256, 0, st>>>(nf, H->wap, s->d_bcol5.p, val0, H->pcol0.p, H->pval0.p,
+                                                        H->apmap0.p, H->apval0.p);
+  AmgLevel& L1 = H->lev[0];
+  k_amg_rap0<NT><<<nblk(L1.n), 256, 0, st>>>(L1.n, H->wap, H->rptr0.p, H->rent0.p, H->pval0.p, H->apcol0.p,
+                                             H->apval0.p, L1.ptr.p, L1.col.p, L1.val.p);
+  s->ctx->launches += 4;
+  for (size_t l = 0; l < H->lev.size(); ++l) {
+    AmgLevel& L = H->lev[l];
+    k_amg_dl1<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.val.p, L.dl1inv.p);
+    s->ctx->launches++;
+    if (l + 1 == H->lev.size()) break;
+    AmgLevel& C = H->lev[l + 1];
+    k_amg_p<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.agg.p, L.tent.p, L.pptr.p,
+                                       L.pcol.p, L.pval.p);
+    k_amg_ap<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.pptr.p, L.pcol.p, L.pval.p, L.apptr.p,
+                                        L.apcol.p, L.apval.p);
+    k_amg_rap<<<nblk(C.n), 256, 0, st>>>(C.n, L.rptr.p, L.rent.p, L.rrow.p, L.pval.p, L.apptr.p, L.apcol.p,
+                                         L.apval.p, C.ptr.p, C.col.p, C.val.p);
+    s->ctx->launches += 3;
+  }
+  const AmgLevel& C = H->lev.back();
+  const size_t smem = sizeof(float) * ((size_t)H->cmax * 2 * H->cmax + H->cmax);
+  static bool attr = false;
+  if (!attr) {
+    HDG_CUDA(cudaFuncSetAttribute(k_amg_coarse_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr = true;
+  }
+  if (H->cmax > 0)
+    k_amg_coarse_inv<<<s->nprob, 256, smem, st>>>(H->crow0.p, H->coff.p, C.ptr.p, C.col.p, C.val.p, H->cinv.p);
+  s->ctx->launches++;
+  HDG_CUDA(cudaGetLastError());
+}
+
+template <int NT> void apply_nt(hdg_system* s, const float* val0, const float* b0, float* z0, cudaStream_t st) {
+  AmgHierarchy* H = s->amg;
+  const int nf = H->nf;
+  const int64_t n0 = (int64_t)nf * NT;
+  const int nl = (int)H->lev.size();
+  // level 0 pre-smoothing: two block-Jacobi sweeps (z0 <- x0 <- D^-1 b)
+  k_amg_face_smooth<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
+                                                  nullptr, H->x0.p, 1);
+  k_amg_face_smooth<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
+                                                  H->x0.p, z0, 0);
+  k_amg_face_residual<NT><<<nblk(n0), 256, 0, st>>>(nf, s->d_bcol5.p, val0, b0, z0, H->r0.p);
+  AmgLevel& L1 = H->lev[0];
+  k_amg_restrict0<NT><<<nblk(L1.n), 256, 0, st>>>(L1.n, H->rptr0.p, H->rent0.p, H->pval0.p, H->r0.p, L1.dl1inv.p,
+                                                  L1.b.p, L1.x.p);
+  int launches = 4;
+  // coarse levels down: x holds the first sweep (from the restriction); the second sweep goes to
+  // t, which then holds the level's iterate until the way up
+  for (int l = 0; l + 1 < nl; ++l) {
+    AmgLevel& L = H->lev[l];
+    AmgLevel& C = H->lev[l + 1];
+    k_amg_l1_sweep<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.x.p, L.t.p);
+    k_amg_residual<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.b.p, L.t.p, L.r.p);
+    const bool coarsest = (l + 2 == nl);
+    k_amg_restrict<<<nblk(C.n), 256, 0, st>>>(C.n, L.rptr.p, L.rent.p, L.rrow.p, L.pval.p, L.r.p,
+                                              coarsest ? nullptr : C.dl1inv.p, C.b.p, C.x.p);
+    launches += 3;
+  }
+  AmgLevel& C = H->lev.back();
+  if (H->cmax > 0) k_amg_coarse_solve<<<s->nprob, 128, 0, st>>>(H->crow0.p, H->coff.p, H->cinv.p, C.b.p, C.x.p);
+  ++launches;
+  // coarse levels up: the coarser level's result is in its x; prolongate into this level's
+  // iterate (t), then two sweeps t -> r -> x
+  for (int l = nl - 2; l >= 0; --l) {
+    AmgLevel& L = H->lev[l];
+    AmgLevel& Cn = H->lev[l + 1];
+    k_amg_prolong<<<nblk(L.n), 256, 0, st>>>(L.n, L.pptr.p, L.pcol.p, L.pval.p, Cn.x.p, L.t.p);
+    k_amg_l1_sweep<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.t.p, L.r.p);
+    k_amg_l1_sweep<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.r.p, L.x.p);
+    launches += 3;
+  }
+  // level 0 up: prolongate, two block-Jacobi sweeps
+  k_amg_prolong0<NT><<<nblk(n0), 256, 0, st>>>(nf, H->pcol0.p, H->pval0.p, L1.x.p, z0);
+  k_amg_face_smooth<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
+                                                  z0, H->x0.p, 0);
+  k_amg_face_smooth<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
+                                                  H->x0.p, z0, 0);
+  launches += 3;
+  (void)launches;  // counted by the caller per replay (amg_cycle_launches)
+}
+
+}  // namespace
+
+// The FP32 level-0 matrix: the system's FP32 copy when it has one, else a copy made here.
+const float* amg_level0_values(hdg_system* s, cudaStream_t st);
+
+void amg_setup_numeric(hdg_system* s, cudaStream_t st) {
+  const float* v0 = amg_level0_values(s, st);
+  switch (s->nt) {
+    case 2: numeric_nt<2>(s, v0, st); break;
+    case 3: numeric_nt<3>(s, v0, st); break;
+    case 4: numeric_nt<4>(s, v0, st); break;
+    case 5: numeric_nt<5>(s, v0, st); break;
+  }
+}
+
+// Algorithmic bytes of one V-cycle: every array a cycle kernel reads or writes, once (gathered
+// neighbour values are counted at their own row).  Level 0: the FP32 block-ELL values, block
+// columns, block inverses and vectors of the four matrix-touching sweeps (second pre-sweep,
+// residual, two post-sweeps), the first sweep, restriction and prolongation; coarse levels: their
+// CSR matrices and vectors in the same sweeps.
+double amg_cycle_bytes(const hdg_system* s) {
+  const AmgHierarchy* H = s->amg;
+  const double nf = H->nf, nt = H->nt, n0 = nf * nt, n1 = H->lev.empty() ? 0.0 : H->lev[0].n;
+  const double mat0 = 20.0 * nt * nt * nf + 20.0 * nf;  // FP32 values + block columns
+  const double dinv = 4.0 * nt * nt * nf;
+  double b = 8.0 * n0 + dinv;                              // first sweep: b, dinv -> x
+  b += 3.0 * (mat0 + dinv + 12.0 * n0);                    // second pre-sweep, two post-sweeps
+  b += mat0 + 12.0 * n0;                                   // residual
+  b += 24.0 * n0 + 20.0 * nf + 8.0 * n1;                   // restriction (P0 values, r) + first coarse sweep
+  b += 28.0 * n0 + 20.0 * nf + 4.0 * n1;                   // prolongation
+  const int nl = (int)H->lev.size();
+  for (int l = 0; l < nl; ++l) {
+    const double n = H->lev[l].n, nnz = (double)H->lev[l].h_col.size();
+    const double spmv = 8.0 * nnz + 4.0 * n;               // values + columns + row pointers
+    if (l + 1 == nl) {
+      b += 8.0 * n + 4.0 * H->cinv.n;                      // coarsest dense solve
+      break;
+    }
+    const double npc = (double)H->lev[l].h_col.size();      // P and P' sizes are comparable to A's
+    b += 3.0 * (spmv + 20.0 * n) + (spmv + 16.0 * n);      // three sweeps, one residual
+    b += 2.0 * (8.0 * npc + 12.0 * n);                      // restriction and prolongation
+  }
+  return b;
+}
+
+int amg_cycle_launches(const hdg_system* s) {
+  const int nl = (int)s->amg->lev.size();
+  return 4 + 3 * (nl - 1) + 1 + 3 * (nl - 1) + 3;
+}
+
+void amg_apply(hdg_system* s, const float* r, float* z, cudaStream_t st) {
+  const float* v0 = s->amg->val0f.p ? s->amg->val0f.p : s->d_valf.p;
+  switch (s->nt) {
+    case 2: apply_nt<2>(s, v0, r, z, st); break;
+    case 3: apply_nt<3>(s, v0, r, z, st); break;
+    case 4: apply_nt<4>(s, v0, r, z, st); break;
+    case 5: apply_nt<5>(s, v0, r, z, st); break;
+  }
+  HDG_CUDA(cudaGetLastError());
+}
+
+namespace {
+__global__ void k_amg_to_float(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    b[t] = (float)a[t];
+}
+}  // namespace
+
+const float* amg_level0_values(hdg_system* s, cudaStream_t st) {
+  AmgHierarchy* H = s->amg;
+  const int64_t nval = (int64_t)hdg_system::SLOTS * s->nt * s->nt * s->nf;
+  H->val0f.alloc((size_t)nval);
+  k_amg_to_float<<<(unsigned)std::min<int64_t>((nval + 255) / 256, 152 * 32), 256, 0, st>>>(nval, s->d_val.p,
+                                                                                            H->val0f.p);
+  HDG_CUDA(cudaGetLastError());
+  s->ctx->launches++;
+  return H->val0f.p;
+}

@@ -46,6 +46,7 @@ thread_local cudaStream_t g_alloc_stream = nullptr;
 
 hdg_system::~hdg_system() {
   if (cg) destroy_cg(cg);
+  if (amg) destroy_amg(amg);
 }
 
 extern "C" {
@@ -629,6 +630,15 @@ int hdg_apply_dirichlet(hdg_system* s, const int32_t* dofs, const double* vals, 
       if (dofs[k] < 1 || dofs[k] > s->ndofs) return fail(s->ctx, HDG_ERR_ARG, "prescribed dof out of range");
       d0[k] = dofs[k] - 1;
     }
+    // prescribed faces (all their dofs are prescribed together): the multigrid setup leaves them
+    // out of its aggregates; a new Dirichlet set invalidates the symbolic setup
+    std::vector<char> dir(s->nf, 0);
+    for (int k = 0; k < n; ++k) dir[d0[k] / s->nt] = 1;
+    if (dir != s->h_dir_face && s->amg) {
+      destroy_amg(s->amg);
+      s->amg = nullptr;
+    }
+    s->h_dir_face.swap(dir);
     if (s->ctx->profiling) s->ev_apply.start(s->ctx->stream);
     launch_apply_dirichlet(s, d0, v, s->ctx->stream);
     if (s->ctx->profiling) s->ev_apply.stop(s->ctx->stream);
@@ -639,13 +649,14 @@ int hdg_apply_dirichlet(hdg_system* s, const int32_t* dofs, const double* vals, 
 
 // ---------------------------------------------------------------- solve / recover
 static hdg_solver solver_defaults(const hdg_solver* o) {
-  hdg_solver d{1e-12, 100000, HDG_PREC_FP64, 32, 1e-5};
+  hdg_solver d{1e-12, 100000, HDG_PREC_FP64, 32, 1e-5, HDG_PRECOND_JACOBI};
   if (!o) return d;
   hdg_solver r = *o;
   if (!(r.tol > 0)) r.tol = d.tol;
   if (r.maxit <= 0) r.maxit = d.maxit;
   if (r.chunk <= 0) r.chunk = d.chunk;
   if (!(r.inner_tol > 0)) r.inner_tol = d.inner_tol;
+  if (r.preconditioner != HDG_PRECOND_AMG) r.preconditioner = HDG_PRECOND_JACOBI;
   return r;
 }
 
@@ -731,6 +742,7 @@ int hdg_system_timings(hdg_system* s, hdg_timings* out) {
       out->cg_b_bytes = s->prof_b_bytes / out->cg_samples;
     }
     out->cg_iterations = s->cg_iterations;
+    out->cg_bytes = s->prof_all_bytes;
     return HDG_OK;
   });
 }

@@ -29,6 +29,9 @@
 
 namespace {
 constexpr int CG_BLOCK = 256;
+// resident blocks per SM the iteration kernels are compiled for (at least the 4 segments of 1024
+// rows per SM that a large problem gets): 6 in FP32 (40 registers), 4 in FP64 (64 registers)
+template <typename T> constexpr int cg_min_blocks() { return sizeof(T) == sizeof(float) ? 6 : 4; }
 constexpr int SAMPLE_EVERY = 8;  // with profiling on, every 8th chunk runs un-graphed and timed
 constexpr int SC = 10;           // per problem: rz, rz_old, pq, rr, bb, tol2, alpha, beta, rr_true, -
 constexpr int ST = 4;            // per problem: status, iterations, maxit, refine flag
@@ -42,9 +45,11 @@ struct CgState {
   DevBuf<double> sc;
   DevBuf<int32_t> st;
   DevBuf<double> r, z, p, q, dinv;
-  DevBuf<float> rf, zf, pf, pf2, qf, dinvf;
+  DevBuf<float> rf, zf, pf, pf2, qf, dinvf, xh, xl;
+  DevBuf<float> r32, z32;  // multigrid preconditioner input / output
   cudaGraphExec_t graph64 = nullptr, graph32 = nullptr;
   int chunk64 = 0, chunk32 = 0;
+  bool graph_mg = false;  // graph64 holds the multigrid iteration
   int32_t* h_st = nullptr;  // pinned mirrors
   double* h_sc = nullptr;
   std::vector<double> rr_best;
@@ -76,6 +81,8 @@ template <typename T> struct CgArgs {
   T* p2;
   double* sc;
   int32_t* st;
+  float* xh;  // FP32 iteration: steps since the last refinement as a float-float pair (hi, lo)
+  float* xl;
 };
 
 // (A v)_row over the block-ELL layout: 5 block slots, values slot-major and row-contiguous.
@@ -104,6 +111,10 @@ template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_i
     const T rv = (T)bv;
     const T zv = a.dinv[row] * rv;
     a.x[row] = 0.0;
+    if (a.xh) {
+      a.xh[row] = 0.f;
+      a.xl[row] = 0.f;
+    }
     a.r[row] = rv;
     a.z[row] = zv;
     a.p[row] = T(0);
@@ -128,7 +139,7 @@ template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_i
 }
 
 // FP64 product kernel with the q recurrence (p, q in place)
-template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_a(CgArgs<T> a) {
+template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK, cg_min_blocks<T>()) k_cg_a(CgArgs<T> a) {
   const int P = a.g.seg_prob[blockIdx.x];
   // status and beta are loaded together (one round trip); beta is formed once by the reducing
   // block of the update kernel
@@ -139,23 +150,24 @@ template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_a
   double pq = 0.0;
   const int r0 = a.g.seg_row0[blockIdx.x], r1 = a.g.seg_row1[blockIdx.x];
   // four rows per thread in flight together (independent gathers and accumulation chains)
-  for (int base = r0 + threadIdx.x; base < r1; base += 4 * CG_BLOCK) {
-    double w[4];
+  constexpr int ROWS = 4;
+  for (int base = r0 + threadIdx.x; base < r1; base += ROWS * CG_BLOCK) {
+    double w[ROWS];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < ROWS; ++u) {
       const int row = min(base + u * CG_BLOCK, r1 - 1);
       w[u] = row_dot<NT>(a.bcol5, a.nf, a.val, row, a.z);
     }
-    T qo[4], po[4], zo[4];
+    T qo[ROWS], po[ROWS], zo[ROWS];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < ROWS; ++u) {
       const int row = min(base + u * CG_BLOCK, r1 - 1);
       qo[u] = a.q[row];
       po[u] = a.p[row];
       zo[u] = a.z[row];
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < ROWS; ++u) {
       const int row = base + u * CG_BLOCK;
       if (row < r1) {
         const T qn = (T)(w[u] + beta * (double)qo[u]);
@@ -178,7 +190,7 @@ template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_a
 // Low-precision product kernel: p_new = z + beta p_old formed on the fly for every column the row
 // touches, q = A p_new a fresh product; p_old / p_new alternate buffers (flip).  p.q is summed
 // in float-float arithmetic (FP32 pipe); only each thread's total is converted to FP64.
-template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_a_fresh(CgArgs<T> a, int flip) {
+template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK, cg_min_blocks<T>()) k_cg_a_fresh(CgArgs<T> a, int flip) {
   const int P = a.g.seg_prob[blockIdx.x];
   const int status = a.st[ST * P];
   const T bt = (T)a.sc[SC * P + 7];
@@ -213,34 +225,54 @@ template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_a
 
 // Update kernel.  In FP64 the dot products are FP64 FMAs; in the FP32 iteration they are summed
 // in float-float arithmetic (FP32 pipe) and only each thread's totals are converted to FP64.
-template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_b(CgArgs<T> a, int flip) {
+template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK, cg_min_blocks<T>()) k_cg_b(CgArgs<T> a, int flip) {
   const int P = a.g.seg_prob[blockIdx.x];
   const int status = a.st[ST * P];
   const double alpha = a.sc[SC * P + 6];
   if (status != 0) return;
   const T at = (T)alpha;
   const T* __restrict__ pcur = flip ? a.p2 : a.p;  // the direction the product kernel just wrote
+  // alpha as a float-float pair for the x update of the FP32 iteration
+  const float ah = (float)alpha, al = (float)(alpha - (double)ah);
   typename DotAcc<T>::type rz, rr;
   const int r0 = a.g.seg_row0[blockIdx.x], r1 = a.g.seg_row1[blockIdx.x];
-  // the loads of four rows are issued before any store (stores may alias the loads, so the
+  // the loads of ROWS rows are issued before any store (stores may alias the loads, so the
   // compiler would not hoist the next row's loads above them by itself)
-  for (int base = r0 + threadIdx.x; base < r1; base += 4 * CG_BLOCK) {
-    double xv[4];
-    T pv[4], rv[4], qv[4], dv[4];
+  constexpr int ROWS = 4;
+  for (int base = r0 + threadIdx.x; base < r1; base += ROWS * CG_BLOCK) {
+    T pv[ROWS], rv[ROWS], qv[ROWS], dv[ROWS];
+    double xv[ROWS];
+    float xhv[ROWS], xlv[ROWS];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < ROWS; ++u) {
       const int row = min(base + u * CG_BLOCK, r1 - 1);
-      xv[u] = a.x[row];
       pv[u] = pcur[row];
       rv[u] = a.r[row];
       qv[u] = a.q[row];
       dv[u] = a.dinv[row];
+      if constexpr (sizeof(T) == sizeof(double)) {
+        xv[u] = a.x[row];
+      } else {
+        xhv[u] = a.xh[row];
+        xlv[u] = a.xl[row];
+      }
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < ROWS; ++u) {
       const int row = base + u * CG_BLOCK;
       if (row < r1) {
-        a.x[row] = xv[u] + alpha * (double)pv[u];
+        if constexpr (sizeof(T) == sizeof(double)) {
+          a.x[row] = xv[u] + alpha * (double)pv[u];
+        } else {  // x += alpha p in float-float: exact ah*p, plus al*p, added with TwoSum
+          const float ph = __fmul_rn(ah, (float)pv[u]);
+          const float pe = __fmaf_rn(al, (float)pv[u], __fmaf_rn(ah, (float)pv[u], -ph));
+          FF xx;
+          xx.hi = xhv[u];
+          xx.lo = xlv[u];
+          xx.add2(ph, pe);
+          a.xh[row] = xx.hi;
+          a.xl[row] = xx.lo;
+        }
         const T rn = rv[u] - at * qv[u];
         const T zn = dv[u] * rn;
         a.r[row] = rn;
@@ -275,14 +307,127 @@ template <int NT, typename T> __global__ void __launch_bounds__(CG_BLOCK) k_cg_b
   }
 }
 
+// ---- multigrid-preconditioned iteration (FP64 CG, FP32 V-cycle) ---------------------------
+// One iteration: k_cg_a (q = A z + beta q, p, alpha) -> k_cg_b_mg (x, r, r32 = r, r.r, status)
+// -> V-cycle z32 = M^-1 r32 -> k_cg_c (z = z32, r.z, beta).
+
+// r = b, x = 0, r32 = b, b.b; z follows from the V-cycle and k_cg_c (mode 1).
+template <int NT> __global__ void __launch_bounds__(CG_BLOCK) k_cg_init_mg(CgArgs<double> a, float* r32) {
+  const int P = a.g.seg_prob[blockIdx.x];
+  double bb = 0.0;
+  for (int row = a.g.seg_row0[blockIdx.x] + threadIdx.x; row < a.g.seg_row1[blockIdx.x]; row += CG_BLOCK) {
+    const double bv = a.b[row];
+    a.x[row] = 0.0;
+    a.r[row] = bv;
+    r32[row] = (float)bv;
+    a.p[row] = 0.0;
+    a.q[row] = 0.0;
+    bb += bv * bv;
+  }
+  double s0;
+  if (seg_finish1<CG_BLOCK>(a.g, P, 0, bb, &s0) && threadIdx.x == 0) {
+    double* sc = a.sc + SC * P;
+    sc[3] = s0;
+    sc[4] = s0;
+    sc[6] = 0.0;
+    sc[7] = 0.0;
+    sc[8] = s0;
+    a.st[ST * P] = (s0 == 0.0) ? 1 : 0;
+    a.st[ST * P + 1] = 0;
+  }
+}
+
+// x += alpha p, r -= alpha q, r32 = r, r.r; convergence and breakdown decisions.
+template <int NT> __global__ void __launch_bounds__(CG_BLOCK, 4) k_cg_b_mg(CgArgs<double> a, float* r32) {
+  const int P = a.g.seg_prob[blockIdx.x];
+  const int status = a.st[ST * P];
+  const double alpha = a.sc[SC * P + 6];
+  if (status != 0) return;
+  double rr = 0.0;
+  const int r0 = a.g.seg_row0[blockIdx.x], r1 = a.g.seg_row1[blockIdx.x];
+  constexpr int ROWS = 4;
+  for (int base = r0 + threadIdx.x; base < r1; base += ROWS * CG_BLOCK) {
+    double xv[ROWS], pv[ROWS], rv[ROWS], qv[ROWS];
+#pragma unroll
+    for (int u = 0; u < ROWS; ++u) {
+      const int row = min(base + u * CG_BLOCK, r1 - 1);
+      xv[u] = a.x[row];
+      pv[u] = a.p[row];
+      rv[u] = a.r[row];
+      qv[u] = a.q[row];
+    }
+#pragma unroll
+    for (int u = 0; u < ROWS; ++u) {
+      const int row = base + u * CG_BLOCK;
+      if (row < r1) {
+        a.x[row] = xv[u] + alpha * pv[u];
+        const double rn = rv[u] - alpha * qv[u];
+        a.r[row] = rn;
+        r32[row] = (float)rn;
+        rr = fma(rn, rn, rr);
+      }
+    }
+  }
+  double s0;
+  if (seg_finish1<CG_BLOCK>(a.g, P, 1, rr, &s0) && threadIdx.x == 0) {
+    double* sc = a.sc + SC * P;
+    const double pq = sc[2], rr_prev = sc[3];
+    sc[3] = s0;
+    const int it = a.st[ST * P + 1] + 1;
+    a.st[ST * P + 1] = it;
+    int next = 0;
+    if (!(pq > 0.0) || !isfinite(s0)) {
+      next = (isfinite(s0) && rr_prev <= fmax(1e-24, 100.0 * sc[5]) * sc[4]) ? 1 : 3;
+    } else if (s0 <= sc[5] * sc[4]) {
+      next = 1;
+    } else if (it >= a.st[ST * P + 2]) {
+      next = 2;
+    }
+    a.st[ST * P] = next;
+  }
+}
+
+// z = z32 (FP64), r.z and beta.  mode 0: a regular iteration of the running problems (beta =
+// rz / rz_old); mode 1: a (re)start of the running problems (init) or of the problems whose
+// refine flag is set (restart), beta = 0.
+template <int NT> __global__ void __launch_bounds__(CG_BLOCK) k_cg_c(CgArgs<double> a, const float* z32, int mode,
+                                                                      int restart) {
+  const int P = a.g.seg_prob[blockIdx.x];
+  const int status = a.st[ST * P];
+  const int flag = a.st[ST * P + 3];
+  if (restart ? (flag == 0) : (status != 0)) return;
+  double rz = 0.0;
+  for (int row = a.g.seg_row0[blockIdx.x] + threadIdx.x; row < a.g.seg_row1[blockIdx.x]; row += CG_BLOCK) {
+    const double zv = (double)z32[row];
+    a.z[row] = zv;
+    rz = fma(a.r[row], zv, rz);
+  }
+  double s0;
+  if (seg_finish1<CG_BLOCK>(a.g, P, 2, rz, &s0) && threadIdx.x == 0) {
+    double* sc = a.sc + SC * P;
+    if (mode == 0) {
+      sc[1] = sc[0];
+      sc[0] = s0;
+      sc[7] = s0 / sc[1];
+    } else {
+      sc[0] = s0;
+      sc[1] = s0;
+      sc[7] = 0.0;
+    }
+  }
+}
+
 // True residual r = b - K x in FP64 (FP64 matrix) for the problems whose refine flag is set;
 // with `replace` it also replaces the Krylov residual: r = r_true, z = D^-1 r, rz and beta.
 // The search direction is kept (beta = rz_true / rz_old) unless the refine flag is 2 or the
 // true residual norm exceeds twice the recursive one, which then restarts the iteration (beta
 // 0, p = z).  In the FP32 iteration the latest direction is moved into p if it sits in p2, and
 // the next refinement is set to trigger once the recursive residual fell by DELTA.
+// With the multigrid preconditioner (r32 != NULL) the replacement writes r and its FP32 copy
+// only; the V-cycle and k_cg_c (restart) then form z, r.z and beta = 0.
 template <int NT, typename T>
-__global__ void __launch_bounds__(CG_BLOCK) k_cg_residual(CgArgs<T> a, const double* __restrict__ val64, int replace) {
+__global__ void __launch_bounds__(CG_BLOCK) k_cg_residual(CgArgs<T> a, const double* __restrict__ val64, int replace,
+                                                          float* r32) {
   const int P = a.g.seg_prob[blockIdx.x];
   if (a.st[ST * P + 3] == 0) return;
   const bool move_p = replace && a.p2 != a.p && a.sc[SC * P + 9] != 0.0;
@@ -290,7 +435,10 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_residual(CgArgs<T> a, const dou
   for (int row = a.g.seg_row0[blockIdx.x] + threadIdx.x; row < a.g.seg_row1[blockIdx.x]; row += CG_BLOCK) {
     const double rv = a.b[row] - row_dot<NT>(a.bcol5, a.nf, val64, row, a.x);
     rr += rv * rv;
-    if (replace) {
+    if (replace && r32) {
+      a.r[row] = (T)rv;
+      r32[row] = (float)rv;
+    } else if (replace) {
       const T rt = (T)rv;
       const T zt = a.dinv[row] * rt;
       a.r[row] = rt;
@@ -303,7 +451,9 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_residual(CgArgs<T> a, const dou
   if (seg_finish<CG_BLOCK>(a.g, P, 2, rz, rr, &s0, &s1) && threadIdx.x == 0) {
     double* sc = a.sc + SC * P;
     sc[8] = s1;
-    if (replace) {
+    if (replace && r32) {
+      sc[3] = s1;
+    } else if (replace) {
       const bool restart = a.st[ST * P + 1] == 0 || a.st[ST * P + 3] == 2 || s1 > 4.0 * sc[3];
       sc[0] = s0;
       sc[3] = s1;
@@ -311,6 +461,17 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_residual(CgArgs<T> a, const dou
       sc[9] = 0.0;
       if (a.p2 != a.p) sc[5] = DELTA * DELTA * s1 / sc[4];
     }
+  }
+}
+
+// FP32 iteration: x = x64 + (xh + xl), where the float-float pair holds the steps taken since the
+// last refinement.  Folding adds the pair to the FP64 x and clears it, so the pair only ever holds
+// a correction; its 2^-44 relative precision then limits the correction, not x itself.
+__global__ void k_x_fold(int64_t n, float* __restrict__ xh, float* __restrict__ xl, double* __restrict__ x) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    x[t] += (double)xh[t] + (double)xl[t];
+    xh[t] = 0.f;
+    xl[t] = 0.f;
   }
 }
 
@@ -334,6 +495,7 @@ template <int NT> struct SolverNT : CgSolver {
   cudaStream_t st;
   int nrow, nprob, chunk = 32;
   bool mixed = false;
+  bool mg = false;  // multigrid preconditioner (FP64 iteration)
   CgArgs<double> a64;
   CgArgs<float> a32;
   // Segment compaction: once most problems have finished, the launch grid is rebuilt from the
@@ -341,8 +503,9 @@ template <int NT> struct SolverNT : CgSolver {
   // would only return.  The full tables are restored when the solve ends.
   std::vector<int32_t> full_prob, full_r0, full_r1, full_b0, full_nb;
   int nseg_full = 0;
-  // Byte accounting of sampled chunks: iteration counts at the launch of the sampled chunk.
-  std::vector<int32_t> sample_it0;
+  // Byte accounting of sampled chunks: iteration counts at the launch of the sampled chunk; and of
+  // every chunk: iteration counts at the previous read-back.
+  std::vector<int32_t> sample_it0, it_prev;
   bool sample_pending = false;
 
   explicit SolverNT(hdg_system* s_) {
@@ -354,6 +517,8 @@ template <int NT> struct SolverNT : CgSolver {
     nprob = s->nprob;
   }
 
+  void set_stream(cudaStream_t stream) override { st = stream; }
+
   SegArgs seg() const {
     return SegArgs{s->d_seg_prob.p, s->d_seg_row0.p, s->d_seg_row1.p, s->d_prob_blk0.p, s->d_prob_nblk.p,
                    s->d_part.p, s->d_cnt.p};
@@ -362,7 +527,13 @@ template <int NT> struct SolverNT : CgSolver {
   template <typename T> void launch_pair(const CgArgs<T>& a, cudaStream_t stream, int it) {
     if constexpr (sizeof(T) == sizeof(double)) {
       k_cg_a<NT, T><<<s->nseg, CG_BLOCK, 0, stream>>>(a);
-      k_cg_b<NT, T><<<s->nseg, CG_BLOCK, 0, stream>>>(a, 0);
+      if (mg) {
+        k_cg_b_mg<NT><<<s->nseg, CG_BLOCK, 0, stream>>>(a, c->r32.p);
+        amg_apply(s, c->r32.p, c->z32.p, stream);
+        k_cg_c<NT><<<s->nseg, CG_BLOCK, 0, stream>>>(a, c->z32.p, 0, 0);
+      } else {
+        k_cg_b<NT, T><<<s->nseg, CG_BLOCK, 0, stream>>>(a, 0);
+      }
     } else {
       k_cg_a_fresh<NT, T><<<s->nseg, CG_BLOCK, 0, stream>>>(a, it & 1);
       k_cg_b<NT, T><<<s->nseg, CG_BLOCK, 0, stream>>>(a, (it & 1) ^ 1);
@@ -385,8 +556,10 @@ template <int NT> struct SolverNT : CgSolver {
   }
 
   void prepare(const hdg_solver& o) override {
-    mixed = (o.precision == HDG_PREC_MIXED);
+    mg = (o.preconditioner == HDG_PRECOND_AMG);
+    mixed = (o.precision == HDG_PREC_MIXED) && !mg;  // the multigrid iteration runs in FP64
     chunk = o.chunk > 1 ? (o.chunk + 1) / 2 * 2 : 2;  // even: the FP32 iteration alternates p buffers
+    if (mg) chunk = std::min(chunk, 8);  // a multigrid iteration is ~25 launches
     if (c->nprob != nprob || c->nrow != nrow) {
       c->sc.alloc((size_t)SC * nprob);
       c->st.alloc((size_t)ST * nprob);
@@ -414,8 +587,9 @@ template <int NT> struct SolverNT : CgSolver {
     for (auto* e : s->ev_cg_b) delete e;
     s->ev_cg_a.clear();
     s->ev_cg_b.clear();
-    s->prof_a_bytes = s->prof_b_bytes = 0.0;
+    s->prof_a_bytes = s->prof_b_bytes = s->prof_all_bytes = 0.0;
     sample_pending = false;
+    it_prev.assign(nprob, 0);
     if (s->ctx->profiling) s->ev_cg.start(st);
     // per-problem tolerance (mixed: the recursive residual only triggers a refinement) and cap
     for (int P = 0; P < nprob; ++P) {
@@ -428,12 +602,28 @@ template <int NT> struct SolverNT : CgSolver {
     }
     HDG_CUDA(cudaMemcpyAsync(c->sc.p, c->h_sc, sizeof(double) * SC * nprob, cudaMemcpyHostToDevice, st));
     HDG_CUDA(cudaMemcpyAsync(c->st.p, c->h_st, sizeof(int32_t) * ST * nprob, cudaMemcpyHostToDevice, st));
-    if (!mixed) {
+    if (mg) {
+      c->r.alloc(nrow); c->z.alloc(nrow); c->p.alloc(nrow); c->q.alloc(nrow); c->dinv.alloc(nrow);
+      c->r32.alloc(nrow); c->z32.alloc(nrow);
+      if (!s->amg) amg_setup_symbolic(s, s->h_dir_face);
+      amg_setup_numeric(s, st);
+      a64 = CgArgs<double>{seg(), s->d_bcol5.p, s->nf, s->d_val.p, s->d_b.p, c->dinv.p, s->d_x.p, c->r.p, c->z.p,
+                           c->p.p, c->q.p, c->p.p, c->sc.p, c->st.p, nullptr, nullptr};
+      k_cg_init_mg<NT><<<s->nseg, CG_BLOCK, 0, st>>>(a64, c->r32.p);
+      amg_apply(s, c->r32.p, c->z32.p, st);
+      k_cg_c<NT><<<s->nseg, CG_BLOCK, 0, st>>>(a64, c->z32.p, 1, 0);
+      if (c->graph64) { cudaGraphExecDestroy(c->graph64); c->graph64 = nullptr; }  // Jacobi and multigrid differ
+      c->chunk64 = 0;
+      build_graph<double>(a64, &c->graph64, &c->chunk64);
+      c->graph_mg = true;
+    } else if (!mixed) {
       c->r.alloc(nrow); c->z.alloc(nrow); c->p.alloc(nrow); c->q.alloc(nrow); c->dinv.alloc(nrow);
       k_dinv<NT, double><<<(nrow + 255) / 256, 256, 0, st>>>(nrow, s->d_kdiag.p, s->d_val.p, c->dinv.p);
       a64 = CgArgs<double>{seg(), s->d_bcol5.p, s->nf, s->d_val.p, s->d_b.p, c->dinv.p, s->d_x.p, c->r.p, c->z.p,
-                           c->p.p, c->q.p, c->p.p, c->sc.p, c->st.p};
+                           c->p.p, c->q.p, c->p.p, c->sc.p, c->st.p, nullptr, nullptr};
       k_cg_init<NT, double><<<s->nseg, CG_BLOCK, 0, st>>>(a64);
+      if (c->graph_mg && c->graph64) { cudaGraphExecDestroy(c->graph64); c->graph64 = nullptr; }
+      c->graph_mg = false;
       build_graph<double>(a64, &c->graph64, &c->chunk64);
     } else {
       const int64_t nval = (int64_t)hdg_system::SLOTS * NT * nrow;
@@ -441,10 +631,10 @@ template <int NT> struct SolverNT : CgSolver {
       k_to_float<<<(unsigned)std::min<int64_t>((nval + 255) / 256, 152 * 32), 256, 0, st>>>(nval, s->d_val.p,
                                                                                            s->d_valf.p);
       c->rf.alloc(nrow); c->zf.alloc(nrow); c->pf.alloc(nrow); c->pf2.alloc(nrow); c->qf.alloc(nrow);
-      c->dinvf.alloc(nrow);
+      c->dinvf.alloc(nrow); c->xh.alloc(nrow); c->xl.alloc(nrow);
       k_dinv<NT, float><<<(nrow + 255) / 256, 256, 0, st>>>(nrow, s->d_kdiag.p, s->d_val.p, c->dinvf.p);
       a32 = CgArgs<float>{seg(), s->d_bcol5.p, s->nf, s->d_valf.p, s->d_b.p, c->dinvf.p, s->d_x.p, c->rf.p, c->zf.p,
-                          c->pf.p, c->qf.p, c->pf2.p, c->sc.p, c->st.p};
+                          c->pf.p, c->qf.p, c->pf2.p, c->sc.p, c->st.p, c->xh.p, c->xl.p};
       k_cg_init<NT, float><<<s->nseg, CG_BLOCK, 0, st>>>(a32);
       build_graph<float>(a32, &c->graph32, &c->chunk32);
       s->ctx->launches++;
@@ -469,7 +659,17 @@ template <int NT> struct SolverNT : CgSolver {
         else k_cg_a_fresh<NT, T><<<s->nseg, CG_BLOCK, 0, st>>>(a, it & 1);
         ea->stop(st);
         eb->start(st);
-        k_cg_b<NT, T><<<s->nseg, CG_BLOCK, 0, st>>>(a, sizeof(T) == sizeof(double) ? 0 : ((it & 1) ^ 1));
+        if constexpr (sizeof(T) == sizeof(double)) {
+          if (mg) {  // the update, the V-cycle and the r.z kernel are timed together
+            k_cg_b_mg<NT><<<s->nseg, CG_BLOCK, 0, st>>>(a, c->r32.p);
+            amg_apply(s, c->r32.p, c->z32.p, st);
+            k_cg_c<NT><<<s->nseg, CG_BLOCK, 0, st>>>(a, c->z32.p, 0, 0);
+          } else {
+            k_cg_b<NT, T><<<s->nseg, CG_BLOCK, 0, st>>>(a, 0);
+          }
+        } else {
+          k_cg_b<NT, T><<<s->nseg, CG_BLOCK, 0, st>>>(a, (it & 1) ^ 1);
+        }
         eb->stop(st);
         s->ev_cg_a.push_back(ea);
         s->ev_cg_b.push_back(eb);
@@ -478,7 +678,7 @@ template <int NT> struct SolverNT : CgSolver {
     } else {
       HDG_CUDA(cudaGraphLaunch(graph, st));
     }
-    s->ctx->launches += 2 * chunk;
+    s->ctx->launches += (int64_t)chunk * (mg ? 3 + amg_cycle_launches(s) : 2);
   }
 
   void launch_chunk(int rep) override {
@@ -492,12 +692,28 @@ template <int NT> struct SolverNT : CgSolver {
   }
 
   // true residuals of the flagged problems (and replacement of their Krylov residual)
-  void residual(bool replace) {
-    HDG_CUDA(cudaMemcpyAsync(c->st.p, c->h_st, sizeof(int32_t) * ST * nprob, cudaMemcpyHostToDevice, st));
-    if (mixed) k_cg_residual<NT, float><<<s->nseg, CG_BLOCK, 0, st>>>(a32, s->d_val.p, replace ? 1 : 0);
-    else k_cg_residual<NT, double><<<s->nseg, CG_BLOCK, 0, st>>>(a64, s->d_val.p, replace ? 1 : 0);
+  // FP64 x: fold the float-float steps of the FP32 iteration into it
+  void x_to_double() {
+    k_x_fold<<<(unsigned)std::min<int64_t>((nrow + 255) / 256, 152 * 16), 256, 0, st>>>(nrow, c->xh.p, c->xl.p,
+                                                                                        s->d_x.p);
     HDG_CUDA(cudaGetLastError());
     s->ctx->launches++;
+  }
+
+  void residual(bool replace) {
+    HDG_CUDA(cudaMemcpyAsync(c->st.p, c->h_st, sizeof(int32_t) * ST * nprob, cudaMemcpyHostToDevice, st));
+    if (mixed) x_to_double();
+    if (mixed) k_cg_residual<NT, float><<<s->nseg, CG_BLOCK, 0, st>>>(a32, s->d_val.p, replace ? 1 : 0, nullptr);
+    else k_cg_residual<NT, double><<<s->nseg, CG_BLOCK, 0, st>>>(a64, s->d_val.p, replace ? 1 : 0,
+                                                                 mg ? c->r32.p : nullptr);
+    HDG_CUDA(cudaGetLastError());
+    s->ctx->launches++;
+    if (mg && replace) {  // z for the replaced residuals, and a restart (beta = 0) of those problems
+      amg_apply(s, c->r32.p, c->z32.p, st);
+      k_cg_c<NT><<<s->nseg, CG_BLOCK, 0, st>>>(a64, c->z32.p, 1, 1);
+      HDG_CUDA(cudaGetLastError());
+      s->ctx->launches++;
+    }
     HDG_CUDA(cudaMemcpyAsync(c->h_sc, c->sc.p, sizeof(double) * SC * nprob, cudaMemcpyDeviceToHost, st));
     HDG_CUDA(cudaStreamSynchronize(st));
   }
@@ -539,9 +755,22 @@ template <int NT> struct SolverNT : CgSolver {
   // the block columns (5 per face), and each vector element read or written once; gathered
   // neighbour values are counted once, at their own row.
   double bytes_per_row_a() const { return mixed ? 20.0 * NT + 20.0 / NT + 16.0 : 40.0 * NT + 20.0 / NT + 40.0; }
-  double bytes_per_row_b() const { return mixed ? 40.0 : 64.0; }
+  // the multigrid "update" is k_cg_b_mg (x, p, r r/w, q, r32) + the V-cycle + k_cg_c (z32, z, r)
+  double bytes_per_row_b() const {
+    if (mg) return 52.0 + 20.0 + amg_cycle_bytes(s) / (double)nrow;
+    return mixed ? 40.0 : 64.0;
+  }
 
   void account_sample() {
+    // all launches: rows x iterations since the previous read-back
+    if ((int)it_prev.size() != nprob) it_prev.assign(nprob, 0);
+    double rows_all = 0.0;
+    for (int P = 0; P < nprob; ++P) {
+      const int32_t now = c->h_st[ST * P + 1];
+      rows_all += (double)(now - it_prev[P]) * (double)(s->h_prob_row0[P + 1] - s->h_prob_row0[P]);
+      it_prev[P] = now;
+    }
+    s->prof_all_bytes += rows_all * (bytes_per_row_a() + bytes_per_row_b());
     if (!sample_pending) return;
     sample_pending = false;
     double rows_it = 0.0;
@@ -621,6 +850,7 @@ template <int NT> struct SolverNT : CgSolver {
   void finish(const hdg_solver& o, std::vector<hdg_stats>* out) override {
     (void)o;
     if (s->nseg != nseg_full) set_segments(true);  // restore the full tables (other kernels use them)
+    if (mixed) x_to_double();
     if (!mixed) {  // report the true FP64 residual of every problem
       for (int P = 0; P < nprob; ++P) c->h_st[ST * P + 3] = 1;
       residual(false);
@@ -671,6 +901,44 @@ int run_solve_many(const std::vector<hdg_system*>& sys, const hdg_solver& o,
   } guard{sv};
   for (auto* s : sys) sv.push_back(make_cg_solver(s));
   for (auto* x : sv) x->prepare(o);
+  // Several systems (degree bins) iterate on streams of their own, forked from and joined back
+  // to the context's stream, so that one bin's reduction tails and chunk boundaries overlap
+  // with the other bins' work.  Every system allocated its buffers in prepare, before the fork.
+  struct Fork {
+    std::vector<cudaStream_t> streams;
+    std::vector<cudaEvent_t> events;
+    cudaStream_t home = nullptr;
+    ~Fork() {
+      for (size_t i = 0; i < streams.size(); ++i) {
+        cudaEventRecord(events[i], streams[i]);
+        cudaStreamWaitEvent(home, events[i], 0);
+      }
+      for (auto e : events) cudaEventDestroy(e);
+      for (auto q : streams) cudaStreamDestroy(q);
+    }
+  } fork;
+  if (sv.size() > 1) {
+    fork.home = sys[0]->ctx->stream;
+    cudaEvent_t start;
+    HDG_CUDA(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
+    for (auto* s : sys)
+      if (s->ctx->stream != fork.home) {
+        HDG_CUDA(cudaEventRecord(start, s->ctx->stream));
+        HDG_CUDA(cudaStreamWaitEvent(fork.home, start, 0));
+      }
+    HDG_CUDA(cudaEventRecord(start, fork.home));
+    for (auto* x : sv) {
+      cudaStream_t q;
+      cudaEvent_t e;
+      HDG_CUDA(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
+      fork.streams.push_back(q);
+      HDG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      fork.events.push_back(e);
+      HDG_CUDA(cudaStreamWaitEvent(q, start, 0));
+      x->set_stream(q);
+    }
+    HDG_CUDA(cudaEventDestroy(start));
+  }
   std::vector<char> done(sv.size(), 0);
   for (int rep = 0;; ++rep) {
     bool all = true;
@@ -682,7 +950,7 @@ int run_solve_many(const std::vector<hdg_system*>& sys, const hdg_solver& o,
       }
     if (all) break;
     for (size_t i = 0; i < sv.size(); ++i)
-      if (!done[i]) HDG_CUDA(cudaStreamSynchronize(sv[i]->s->ctx->stream));
+      if (!done[i]) HDG_CUDA(cudaStreamSynchronize(fork.streams.empty() ? sv[i]->s->ctx->stream : fork.streams[i]));
     for (size_t i = 0; i < sv.size(); ++i)
       if (!done[i] && sv[i]->process(o)) done[i] = 1;
   }

@@ -12,6 +12,10 @@
 //   4. forms [Ate | bte] = [Ee;Fe]' X - [He | 0] through the factorised form of Ee and Fe
 //      (Ee = wn_f (x) F_{f,o}, Fe = tau |e_f| F_{f,o}), with bte = -[Ee;Fe]' b_e (:172,:174).
 // Outputs per cell: AB = [Ate | bte] (m x (m+1)) and KB = [K_e | b_e] (n x (m+1)), row-major.
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <cstdlib>
 #include "hdg_device.cuh"
 
 namespace {
@@ -31,9 +35,9 @@ struct ElemArgs {
   int* err;
 };
 
-constexpr int EWARPS = 4;
-
-template <int P> __global__ void __launch_bounds__(EWARPS * 32) k_element_condense(ElemArgs a) {
+// One warp per cell; EWARPS warps (cells) per CTA, picked per degree, quadrature size and mesh
+// size by the launch-time autotuner below.
+template <int P, int EWARPS> __global__ void __launch_bounds__(EWARPS * 32) k_element_condense(ElemArgs a) {
   using D = Dims<P>;
   constexpr int NW = D::NW, NT = D::NT, NV = D::NV, N = D::N, M = D::M, NC = D::NC, LD = D::LD;
   extern __shared__ double smem[];
@@ -241,27 +245,99 @@ template <int P> __global__ void __launch_bounds__(EWARPS * 32) k_element_conden
   }
 }
 
-template <int P> void launch_p(hdg_system* s, cudaStream_t st, const ElemArgs& a) {
+template <int P, int EWARPS> size_t smem_bytes(const ElemArgs& a) {
   using D = Dims<P>;
-  const int nq = a.nq;
-  const int wstride = D::N * D::LD + 2 * nq + D::NW + D::N + 2;
-  size_t smem = (size_t)(((a.ref_len + 1) & ~1) + EWARPS * wstride) * sizeof(double);
+  const int wstride = D::N * D::LD + 2 * a.nq + D::NW + D::N + 2;
+  return (size_t)(((a.ref_len + 1) & ~1) + EWARPS * wstride) * sizeof(double);
+}
+
+constexpr size_t ELEM_SMEM_MAX = 200 * 1024;
+
+// Launches the kernel with EWARPS warps per CTA and a grid of `oversub` x the resident CTAs
+// (a grid-stride loop covers the rest).  Returns false when the configuration does not fit.
+template <int P, int EWARPS> bool launch_pw(hdg_system* s, cudaStream_t st, const ElemArgs& a, int oversub) {
+  const size_t smem = smem_bytes<P, EWARPS>(a);
+  if (smem > ELEM_SMEM_MAX) return false;
   static bool attr_set = false;
   if (!attr_set) {
-    HDG_CUDA(cudaFuncSetAttribute(k_element_condense<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    HDG_CUDA(cudaFuncSetAttribute(k_element_condense<P, EWARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)ELEM_SMEM_MAX));
     attr_set = true;
   }
   int dev_sms = 152;
   cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, s->ctx->device);
   int blocks_per_sm = 0;
-  HDG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_element_condense<P>, EWARPS * 32, smem));
-  if (blocks_per_sm < 1) blocks_per_sm = 1;
-  long need = (a.nc + EWARPS - 1) / EWARPS;
-  long grid = std::min<long>(need, (long)dev_sms * blocks_per_sm * 4);
+  HDG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_element_condense<P, EWARPS>, EWARPS * 32,
+                                                         smem));
+  if (blocks_per_sm < 1) return false;
+  const long need = (a.nc + EWARPS - 1) / EWARPS;
+  long grid = std::min<long>(need, (long)dev_sms * blocks_per_sm * oversub);
   if (grid < 1) grid = 1;
-  k_element_condense<P><<<(unsigned)grid, EWARPS * 32, smem, st>>>(a);
+  k_element_condense<P, EWARPS><<<(unsigned)grid, EWARPS * 32, smem, st>>>(a);
   HDG_CUDA(cudaGetLastError());
   s->ctx->launches++;
+  return true;
+}
+
+template <int P> bool launch_cfg(hdg_system* s, cudaStream_t st, const ElemArgs& a, int warps, int oversub) {
+  switch (warps) {
+    case 1: return launch_pw<P, 1>(s, st, a, oversub);
+    case 2: return launch_pw<P, 2>(s, st, a, oversub);
+    case 4: return launch_pw<P, 4>(s, st, a, oversub);
+    case 8: return launch_pw<P, 8>(s, st, a, oversub);
+  }
+  return false;
+}
+
+// Autotuner: the first launch for a (device, degree, quadrature size, log2 of the cell count)
+// times every (warps per CTA, grid oversubscription) pair on the real inputs (the kernel only
+// writes its outputs from its inputs, and every configuration computes each cell with the same
+// instruction sequence, so the results are bit-identical) and keeps the fastest.  The choice is
+// cached for the process.  HDG_ELEMENT_WARPS=<1|2|4|8> fixes the warps per CTA instead.
+template <int P> void launch_p(hdg_system* s, cudaStream_t st, const ElemArgs& a) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int>, std::pair<int, int>> best;
+  if (const char* env = std::getenv("HDG_ELEMENT_WARPS")) {
+    if (!launch_cfg<P>(s, st, a, std::atoi(env), 4)) throw HdgError{HDG_ERR_ARG, "HDG_ELEMENT_WARPS does not fit"};
+    return;
+  }
+  int lg = 0;
+  while ((1L << (lg + 1)) <= (long)a.nc) ++lg;
+  const auto key = std::make_tuple(s->ctx->device, a.nq, lg);
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = best.find(key);
+    if (it != best.end()) {
+      launch_cfg<P>(s, st, a, it->second.first, it->second.second);
+      return;
+    }
+  }
+  float best_ms = 1e30f;
+  std::pair<int, int> pick{4, 4};
+  cudaEvent_t e0, e1;
+  HDG_CUDA(cudaEventCreate(&e0));
+  HDG_CUDA(cudaEventCreate(&e1));
+  for (int w : {1, 2, 4, 8})
+    for (int g : {1, 4}) {
+      if (!launch_cfg<P>(s, st, a, w, g)) continue;  // warm-up launch of this configuration
+      HDG_CUDA(cudaEventRecord(e0, st));
+      launch_cfg<P>(s, st, a, w, g);
+      HDG_CUDA(cudaEventRecord(e1, st));
+      HDG_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      HDG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best_ms) {
+        best_ms = ms;
+        pick = {w, g};
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    best[key] = pick;
+  }
+  launch_cfg<P>(s, st, a, pick.first, pick.second);
 }
 
 }  // namespace

@@ -190,14 +190,13 @@ __device__ __forceinline__ void block_sum_lean(const FF (&v)[NV], double (&out)[
 }
 
 // Cross-block stage: the block's partials (valid in thread 0) go to part[], and the last block of
-// the problem adds the problem's partials in block order (lanes over strided partials, then one
-// shuffle tree per value).  Returns true in every thread of that last block; the sums are valid
-// in its thread 0.
+// the problem adds the problem's partials (each thread its strided share, then a block sum, in a
+// fixed order).  Returns true in every thread of that last block; the sums are valid in its
+// thread 0.
 template <int BLOCK, int NV>
 __device__ __forceinline__ bool seg_combine(const SegArgs& g, int P, int slot, const double (&bp)[NV],
                                             double (&sum)[NV]) {
   __shared__ bool last;
-  __shared__ double fin[NV];
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int i = 0; i < NV; ++i) g.part[2 * blockIdx.x + i] = bp[i];
@@ -209,17 +208,17 @@ __device__ __forceinline__ bool seg_combine(const SegArgs& g, int P, int slot, c
   if (!last) return false;
   __threadfence();
   const int b0 = g.prob_blk0[P], nb = g.prob_nblk[P];
-  if (threadIdx.x < 32 * NV) {
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    double s = 0.0;
-    for (int k = l; k < nb; k += 32) s += ((volatile double*)g.part)[2 * (b0 + k) + w];
-    s = warp_sum(s);
-    if (l == 0) fin[w] = s;
-  }
-  __syncthreads();
+  double s[NV];
+#pragma unroll
+  for (int i = 0; i < NV; ++i) s[i] = 0.0;
+  for (int k = threadIdx.x; k < nb; k += BLOCK)  // every thread loads its strided partials
+#pragma unroll
+    for (int i = 0; i < NV; ++i) s[i] += ((volatile double*)g.part)[2 * (b0 + k) + i];
+  double tot[NV];
+  block_sum_lean<BLOCK, NV>(s, tot);
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int i = 0; i < NV; ++i) sum[i] = fin[i];
+    for (int i = 0; i < NV; ++i) sum[i] = tot[i];
     g.cnt[4 * P + slot] = 0;
   }
   return true;

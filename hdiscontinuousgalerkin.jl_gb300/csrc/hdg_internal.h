@@ -37,6 +37,21 @@ template <class T> struct DevBuf {
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n), s(o.s) {
+    o.p = nullptr;
+    o.n = 0;
+  }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) {
+      release();
+      p = o.p;
+      n = o.n;
+      s = o.s;
+      o.p = nullptr;
+      o.n = 0;
+    }
+    return *this;
+  }
   ~DevBuf() { release(); }
   void release() {
     if (p) cudaFreeAsync(p, s);
@@ -185,7 +200,8 @@ struct hdg_space {
   DevBuf<float> d_reff;
 };
 
-struct CgState;  // cg.cu
+struct CgState;       // cg.cu
+struct AmgHierarchy;  // amg.cu
 
 struct hdg_system {
   hdg_space* space = nullptr;
@@ -252,6 +268,7 @@ struct hdg_system {
   std::vector<EventPair*> ev_cg_a, ev_cg_b;
   // algorithmic bytes moved by the sampled CG launches (rows of the problems that iterated)
   double prof_a_bytes = 0.0, prof_b_bytes = 0.0;
+  double prof_all_bytes = 0.0;  // algorithmic bytes of every iteration launch of the last solve
   int cg_iterations = 0;
   double mdiag = 0.0;
   // solution and recovery
@@ -259,6 +276,8 @@ struct hdg_system {
   DevBuf<double> d_qu;  // [nc][n] recovered (q; u)
   bool have_solution = false, have_recovery = false;
   CgState* cg = nullptr;
+  AmgHierarchy* amg = nullptr;      // multigrid preconditioner (symbolic part kept across reassembly)
+  std::vector<char> h_dir_face;     // faces whose dofs apply! prescribed (set by hdg_apply_dirichlet)
   ~hdg_system();
   // partials: 2 per segment; tickets: 4 per problem (CG product, CG update, residual, meandiag)
   void ensure_reduction_buffers() {
@@ -289,6 +308,7 @@ struct CgSolver {
   virtual void enqueue_status_copy() = 0;             // enqueue the per-problem status read-back
   virtual bool process(const hdg_solver& o) = 0;      // after the read-back: true when all problems are done
   virtual void finish(const hdg_solver& o, std::vector<hdg_stats>* out) = 0;
+  virtual void set_stream(cudaStream_t stream) = 0;   // stream of the iteration (after prepare)
   hdg_system* s = nullptr;
 };
 CgSolver* make_cg_solver(hdg_system* s);
@@ -296,6 +316,12 @@ void mesh_concat(hdg_mesh* out, const std::vector<const hdg_mesh*>& parts);
 void launch_recover(hdg_system* s, cudaStream_t st);
 double run_errornorm(hdg_system* s, const FieldSpec& uex, cudaStream_t st);
 void destroy_cg(CgState* c);
+void destroy_amg(AmgHierarchy* h);
+void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face);
+void amg_setup_numeric(hdg_system* s, cudaStream_t st);
+void amg_apply(hdg_system* s, const float* r, float* z, cudaStream_t st);  // z = M^-1 r (FP32)
+int amg_cycle_launches(const hdg_system* s);                             // kernels per V-cycle
+double amg_cycle_bytes(const hdg_system* s);                             // algorithmic bytes per V-cycle
 
 void mesh_build_rectangle(hdg_mesh* m, int nx, int ny, const double LL[2], const double UR[2]);
 int mesh_build_from_cells(hdg_mesh* m, int nnodes, const double* xy, int ncells, const int32_t* cells1, int nedges,

@@ -208,11 +208,12 @@ int hdg_engine_create(hdg_ctx* ctx, double hbm_budget_gb, int max_batch, int max
     e->budget = hbm_budget_gb * 1e9;
     e->max_batch = max_batch;
     e->max_flights = max_flights;
-    hdg_solver d{1e-10, 100000, HDG_PREC_MIXED, 32, 1e-5};
+    hdg_solver d{1e-10, 100000, HDG_PREC_MIXED, 32, 1e-5, HDG_PRECOND_JACOBI};
     e->solver = opts ? *opts : d;
     if (!(e->solver.tol > 0)) e->solver.tol = d.tol;
     if (e->solver.maxit <= 0) e->solver.maxit = d.maxit;
     if (e->solver.chunk <= 0) e->solver.chunk = d.chunk;
+    if (e->solver.preconditioner != HDG_PRECOND_AMG) e->solver.preconditioner = HDG_PRECOND_JACOBI;
     e->streams.resize(max_flights);
     e->stream_busy.assign(max_flights, 0);
     for (auto& s : e->streams) HDG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));

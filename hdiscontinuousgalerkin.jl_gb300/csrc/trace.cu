@@ -13,6 +13,8 @@
 // row-contiguous, so every warp-wide load of the matrix in the CG is one contiguous segment.
 #include <algorithm>
 
+#include <numeric>
+
 #include "hdg_device.cuh"
 
 void build_block_structure(hdg_system* s) {
@@ -76,17 +78,36 @@ void build_block_structure(hdg_system* s) {
 // Segments of the row-parallel kernels: every problem's trace rows are cut into ranges of at most
 // SEG_ROWS rows, one CUDA block each, so a block never spans two problems.
 void build_segments(hdg_system* s) {
-  constexpr int SEG_ROWS = 1024;  // 4 rows per thread (interleaved in the CG kernels for ILP)
+  // About 1024 rows per segment (four per thread in the CG kernels).  Once the segments can fill
+  // the GPU, their number is rounded up to a multiple of the SM count (the extra segments go to
+  // the largest problems), so that every SM gets the same number of equal blocks.
+  constexpr int SEG_ROWS = 1024, NUM_SM = 152;
   const hdg_mesh* m = s->space->mesh;
   s->nprob = m->nprob;
   s->h_prob_row0.assign(s->nprob + 1, 0);
   std::vector<int32_t> sp, r0, r1, b0(s->nprob), nb(s->nprob), rowp((size_t)s->ndofs);
+  std::vector<int> nseg(s->nprob);
+  int64_t total = 0;
   for (int P = 0; P < s->nprob; ++P) {
-    const int a = m->prob_face0[P] * s->nt, e = m->prob_face0[P + 1] * s->nt;
-    s->h_prob_row0[P] = a;
-    s->h_prob_row0[P + 1] = e;
+    s->h_prob_row0[P] = m->prob_face0[P] * s->nt;
+    s->h_prob_row0[P + 1] = m->prob_face0[P + 1] * s->nt;
+    const int rows = std::max(s->h_prob_row0[P + 1] - s->h_prob_row0[P], 1);
+    nseg[P] = (rows + SEG_ROWS - 1) / SEG_ROWS;
+    total += nseg[P];
+  }
+  if (total >= NUM_SM) {
+    int64_t extra = (NUM_SM - total % NUM_SM) % NUM_SM;
+    std::vector<int> order(s->nprob);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+      return s->h_prob_row0[x + 1] - s->h_prob_row0[x] > s->h_prob_row0[y + 1] - s->h_prob_row0[y];
+    });
+    for (size_t k = 0; extra > 0; k = (k + 1) % order.size(), --extra) ++nseg[order[k]];
+  }
+  for (int P = 0; P < s->nprob; ++P) {
+    const int a = s->h_prob_row0[P], e = s->h_prob_row0[P + 1];
     const int rows = std::max(e - a, 1);
-    const int n = std::max(1, std::min((rows + SEG_ROWS - 1) / SEG_ROWS, 1216));
+    const int n = std::min(nseg[P], rows);
     const int per = (rows + n - 1) / n;
     b0[P] = (int32_t)sp.size();
     nb[P] = n;

@@ -19,9 +19,9 @@ from .fields import as_field
 
 class Engine:
     def __init__(self, ctx, hbm_budget_gb=32.0, max_batch=64, max_flights=8, tol=1e-10,
-                 precision=L.PREC_MIXED, chunk=32, maxit=100000, keep_results=True):
+                 precision=L.PREC_MIXED, chunk=32, maxit=100000, keep_results=True, preconditioner=L.PRECOND_JACOBI):
         self.ctx = ctx
-        o = L.hdg_solver(float(tol), int(maxit), int(precision), int(chunk), 1e-5)
+        o = L.hdg_solver(float(tol), int(maxit), int(precision), int(chunk), 1e-5, int(preconditioner))
         h = C.c_void_p()
         L.check(L.load().hdg_engine_create(ctx.handle, float(hbm_budget_gb), int(max_batch), int(max_flights),
                                            C.byref(o), C.byref(h)), ctx.handle)

@@ -116,9 +116,11 @@ class TraceSystem:
         d, v = L.i32(dofs), L.f64(vals)
         L.check(L.load().hdg_apply_dirichlet(self._h, L.i32ptr(d), L.dptr(v), len(d)), self.ctx)
 
-    def solve(self, tol=1e-12, maxit=100000, precision=None, chunk=32, inner_tol=1e-5, to_host=True):
+    def solve(self, tol=1e-12, maxit=100000, precision=None, chunk=32, inner_tol=1e-5, to_host=True,
+              preconditioner=L.PRECOND_JACOBI):
+        """K \\ b by preconditioned CG (Jacobi, or the multigrid V-cycle with preconditioner=PRECOND_AMG)."""
         o = L.hdg_solver(float(tol), int(maxit), int(self.precision if precision is None else precision), int(chunk),
-                         float(inner_tol))
+                         float(inner_tol), int(preconditioner))
         st = L.hdg_stats()
         out = np.zeros(self.ndofs) if to_host else None
         L.check(L.load().hdg_solve(self._h, C.byref(o), L.dptr(out), C.byref(st)), self.ctx)
@@ -273,7 +275,7 @@ class CellIterator:
 
 
 def solve_poisson(mesh, p: int, f, tau: float = 1.0, kappa=None, kappa_cell=None, faceset="boundary", g=None,
-                  quad_degree=None, precision=L.PREC_FP64, tol=1e-12, maxit=100000):
+                  quad_degree=None, precision=L.PREC_FP64, tol=1e-12, maxit=100000, preconditioner=L.PRECOND_JACOBI):
     """The whole poisson2D_HDG flow in one C-ABI call (hdg_solve_poisson); returns (uhat, q, u, stats)."""
     from .spaces import GenericFiniteElement, Dubiner, _handle
     sp = _handle(mesh, p, quad_degree if quad_degree is not None else p + 1)
@@ -281,7 +283,7 @@ def solve_poisson(mesh, p: int, f, tau: float = 1.0, kappa=None, kappa_cell=None
     fc, gc = f.as_c(), g.as_c()
     kc = kappa.as_c() if kappa is not None else None
     kk = L.f64(kappa_cell) if kappa_cell is not None else None
-    o = L.hdg_solver(float(tol), int(maxit), int(precision), 32, 1e-5)
+    o = L.hdg_solver(float(tol), int(maxit), int(precision), 32, 1e-5, int(preconditioner))
     st = L.hdg_stats()
     nd = mesh.nfaces * sp.nt
     uhat, q, u = np.zeros(nd), np.zeros((mesh.ncells, sp.nv)), np.zeros((mesh.ncells, sp.nw))

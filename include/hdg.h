@@ -159,12 +159,18 @@ int hdg_dirichlet(const hdg_space* space, const char* faceset, const hdg_field* 
 int hdg_apply_dirichlet(hdg_system* sys, const int32_t* dofs, const double* vals, int n);
 
 /* ---- solve --------------------------------------------------------------------------- */
+/* Preconditioner of the trace CG. */
+enum {
+  HDG_PRECOND_JACOBI = 0, /* diagonal (the default) */
+  HDG_PRECOND_AMG = 1     /* smoothed-aggregation multigrid V(2,2) cycle in FP32 (CG itself in FP64) */
+};
 typedef struct {
   double tol;         /* relative residual |r|/|b| to reach (default 1e-12) */
   int maxit;          /* iteration cap (default 100000) */
-  int precision;      /* HDG_PREC_FP64: Jacobi-PCG in FP64; HDG_PREC_MIXED: FP32 inner PCG + FP64 refinement */
+  int precision;      /* HDG_PREC_FP64: Jacobi-PCG in FP64; HDG_PREC_MIXED: FP32 iteration + FP64 refinement */
   int chunk;          /* CG iterations per CUDA-graph launch between convergence checks (default 32) */
-  double inner_tol;   /* mixed only: relative reduction per inner solve (default 1e-5) */
+  double inner_tol;   /* unused (kept for the layout of earlier callers) */
+  int preconditioner; /* HDG_PRECOND_*; with AMG the CG runs in FP64 whatever `precision` says */
 } hdg_solver;
 typedef struct {
   int iterations;     /* inner CG iterations in total */
@@ -211,6 +217,7 @@ typedef struct {
   double recover_ms;   /* last recovery */
   double cg_a_bytes;   /* mean algorithmic bytes of a sampled product-kernel launch (rows that iterated) */
   double cg_b_bytes;   /* mean algorithmic bytes of a sampled update-kernel launch */
+  double cg_bytes;     /* algorithmic bytes of all iteration launches of the last solve */
 } hdg_timings;
 /* Per-phase device times recorded while profiling was on (0 where nothing was recorded). */
 int hdg_system_timings(hdg_system* sys, hdg_timings* out);

@@ -257,3 +257,57 @@ def test_serving_same_alone_and_in_mix(H):
         alone = serve([i], resident=False)[i]
         for a, b in zip(mix[i], alone):
             assert rel(a, b) < 1e-8, i
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,p,qd,var", [(10, 1, None, False), (16, 2, None, True), (12, 3, 6, True), (8, 4, 9, True)])
+def test_multigrid_solution_matches_oracle(H, oracle, n, p, qd, var):
+    """The multigrid-preconditioned CG (FP64 CG, FP32 smoothed-aggregation V-cycle) reaches the
+    same trace solution as the oracle's direct solve, in fewer iterations than Jacobi-PCG."""
+    rng = np.random.default_rng(n * 10 + p)
+    kc = np.exp(rng.uniform(np.log(1e-2), np.log(1e2), 2 * n * n)) if var else None
+    f = H.Field.bumps(rng.random((8, 2)), 0.1 + 0.1 * rng.random(8), rng.standard_normal(8))
+    pr = H.Problem(n=n, p=p, f=f, kappa_cell=kc, jitter=0.2 if var else 0.0, seed=3)
+    hm = H.batch.host_mesh(pr)
+    mesh = H.rectangle_mesh(H.TriangleCell, (n, n), (0.0, 0.0), (1.0, 1.0))
+    mesh.set_coordinates(hm._topology()[0])
+    q_deg = qd if qd else p + 1
+    fe = H.GenericFiniteElement(H.Dubiner(2, H.RefTetrahedron, p))
+    Wh = H.ScalarFunctionSpace(mesh, fe, quad_degree=q_deg)
+    Vh = H.VectorFunctionSpace(mesh, fe, quad_degree=q_deg)
+    Mh = H.ScalarTraceFunctionSpace(Wh, H.GenericFiniteElement(H.Legendre(1, H.RefTetrahedron, p)))
+    K, b, _, _ = H.doassemble(Vh, Wh, Mh, 1.0, f, kappa_cell=kc)
+    dbc = H.Dirichlet(H.TrialFunction(Mh), mesh, "boundary")
+    H.apply_(K, b, dbc)
+    u_mg = K.solve(tol=1e-12, preconditioner=H.PRECOND_AMG)
+    it_mg = K.stats.iterations
+    K.reassemble(1.0, f, kappa_cell=kc)
+    K.apply_dirichlet(dbc.prescribed_dofs, dbc.values)
+    u_j = K.solve(tol=1e-12)
+    it_j = K.stats.iterations
+    om = oracle.rectangle_mesh(n, n)
+    om.set_xy(hm._topology()[0])
+    r = oracle.solve_poisson(om, p, qd=q_deg, f=f.as_oracle(), kappa_cell=kc)
+    assert rel(u_mg, r["uhat"]) < 1e-10, (rel(u_mg, r["uhat"]), it_mg)
+    assert rel(u_mg, u_j) < 1e-10
+    assert it_mg < it_j / 2, (it_mg, it_j)  # the gap widens with the mesh size (see the benches)
+
+
+@pytest.mark.gpu
+def test_multigrid_batch_matches_single_problems(H, oracle):
+    """A degree-binned batch solved with the multigrid preconditioner (each problem its own
+    hierarchy inside the shared arrays) gives each problem the oracle's solution."""
+    rng = np.random.default_rng(7)
+    probs = []
+    for k, (n, p) in enumerate([(4, 1), (7, 2), (3, 3), (5, 4), (6, 1), (2, 2), (4, 3), (12, 2)]):
+        f = H.Field.bumps(rng.random((8, 2)), 0.1 + 0.1 * rng.random(8), rng.standard_normal(8))
+        kc = np.exp(rng.uniform(np.log(1e-2), np.log(1e2), 2 * n * n))
+        probs.append(H.Problem(n=n, p=p, f=f, kappa_cell=kc, jitter=0.2, seed=100 + k))
+    B = H.Batch(H.default_context(), probs, precision=H.PREC_FP64)
+    stats = B.solve(tol=1e-12, preconditioner=H.PRECOND_AMG)
+    assert all(s.converged for s in stats)
+    for pr, (uh, q, u) in zip(probs, B.solutions()):
+        om = oracle.rectangle_mesh(pr.n, pr.n)
+        om.set_xy(H.batch.host_mesh(pr)._topology()[0])
+        r = oracle.solve_poisson(om, pr.p, qd=pr.qd(), f=pr.f.as_oracle(), kappa_cell=pr.kappa_cell)
+        assert rel(uh, r["uhat"]) < 1e-10, (pr.n, pr.p)
