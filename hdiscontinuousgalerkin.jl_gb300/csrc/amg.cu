@@ -16,9 +16,11 @@
 //    l1 row sums on the coarse levels with w = 4/3 (their spectrum lies in (0, 1]).
 //  * Coarse operator A_{l+1} = P' A P.  Coarsening stops once every problem has at most 96
 //    coarse rows; the coarsest systems are inverted densely, one per problem.
-//  * V(2,2) cycle: damped block Jacobi on level 0 (x += D^-1 (b - A x) / lambda), l1-Jacobi on
-//    the coarse levels, exact coarsest solve.  Pre- and post-smoothing are the same symmetric
-//    iteration, so the cycle is a symmetric positive definite preconditioner.
+//  * Cycle: degree-2 Chebyshev smoothing with the face-block diagonal on level 0 (the interval
+//    [lambda/30, lambda] of D^-1 A) before and after the correction, one l1-Jacobi sweep before
+//    and after on the coarse levels (each level's way down and way up fused into one kernel),
+//    exact coarsest solve.  Pre- and post-smoothing apply the same polynomial, so the cycle is a
+//    symmetric positive definite preconditioner.
 //
 // Aggregates depend only on the mesh and the Dirichlet faces, never on matrix values.  The
 // symbolic setup (aggregates, every sparsity pattern, the P' lists) therefore runs once per
@@ -168,7 +170,7 @@ struct AmgHierarchy {
   DevBuf<float> lam0;        // [nprob] Gershgorin bound of D^-1 A0
   DevBuf<int32_t> face_prob; // [nf]
   DevBuf<float> val0f;       // FP32 trace matrix (when the system has none)
-  DevBuf<float> x0, r0;      // level-0 cycle vectors
+  DevBuf<float> x0, r0, d0;  // level-0 cycle vectors (iterate, residual, Chebyshev correction)
   std::vector<AmgLevel> lev; // lev[0] is level 1
   // coarsest (last level): per-problem dense inverses
   std::vector<int32_t> h_crow0;  // [nprob+1] first coarsest row of each problem
@@ -302,6 +304,7 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
   H->face_prob.upload(fprob.data(), fprob.size(), st);
   H->x0.alloc((size_t)nf * nt);
   H->r0.alloc((size_t)nf * nt);
+  H->d0.alloc((size_t)nf * nt);
   H->lev.clear();
   H->lev.push_back(std::move(L1));
   // coarser levels
@@ -736,18 +739,23 @@ __global__ void k_amg_coarse_inv(const int32_t* __restrict__ crow0, const int32_
 
 // ------------------------------------------------------------------------------------------
 // Cycle kernels
+// Level-0 smoother: step `step` of the Chebyshev iteration (Saad, Iterative Methods, 12.3) for
+// D^-1 A0 on [lambda / CHEB_RATIO, lambda], D the face-block diagonal and lambda the problem's
+// Gershgorin bound.  xin == NULL stands for x = 0 (no product); d holds the previous step's
+// correction and is updated in place (each face reads and writes only its own rows of d).
+constexpr float CHEB_RATIO = 30.f;
 template <int NT>
-__global__ void k_amg_face_smooth(int nf, const int32_t* __restrict__ bcol5, const float* __restrict__ val,
-                                  const float* __restrict__ dinv, const float* __restrict__ lam,
-                                  const int32_t* __restrict__ face_prob, const float* __restrict__ b,
-                                  const float* __restrict__ xin, float* __restrict__ xout, int first) {
-  // first: x = D^-1 b / lambda;  else x = xin + D^-1 (b - A xin) / lambda  (xout != xin)
+__global__ void k_amg_face_cheb(int nf, const int32_t* __restrict__ bcol5, const float* __restrict__ val,
+                                const float* __restrict__ dinv, const float* __restrict__ lam,
+                                const int32_t* __restrict__ face_prob, const float* __restrict__ b,
+                                const float* __restrict__ xin, float* __restrict__ xout, float* __restrict__ d,
+                                int step) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
   const int64_t nd = (int64_t)nf * NT;
   float res[NT];
   for (int i = 0; i < NT; ++i) res[i] = b[(int64_t)f * NT + i];
-  if (!first) {
+  if (xin) {
     int seen[5];
     int ns = 0;
     for (int k = 0; k < 5; ++k) {
@@ -762,11 +770,21 @@ __global__ void k_amg_face_smooth(int nf, const int32_t* __restrict__ bcol5, con
       }
     }
   }
-  const float sc = 1.f / fmaxf(lam[face_prob[f]], 1e-30f);
+  const float hi = fmaxf(lam[face_prob[f]], 1e-30f), lo = hi / CHEB_RATIO;
+  const float theta = 0.5f * (hi + lo), delta = 0.5f * (hi - lo), sigma = theta / delta;
+  float rp = 1.f / sigma, rc = rp;  // rho_{step-1}, rho_step
+  for (int t = 1; t <= step; ++t) {
+    rc = 1.f / (2.f * sigma - rp);
+    if (t < step) rp = rc;
+  }
+  const float cd = (step == 0) ? 0.f : rc * rp, cr = (step == 0) ? 1.f / theta : 2.f * rc / delta;
   for (int i = 0; i < NT; ++i) {
     float t = 0.f;
     for (int l = 0; l < NT; ++l) t += dinv[((int64_t)f * NT + i) * NT + l] * res[l];
-    xout[(int64_t)f * NT + i] = (first ? 0.f : xin[(int64_t)f * NT + i]) + sc * t;
+    const int64_t row = (int64_t)f * NT + i;
+    const float dn = cr * t + (step == 0 ? 0.f : cd * d[row]);
+    d[row] = dn;
+    xout[row] = (xin ? xin[row] : 0.f) + dn;
   }
 }
 
@@ -824,49 +842,43 @@ __global__ void k_amg_prolong0(int nf, const int32_t* __restrict__ pcol0, const 
   x0[row] += s;
 }
 
-// CSR level: x_out = x_in + (b - A x_in) / dl1
-__global__ void k_amg_l1_sweep(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
-                               const float* __restrict__ val, const float* __restrict__ dl1inv,
-                               const float* __restrict__ b, const float* __restrict__ xin, float* __restrict__ xout) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  float s = b[i];
-  for (int e = ptr[i]; e < ptr[i + 1]; ++e) s -= val[e] * xin[col[e]];
-  xout[i] = xin[i] + s * dl1inv[i];
-}
-
-// CSR level: r = b - A x
-__global__ void k_amg_residual(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
-                               const float* __restrict__ val, const float* __restrict__ b, const float* __restrict__ x,
-                               float* __restrict__ r) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  float s = b[i];
-  for (int e = ptr[i]; e < ptr[i + 1]; ++e) s -= val[e] * x[col[e]];
-  r[i] = s;
-}
-
-// b_c = P' r and x_c = b_c / dl1_c (first sweep of the coarse level; dl1 NULL on the coarsest)
-__global__ void k_amg_restrict(int nc, const int32_t* __restrict__ rptr, const int32_t* __restrict__ rent,
-                               const int32_t* __restrict__ rrow, const float* __restrict__ pval,
-                               const float* __restrict__ r, const float* __restrict__ dl1inv, float* __restrict__ bc,
-                               float* __restrict__ xc) {
+// Coarse levels use one l1-Jacobi sweep before and after the coarse correction (V(1,1)), which
+// lets each level's way down and way up be one kernel each.
+// Down: the pre-smoothed iterate is x = b / dl1, so the restricted residual of coarse row J is
+//   b_c[J] = sum_{i in P'(J)} P[i,J] (b_i - sum_k A[i,k] b_k / dl1_k).
+__global__ void k_amg_down(int nc, const int32_t* __restrict__ rptr, const int32_t* __restrict__ rent,
+                           const int32_t* __restrict__ rrow, const float* __restrict__ pval,
+                           const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                           const float* __restrict__ val, const float* __restrict__ dl1inv, const float* __restrict__ b,
+                           float* __restrict__ bc) {
   const int J = blockIdx.x * blockDim.x + threadIdx.x;
   if (J >= nc) return;
   float s = 0.f;
-  for (int t = rptr[J]; t < rptr[J + 1]; ++t) s += pval[rent[t]] * r[rrow[t]];
+  for (int t = rptr[J]; t < rptr[J + 1]; ++t) {
+    const int i = rrow[t];
+    float r = b[i];
+    for (int e = ptr[i]; e < ptr[i + 1]; ++e) r -= val[e] * b[col[e]] * dl1inv[col[e]];
+    s += pval[rent[t]] * r;
+  }
   bc[J] = s;
-  if (dl1inv) xc[J] = s * dl1inv[J];
 }
 
-// x += P x_c
-__global__ void k_amg_prolong(int n, const int32_t* __restrict__ pptr, const int32_t* __restrict__ pcol,
-                              const float* __restrict__ pval, const float* __restrict__ xc, float* __restrict__ x) {
+// Up: the corrected iterate is xp_k = b_k / dl1_k + (P x_c)_k; one more sweep gives
+//   x_i = xp_i + (b_i - sum_k A[i,k] xp_k) / dl1_i.
+__global__ void k_amg_up(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                         const float* __restrict__ val, const float* __restrict__ dl1inv, const float* __restrict__ b,
+                         const int32_t* __restrict__ pptr, const int32_t* __restrict__ pcol,
+                         const float* __restrict__ pval, const float* __restrict__ xc, float* __restrict__ x) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  float s = 0.f;
-  for (int e = pptr[i]; e < pptr[i + 1]; ++e) s += pval[e] * xc[pcol[e]];
-  x[i] += s;
+  auto xp = [&](int k) {
+    float v = b[k] * dl1inv[k];
+    for (int t = pptr[k]; t < pptr[k + 1]; ++t) v += pval[t] * xc[pcol[t]];
+    return v;
+  };
+  float r = b[i];
+  for (int e = ptr[i]; e < ptr[i + 1]; ++e) r -= val[e] * xp(col[e]);
+  x[i] = xp(i) + r * dl1inv[i];
 }
 
 // coarsest: x = A^-1 b per problem (one CTA per problem)
@@ -930,47 +942,40 @@ template <int NT> void apply_nt(hdg_system* s, const float* val0, const float* b
   const int nf = H->nf;
   const int64_t n0 = (int64_t)nf * NT;
   const int nl = (int)H->lev.size();
-  // level 0 pre-smoothing: two block-Jacobi sweeps (z0 <- x0 <- D^-1 b)
-  k_amg_face_smooth<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
-                                                  nullptr, H->x0.p, 1);
-  k_amg_face_smooth<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
-                                                  H->x0.p, z0, 0);
+  // level 0 pre-smoothing: degree-2 Chebyshev from x = 0 (x0, then z0)
+  k_amg_face_cheb<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
+                                                nullptr, H->x0.p, H->d0.p, 0);
+  k_amg_face_cheb<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
+                                                H->x0.p, z0, H->d0.p, 1);
   k_amg_face_residual<NT><<<nblk(n0), 256, 0, st>>>(nf, s->d_bcol5.p, val0, b0, z0, H->r0.p);
   AmgLevel& L1 = H->lev[0];
   k_amg_restrict0<NT><<<nblk(L1.n), 256, 0, st>>>(L1.n, H->rptr0.p, H->rent0.p, H->pval0.p, H->r0.p, L1.dl1inv.p,
                                                   L1.b.p, L1.x.p);
   int launches = 4;
-  // coarse levels down: x holds the first sweep (from the restriction); the second sweep goes to
-  // t, which then holds the level's iterate until the way up
+  // coarse levels: one kernel down and one up per level (V(1,1), see k_amg_down / k_amg_up)
   for (int l = 0; l + 1 < nl; ++l) {
     AmgLevel& L = H->lev[l];
     AmgLevel& C = H->lev[l + 1];
-    k_amg_l1_sweep<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.x.p, L.t.p);
-    k_amg_residual<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.b.p, L.t.p, L.r.p);
-    const bool coarsest = (l + 2 == nl);
-    k_amg_restrict<<<nblk(C.n), 256, 0, st>>>(C.n, L.rptr.p, L.rent.p, L.rrow.p, L.pval.p, L.r.p,
-                                              coarsest ? nullptr : C.dl1inv.p, C.b.p, C.x.p);
-    launches += 3;
+    k_amg_down<<<nblk(C.n), 256, 0, st>>>(C.n, L.rptr.p, L.rent.p, L.rrow.p, L.pval.p, L.ptr.p, L.col.p, L.val.p,
+                                          L.dl1inv.p, L.b.p, C.b.p);
+    ++launches;
   }
   AmgLevel& C = H->lev.back();
   if (H->cmax > 0) k_amg_coarse_solve<<<s->nprob, 128, 0, st>>>(H->crow0.p, H->coff.p, H->cinv.p, C.b.p, C.x.p);
   ++launches;
-  // coarse levels up: the coarser level's result is in its x; prolongate into this level's
-  // iterate (t), then two sweeps t -> r -> x
   for (int l = nl - 2; l >= 0; --l) {
     AmgLevel& L = H->lev[l];
     AmgLevel& Cn = H->lev[l + 1];
-    k_amg_prolong<<<nblk(L.n), 256, 0, st>>>(L.n, L.pptr.p, L.pcol.p, L.pval.p, Cn.x.p, L.t.p);
-    k_amg_l1_sweep<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.t.p, L.r.p);
-    k_amg_l1_sweep<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.r.p, L.x.p);
-    launches += 3;
+    k_amg_up<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.pptr.p, L.pcol.p,
+                                        L.pval.p, Cn.x.p, L.x.p);
+    ++launches;
   }
-  // level 0 up: prolongate, two block-Jacobi sweeps
+  // level 0 up: prolongate, degree-2 Chebyshev from the corrected iterate
   k_amg_prolong0<NT><<<nblk(n0), 256, 0, st>>>(nf, H->pcol0.p, H->pval0.p, L1.x.p, z0);
-  k_amg_face_smooth<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
-                                                  z0, H->x0.p, 0);
-  k_amg_face_smooth<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
-                                                  H->x0.p, z0, 0);
+  k_amg_face_cheb<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
+                                                z0, H->x0.p, H->d0.p, 0);
+  k_amg_face_cheb<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
+                                                H->x0.p, z0, H->d0.p, 1);
   launches += 3;
   (void)launches;  // counted by the caller per replay (amg_cycle_launches)
 }
@@ -1013,16 +1018,16 @@ double amg_cycle_bytes(const hdg_system* s) {
       b += 8.0 * n + 4.0 * H->cinv.n;                      // coarsest dense solve
       break;
     }
-    const double npc = (double)H->lev[l].h_col.size();      // P and P' sizes are comparable to A's
-    b += 3.0 * (spmv + 20.0 * n) + (spmv + 16.0 * n);      // three sweeps, one residual
-    b += 2.0 * (8.0 * npc + 12.0 * n);                      // restriction and prolongation
+    const double np = (double)H->lev[l].h_col.size();       // P and P' sizes are comparable to A's
+    b += spmv + 8.0 * np + 12.0 * n;                        // down: A, dl1, b, P' values
+    b += spmv + 8.0 * np + 16.0 * n;                        // up: A, dl1, b, P values, x
   }
   return b;
 }
 
 int amg_cycle_launches(const hdg_system* s) {
   const int nl = (int)s->amg->lev.size();
-  return 4 + 3 * (nl - 1) + 1 + 3 * (nl - 1) + 3;
+  return 4 + (nl - 1) + 1 + (nl - 1) + 3;
 }
 
 void amg_apply(hdg_system* s, const float* r, float* z, cudaStream_t st) {
