@@ -16,10 +16,9 @@
 //    l1 row sums on the coarse levels with w = 4/3 (their spectrum lies in (0, 1]).
 //  * Coarse operator A_{l+1} = P' A P.  Coarsening stops once every problem has at most 96
 //    coarse rows; the coarsest systems are inverted densely, one per problem.
-//  * Cycle: degree-2 Chebyshev smoothing with the face-block diagonal on level 0 (the interval
-//    [lambda/30, lambda] of D^-1 A) before and after the correction, one l1-Jacobi sweep before
-//    and after on the coarse levels (each level's way down and way up fused into one kernel),
-//    exact coarsest solve.  Pre- and post-smoothing apply the same polynomial, so the cycle is a
+//  * V(2,2) cycle: degree-2 Chebyshev smoothing with the face-block diagonal on level 0 (the
+//    interval [lambda/30, lambda] of D^-1 A), two l1-Jacobi sweeps on the coarse levels, exact
+//    coarsest solve.  Pre- and post-smoothing apply the same polynomial, so the cycle is a
 //    symmetric positive definite preconditioner.
 //
 // Aggregates depend only on the mesh and the Dirichlet faces, never on matrix values.  The
@@ -842,43 +841,49 @@ __global__ void k_amg_prolong0(int nf, const int32_t* __restrict__ pcol0, const 
   x0[row] += s;
 }
 
-// Coarse levels use one l1-Jacobi sweep before and after the coarse correction (V(1,1)), which
-// lets each level's way down and way up be one kernel each.
-// Down: the pre-smoothed iterate is x = b / dl1, so the restricted residual of coarse row J is
-//   b_c[J] = sum_{i in P'(J)} P[i,J] (b_i - sum_k A[i,k] b_k / dl1_k).
-__global__ void k_amg_down(int nc, const int32_t* __restrict__ rptr, const int32_t* __restrict__ rent,
-                           const int32_t* __restrict__ rrow, const float* __restrict__ pval,
-                           const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
-                           const float* __restrict__ val, const float* __restrict__ dl1inv, const float* __restrict__ b,
-                           float* __restrict__ bc) {
+// CSR level: x_out = x_in + (b - A x_in) / dl1
+__global__ void k_amg_l1_sweep(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                               const float* __restrict__ val, const float* __restrict__ dl1inv,
+                               const float* __restrict__ b, const float* __restrict__ xin, float* __restrict__ xout) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float s = b[i];
+  for (int e = ptr[i]; e < ptr[i + 1]; ++e) s -= val[e] * xin[col[e]];
+  xout[i] = xin[i] + s * dl1inv[i];
+}
+
+// CSR level: r = b - A x
+__global__ void k_amg_residual(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
+                               const float* __restrict__ val, const float* __restrict__ b, const float* __restrict__ x,
+                               float* __restrict__ r) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float s = b[i];
+  for (int e = ptr[i]; e < ptr[i + 1]; ++e) s -= val[e] * x[col[e]];
+  r[i] = s;
+}
+
+// b_c = P' r and x_c = b_c / dl1_c (first sweep of the coarse level; dl1 NULL on the coarsest)
+__global__ void k_amg_restrict(int nc, const int32_t* __restrict__ rptr, const int32_t* __restrict__ rent,
+                               const int32_t* __restrict__ rrow, const float* __restrict__ pval,
+                               const float* __restrict__ r, const float* __restrict__ dl1inv, float* __restrict__ bc,
+                               float* __restrict__ xc) {
   const int J = blockIdx.x * blockDim.x + threadIdx.x;
   if (J >= nc) return;
   float s = 0.f;
-  for (int t = rptr[J]; t < rptr[J + 1]; ++t) {
-    const int i = rrow[t];
-    float r = b[i];
-    for (int e = ptr[i]; e < ptr[i + 1]; ++e) r -= val[e] * b[col[e]] * dl1inv[col[e]];
-    s += pval[rent[t]] * r;
-  }
+  for (int t = rptr[J]; t < rptr[J + 1]; ++t) s += pval[rent[t]] * r[rrow[t]];
   bc[J] = s;
+  if (dl1inv) xc[J] = s * dl1inv[J];
 }
 
-// Up: the corrected iterate is xp_k = b_k / dl1_k + (P x_c)_k; one more sweep gives
-//   x_i = xp_i + (b_i - sum_k A[i,k] xp_k) / dl1_i.
-__global__ void k_amg_up(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
-                         const float* __restrict__ val, const float* __restrict__ dl1inv, const float* __restrict__ b,
-                         const int32_t* __restrict__ pptr, const int32_t* __restrict__ pcol,
-                         const float* __restrict__ pval, const float* __restrict__ xc, float* __restrict__ x) {
+// x += P x_c
+__global__ void k_amg_prolong(int n, const int32_t* __restrict__ pptr, const int32_t* __restrict__ pcol,
+                              const float* __restrict__ pval, const float* __restrict__ xc, float* __restrict__ x) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  auto xp = [&](int k) {
-    float v = b[k] * dl1inv[k];
-    for (int t = pptr[k]; t < pptr[k + 1]; ++t) v += pval[t] * xc[pcol[t]];
-    return v;
-  };
-  float r = b[i];
-  for (int e = ptr[i]; e < ptr[i + 1]; ++e) r -= val[e] * xp(col[e]);
-  x[i] = xp(i) + r * dl1inv[i];
+  float s = 0.f;
+  for (int e = pptr[i]; e < pptr[i + 1]; ++e) s += pval[e] * xc[pcol[e]];
+  x[i] += s;
 }
 
 // coarsest: x = A^-1 b per problem (one CTA per problem)
@@ -952,23 +957,30 @@ template <int NT> void apply_nt(hdg_system* s, const float* val0, const float* b
   k_amg_restrict0<NT><<<nblk(L1.n), 256, 0, st>>>(L1.n, H->rptr0.p, H->rent0.p, H->pval0.p, H->r0.p, L1.dl1inv.p,
                                                   L1.b.p, L1.x.p);
   int launches = 4;
-  // coarse levels: one kernel down and one up per level (V(1,1), see k_amg_down / k_amg_up)
+  // coarse levels down: x holds the first sweep (from the restriction); the second sweep goes to
+  // t, which then holds the level's iterate until the way up
   for (int l = 0; l + 1 < nl; ++l) {
     AmgLevel& L = H->lev[l];
     AmgLevel& C = H->lev[l + 1];
-    k_amg_down<<<nblk(C.n), 256, 0, st>>>(C.n, L.rptr.p, L.rent.p, L.rrow.p, L.pval.p, L.ptr.p, L.col.p, L.val.p,
-                                          L.dl1inv.p, L.b.p, C.b.p);
-    ++launches;
+    k_amg_l1_sweep<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.x.p, L.t.p);
+    k_amg_residual<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.b.p, L.t.p, L.r.p);
+    const bool coarsest = (l + 2 == nl);
+    k_amg_restrict<<<nblk(C.n), 256, 0, st>>>(C.n, L.rptr.p, L.rent.p, L.rrow.p, L.pval.p, L.r.p,
+                                              coarsest ? nullptr : C.dl1inv.p, C.b.p, C.x.p);
+    launches += 3;
   }
   AmgLevel& C = H->lev.back();
   if (H->cmax > 0) k_amg_coarse_solve<<<s->nprob, 128, 0, st>>>(H->crow0.p, H->coff.p, H->cinv.p, C.b.p, C.x.p);
   ++launches;
+  // coarse levels up: the coarser level's result is in its x; prolongate into this level's
+  // iterate (t), then two sweeps t -> r -> x
   for (int l = nl - 2; l >= 0; --l) {
     AmgLevel& L = H->lev[l];
     AmgLevel& Cn = H->lev[l + 1];
-    k_amg_up<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.pptr.p, L.pcol.p,
-                                        L.pval.p, Cn.x.p, L.x.p);
-    ++launches;
+    k_amg_prolong<<<nblk(L.n), 256, 0, st>>>(L.n, L.pptr.p, L.pcol.p, L.pval.p, Cn.x.p, L.t.p);
+    k_amg_l1_sweep<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.t.p, L.r.p);
+    k_amg_l1_sweep<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.r.p, L.x.p);
+    launches += 3;
   }
   // level 0 up: prolongate, degree-2 Chebyshev from the corrected iterate
   k_amg_prolong0<NT><<<nblk(n0), 256, 0, st>>>(nf, H->pcol0.p, H->pval0.p, L1.x.p, z0);
@@ -1018,16 +1030,16 @@ double amg_cycle_bytes(const hdg_system* s) {
       b += 8.0 * n + 4.0 * H->cinv.n;                      // coarsest dense solve
       break;
     }
-    const double np = (double)H->lev[l].h_col.size();       // P and P' sizes are comparable to A's
-    b += spmv + 8.0 * np + 12.0 * n;                        // down: A, dl1, b, P' values
-    b += spmv + 8.0 * np + 16.0 * n;                        // up: A, dl1, b, P values, x
+    const double npc = (double)H->lev[l].h_col.size();      // P and P' sizes are comparable to A's
+    b += 3.0 * (spmv + 20.0 * n) + (spmv + 16.0 * n);      // three sweeps, one residual
+    b += 2.0 * (8.0 * npc + 12.0 * n);                      // restriction and prolongation
   }
   return b;
 }
 
 int amg_cycle_launches(const hdg_system* s) {
   const int nl = (int)s->amg->lev.size();
-  return 4 + (nl - 1) + 1 + (nl - 1) + 3;
+  return 4 + 3 * (nl - 1) + 1 + 3 * (nl - 1) + 3;
 }
 
 void amg_apply(hdg_system* s, const float* r, float* z, cudaStream_t st) {
