@@ -36,7 +36,7 @@ WORKLOADS = {
     "c1": dict(n=32, p=1, qd=None, desc="2·32·32=2048 triangles, p=1, tau=1, FP64, manufactured sin·sin, "
                                        "homogeneous Dirichlet"),
     "c2": dict(n=256, p=2, qd=None, desc="2·256·256=131072 triangles, p=2, tau=1, FP64, manufactured sin·sin, "
-                                        "homogeneous Dirichlet, Jacobi-PCG to 1e-12 relative residual"),
+                                        "homogeneous Dirichlet, PCG to 1e-12 relative residual"),
 }
 
 
@@ -179,6 +179,10 @@ def run_c4(args, ws, rank, local):
     peaks, peak_kind = measured_peaks()
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     tims = [bn.timings() for bn in B.bins]
+    bins_detail = [{"p": bn.p, "problems": len(bn.problems), "cells": bn.mesh.ncells, "trace_dofs": bn.ndofs,
+                    "element_ms": t["element_ms"], "cg_ms": t["cg_ms"],
+                    "cg_iterations_max": max(B.stats[i].iterations for i in bn.idx)}
+                   for bn, t in zip(B.bins, tims)]
     cg_ms = max(t["cg_ms"] for t in tims)
     cg_bytes = sum(t["cg_bytes"] for t in tims)
     el_ms = sum(t["element_ms"] for t in tims)
@@ -251,6 +255,7 @@ def run_c4(args, ws, rank, local):
         "max_rel_residual": float(max(s.rel_residual for s in B.stats)),
         "cg_iterations_max": max(iters), "cg_iterations_mean": float(np.mean(iters)),
         "phase_ms": {"element_ms_sum_of_bins": el_ms, "cg_ms_longest_bin": cg_ms},
+        "bins": bins_detail,
         "gpu_launches": launches,
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
@@ -424,7 +429,8 @@ def run_c5(args, ws, rank, local):
                              mesh=H.batch.host_mesh(H.Problem(n=n, p=p, f=f, jitter=0.2, seed=sd))))
 
     eng = H.Engine(ctx, hbm_budget_gb=args.hbm_budget_gb, max_batch=args.max_batch, max_flights=args.max_flights,
-                   tol=tol, precision=H.PREC_MIXED if args.precision == "mixed" else H.PREC_FP64, keep_results=True)
+                   tol=tol, precision=H.PREC_MIXED if args.precision == "mixed" else H.PREC_FP64, keep_results=True,
+                   preconditioner=H.PRECOND_AMG if args.preconditioner == "amg" else H.PRECOND_JACOBI)
     host_res = [H.batch.host_mesh(pr) for pr in resident]
     mids = [eng.add_resident(hm, pr.p) for hm, pr in zip(host_res, resident)]
 
@@ -492,7 +498,8 @@ def run_c5(args, ws, rank, local):
         t1 = time.perf_counter()
         K, b, _, _ = H.doassemble(Vh, Wh, Mh, 1.0, pr.f, kappa_cell=pr.kappa_cell)
         H.apply_(K, b, H.Dirichlet(H.TrialFunction(Mh), dm, "boundary"))
-        uh = H.solve(K, b, tol=tol_, precision=H.PREC_FP64)
+        uh = H.solve(K, b, tol=tol_, precision=H.PREC_FP64,
+                     preconditioner=H.PRECOND_AMG if args.preconditioner == "amg" else H.PRECOND_JACOBI)
         q, u, _ = K.recover()
         t2 = time.perf_counter()
         return t2 - t1, (uh, q, u)
@@ -511,7 +518,8 @@ def run_c5(args, ws, rank, local):
         "data": "synthetic",
         "config": {"workload": "c5: Poisson request stream at 2000 req/s (seeded), each drawn like the batching "
                                "workload; 70% on one of 32 resident meshes with a new source and kappa, 30% new meshes;"
-                               f" continuous batching, {args.precision}, CG tol {tol:g}",
+                               f" continuous batching, {args.precision}, {args.preconditioner}-preconditioned CG "
+                               f"tol {tol:g}",
                    "requests": nreq, "hbm_budget_gb": args.hbm_budget_gb, "max_batch": args.max_batch,
                    "max_flights": args.max_flights, "step": "one request solved"},
         "p50_ms": lat_ms[len(lat_ms) // 2], "p99_ms": lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))],
@@ -544,6 +552,8 @@ def parse():
                     help="trace CG preconditioner (default: amg for the batch c4, jacobi otherwise); the plain "
                          "FP64 path of c4 uses the same one")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--n", type=int, default=None, help="c1/c2 only: cells per side (a profiling case, not a bench line)")
+    ap.add_argument("--p", type=int, default=None, help="c1/c2 only: polynomial degree (a profiling case)")
     args = ap.parse_args()
     if args.precision is None:
         args.precision = "mixed" if args.workload in ("c3", "c4", "c5") else "fp64"
@@ -730,7 +740,12 @@ def run_ours(args, ws, rank, local):
     import __graft_entry__ as g
     g.build()
     H = g.import_package()
-    w = WORKLOADS[args.workload]
+    w = dict(WORKLOADS[args.workload])
+    if args.n or args.p:
+        w["n"], w["p"] = args.n or w["n"], args.p or w["p"]
+        w["qd"] = {3: 6, 4: 9}.get(w["p"], w["qd"])  # Strang(p+1) leaves M singular for p >= 3
+        w["desc"] = (f"profiling case 2·{w['n']}·{w['n']} triangles, p={w['p']}, quadrature degree "
+                     f"{w['qd'] or w['p'] + 1}, tau=1, manufactured sin·sin")
     prec = H.PREC_FP64 if args.precision == "fp64" else H.PREC_MIXED
     pc = H.PRECOND_AMG if args.preconditioner == "amg" else H.PRECOND_JACOBI
     torch.cuda.set_device(local)
@@ -804,15 +819,22 @@ def run_ours(args, ws, rank, local):
     bytes_elem = ncells * (12 + 48 + 1 + 8 * (m_ * (m_ + 1) + 3 * nw_ * (m_ + 1)))
     avg = lambda key: statistics.mean(t[key] for t in tims)
     it_mean = statistics.mean(iters)
+    # the CG kernels' algorithmic bytes come from the library's accounting of the sampled launches
+    # (rows that iterated x per-row bytes; with the multigrid preconditioner the "update" sample
+    # covers k_cg_b_mg, the V-cycle and k_cg_c)
+    lib_a, lib_b = avg("cg_a_bytes"), avg("cg_b_bytes")
+    name_a = "k_cg_a_fresh (q = A p_new, p.q)" if (prec == H.PREC_MIXED and pc != H.PRECOND_AMG) else \
+        "k_cg_a (q = A z + beta q, p update, p.q)"
+    name_b = ("k_cg_b_mg + multigrid V-cycle + k_cg_c" if pc == H.PRECOND_AMG else "k_cg_b (x, r, z update, r.z, r.r)")
     kern = {
-        "k_cg_a (q = A z + beta q, p update, p.q)": (avg("cg_a_ms"), bytes_a, it_mean),
-        "k_cg_b (x, r, z update, r.z, r.r)": (avg("cg_b_ms"), bytes_b, it_mean),
+        name_a: (avg("cg_a_ms"), lib_a if lib_a > 0 else bytes_a, it_mean),
+        name_b: (avg("cg_b_ms"), lib_b if lib_b > 0 else bytes_b, it_mean),
         "k_element_condense": (avg("element_ms"), bytes_elem, 1),
     }
     dom = max(kern, key=lambda k: kern[k][0] * kern[k][2])
     dur, alg, cnt = kern[dom]
     achieved = alg / (dur / 1e3) / 1e9 if dur > 0 else None
-    traffic = profile_traffic("k_cg_a" if dom.startswith("k_cg_a") else dom.split()[0])
+    traffic = profile_traffic(dom.split()[0]) if not dom.startswith("k_cg_b_mg") else None
 
     # ---- end-to-end through the public API with host buffers ----
     import numpy as np
@@ -847,7 +869,7 @@ def run_ours(args, ws, rank, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == H.PREC_FP64 else "f32+f64",
         "data": "synthetic",
         "config": {"workload": f"{args.workload}: {w['desc']}", "n": n, "p": p, "cells": ncells, "trace_dofs": ndofs,
-                   "nnz": nnz, "precision": args.precision, "tol": args.tol,
+                   "nnz": nnz, "precision": args.precision, "preconditioner": args.preconditioner, "tol": args.tol,
                    "l2": "inputs larger than L2: each step rewrites the per-cell condensed blocks "
                          f"({bytes_elem / 1e6:.0f} MB) before the solve",
                    "parallelism": f"{ws} independent replica(s), one per GPU"},

@@ -22,7 +22,7 @@ from .spaces import (ContinuousLagrange, Dubiner, GenericFiniteElement, Legendre
                      getnbasefunctions, getnfacequadpoints, getnlocaldofs, getnquadpoints, reinit_, shape_divergence,
                      shape_gradient, shape_value)
 from .system import (CellIterator, Dirichlet, SolveStats, TraceSystem, TrialFunction, apply_, doassemble, errornorm,
-                     get_usigma_, solve, solve_poisson)
+                     get_usigma_, nodal_avg, solve, solve_poisson)
 
 
 def load_library():

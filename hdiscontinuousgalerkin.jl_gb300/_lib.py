@@ -22,6 +22,7 @@ ERRORS = {
 }
 PREC_FP64, PREC_MIXED = 0, 1
 PRECOND_JACOBI, PRECOND_AMG = 0, 1
+STEP_ASSEMBLE, STEP_APPLY, STEP_RECOVER = 1, 2, 4  # hdg_batch_step flags
 FIELD_CONST, FIELD_SINSIN, FIELD_BUMPS, FIELD_FOURIER, FIELD_EXP_FOURIER = 0, 1, 2, 3, 4
 
 
@@ -91,6 +92,7 @@ SIGNATURES = {
     "hdg_solve": ([vp, C.POINTER(hdg_solver), dp, C.POINTER(hdg_stats)], ip),
     "hdg_recover": ([vp, dp, dp, dp], ip),
     "hdg_errornorm_l2sq": ([vp, C.POINTER(hdg_field), dp], ip),
+    "hdg_nodal_avg": ([vp, dp], ip),
     "hdg_system_destroy": ([vp], ip),
     "hdg_errornorm_l2sq_noalloc": ([ip, vp, ip, ip, ip, vp, vp, vp, C.POINTER(hdg_field), dp], ip),
     "hdg_noalloc_last_error": ([], C.c_char_p),
@@ -101,6 +103,9 @@ SIGNATURES = {
     "hdg_assemble_condense_batch": ([vp, dp, C.POINTER(hdg_field), C.POINTER(hdg_field), dp, ip, C.POINTER(vp)], ip),
     "hdg_system_reassemble_batch": ([vp, dp, C.POINTER(hdg_field), C.POINTER(hdg_field), dp], ip),
     "hdg_solve_batch": ([ip, C.POINTER(vp), C.POINTER(hdg_solver), C.POINTER(hdg_stats)], ip),
+    "hdg_system_set_coefficients_batch": ([vp, dp, C.POINTER(hdg_field), C.POINTER(hdg_field), dp], ip),
+    "hdg_system_set_dirichlet": ([vp, i32p, dp, ip], ip),
+    "hdg_batch_step": ([ip, C.POINTER(vp), C.POINTER(hdg_solver), ip, C.POINTER(hdg_stats)], ip),
     "hdg_system_get_solution": ([vp, dp, dp], ip),
     "hdg_engine_create": ([vp, C.c_double, ip, ip, C.POINTER(hdg_solver), C.POINTER(vp)], ip),
     "hdg_engine_add_resident_mesh": ([vp, vp, ip, intp], ip),

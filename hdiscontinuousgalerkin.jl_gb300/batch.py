@@ -83,6 +83,7 @@ class Bin:
         L.check(L.load().hdg_system_sizes(self.h, C.byref(nd), C.byref(nnz), C.byref(n), C.byref(m)))
         self.ndofs, self.n = nd.value, n.value
         self._dirichlet()
+        self._dir_set = False
 
     def _coef_arrays(self):
         np_ = len(self.problems)
@@ -115,6 +116,16 @@ class Bin:
 
     def apply(self):
         L.check(L.load().hdg_apply_dirichlet(self.h, L.i32ptr(self.dofs), L.dptr(self.vals), len(self.dofs)),
+                self.ctx.handle)
+
+    def set_coefficients(self):
+        """Upload the problems' coefficients without assembling (the next step assembles)."""
+        L.check(L.load().hdg_system_set_coefficients_batch(self.h, L.dptr(self.taus), self.farr, None,
+                                                           L.dptr(self.kc)), self.ctx.handle)
+
+    def set_dirichlet(self):
+        """Record (upload and scatter) the Dirichlet set without applying it."""
+        L.check(L.load().hdg_system_set_dirichlet(self.h, L.i32ptr(self.dofs), L.dptr(self.vals), len(self.dofs)),
                 self.ctx.handle)
 
     def recover(self):
@@ -160,23 +171,29 @@ class Batch:
         self.stats = None
 
     def solve(self, tol=1e-10, maxit=100000, chunk=32, reassemble=True, preconditioner=L.PRECOND_JACOBI):
-        """assemble + condense (all bins), apply!, interleaved CG over the bins, recovery.
-        reassemble: True (upload the coefficients and assemble), "resident" (assemble from the
-        coefficients already on the device) or False (keep the assembled systems)."""
+        """assemble + condense, apply!, CG and recovery of every problem, as one pipelined step
+        (hdg_batch_step): each degree bin runs on a stream of its own, so one bin's assembly and
+        recovery overlap the other bins' iterations.
+        reassemble: True (upload the coefficients and Dirichlet data, then assemble), "resident"
+        (assemble from the coefficients and Dirichlet data already on the device) or False (keep
+        the assembled systems; they must not have been applied yet)."""
+        flags = L.STEP_APPLY | L.STEP_RECOVER
         for b in self.bins:
-            if reassemble:
-                b.reassemble(resident=(reassemble == "resident"))
-            b.apply()
+            if reassemble is True:
+                b.set_coefficients()
+            if reassemble is True or not b._dir_set:
+                b.set_dirichlet()
+                b._dir_set = True
+        if reassemble:
+            flags |= L.STEP_ASSEMBLE
         prec = self.bins[0].precision
         o = L.hdg_solver(float(tol), int(maxit), int(prec), int(chunk), 1e-5, int(preconditioner))
         n = len(self.problems)
         st = (L.hdg_stats * n)()
         arr = (C.c_void_p * len(self.bins))(*[b.h for b in self.bins])
-        rc = L.load().hdg_solve_batch(len(self.bins), arr, C.byref(o), st)
+        rc = L.load().hdg_batch_step(len(self.bins), arr, C.byref(o), flags, st)
         if rc not in (0, -5):  # a problem that misses the tolerance is reported in its stats
             L.check(rc, self.ctx.handle)
-        for b in self.bins:
-            b.recover()
         stats = [None] * n
         k = 0
         for b in self.bins:

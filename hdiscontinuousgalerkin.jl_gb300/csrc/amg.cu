@@ -32,6 +32,8 @@
 // SPD approximation.  All sums run in a fixed order, so the cycle is deterministic.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <numeric>
 
 #include "hdg_device.cuh"
@@ -186,6 +188,7 @@ void destroy_amg(AmgHierarchy* h) { delete h; }
 void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) {
   if (s->amg) destroy_amg(s->amg);
   s->amg = new AmgHierarchy();
+  ++s->amg_gen;
   AmgHierarchy* H = s->amg;
   const int nf = s->nf, nt = s->nt;
   H->nf = nf;
@@ -422,6 +425,15 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
   H->coff.upload(coff.data(), coff.size(), st);
   H->cinv.alloc(std::max(coff[s->nprob], 1));
   H->built = true;
+  if (std::getenv("HDG_AMG_VERBOSE")) {  // level sizes: rows (largest problem's rows)
+    std::fprintf(stderr, "amg: %d problems, level 0: %d faces x %d", s->nprob, nf, nt);
+    for (const AmgLevel& L : H->lev) {
+      std::vector<int> cnt(s->nprob, 0);
+      for (int i = 0; i < L.n; ++i) ++cnt[L.h_prob[i]];
+      std::fprintf(stderr, ", %d (%d)", L.n, *std::max_element(cnt.begin(), cnt.end()));
+    }
+    std::fprintf(stderr, "\n");
+  }
   HDG_CUDA(cudaStreamSynchronize(st));
 }
 
@@ -841,49 +853,78 @@ __global__ void k_amg_prolong0(int nf, const int32_t* __restrict__ pcol0, const 
   x0[row] += s;
 }
 
-// CSR level: x_out = x_in + (b - A x_in) / dl1
+// Coarse-level kernels: G lanes per row (G a power of two <= 32).  The lanes of a group take a
+// row's entries in turn and add their partial sums with a shuffle tree (FP32, fixed order), so
+// the result does not depend on the launch.  Small levels (a few thousand rows) are latency-bound
+// and use whole warps, which shortens each row's chain of dependent loads; large levels (the
+// first coarse levels of a batch hold 10^5 rows and more) are bandwidth-bound and use 4 lanes,
+// which keeps most lanes busy on rows of 10-20 entries.
+// Row and lane of a thread.  Warps whose first row is past the end leave at once (uniformly);
+// in the last warp every lane stays until the shuffle, which names all 32 lanes.
+#define AMG_GROUP_ROW(ROW, LANE, N)                                                   \
+  const int64_t t_ = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;                 \
+  if ((t_ - (threadIdx.x & 31)) / G >= (N)) return;                                   \
+  const int ROW = (int)(t_ / G), LANE = (int)(t_ % G)
+
+template <int G> __device__ __forceinline__ float group_sum_f(float v) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// x_out = x_in + (b - A x_in) / dl1
+template <int G>
 __global__ void k_amg_l1_sweep(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
                                const float* __restrict__ val, const float* __restrict__ dl1inv,
                                const float* __restrict__ b, const float* __restrict__ xin, float* __restrict__ xout) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  float s = b[i];
-  for (int e = ptr[i]; e < ptr[i + 1]; ++e) s -= val[e] * xin[col[e]];
-  xout[i] = xin[i] + s * dl1inv[i];
+  AMG_GROUP_ROW(i, lane, n);
+  float s = 0.f;
+  if (i < n)
+    for (int e = ptr[i] + lane; e < ptr[i + 1]; e += G) s += val[e] * xin[col[e]];
+  s = group_sum_f<G>(s);
+  if (lane == 0 && i < n) xout[i] = xin[i] + (b[i] - s) * dl1inv[i];
 }
 
-// CSR level: r = b - A x
+// r = b - A x
+template <int G>
 __global__ void k_amg_residual(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
                                const float* __restrict__ val, const float* __restrict__ b, const float* __restrict__ x,
                                float* __restrict__ r) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  float s = b[i];
-  for (int e = ptr[i]; e < ptr[i + 1]; ++e) s -= val[e] * x[col[e]];
-  r[i] = s;
+  AMG_GROUP_ROW(i, lane, n);
+  float s = 0.f;
+  if (i < n)
+    for (int e = ptr[i] + lane; e < ptr[i + 1]; e += G) s += val[e] * x[col[e]];
+  s = group_sum_f<G>(s);
+  if (lane == 0 && i < n) r[i] = b[i] - s;
 }
 
 // b_c = P' r and x_c = b_c / dl1_c (first sweep of the coarse level; dl1 NULL on the coarsest)
+template <int G>
 __global__ void k_amg_restrict(int nc, const int32_t* __restrict__ rptr, const int32_t* __restrict__ rent,
                                const int32_t* __restrict__ rrow, const float* __restrict__ pval,
                                const float* __restrict__ r, const float* __restrict__ dl1inv, float* __restrict__ bc,
                                float* __restrict__ xc) {
-  const int J = blockIdx.x * blockDim.x + threadIdx.x;
-  if (J >= nc) return;
+  AMG_GROUP_ROW(J, lane, nc);
   float s = 0.f;
-  for (int t = rptr[J]; t < rptr[J + 1]; ++t) s += pval[rent[t]] * r[rrow[t]];
-  bc[J] = s;
-  if (dl1inv) xc[J] = s * dl1inv[J];
+  if (J < nc)
+    for (int k = rptr[J] + lane; k < rptr[J + 1]; k += G) s += pval[rent[k]] * r[rrow[k]];
+  s = group_sum_f<G>(s);
+  if (lane == 0 && J < nc) {
+    bc[J] = s;
+    if (dl1inv) xc[J] = s * dl1inv[J];
+  }
 }
 
 // x += P x_c
+template <int G>
 __global__ void k_amg_prolong(int n, const int32_t* __restrict__ pptr, const int32_t* __restrict__ pcol,
                               const float* __restrict__ pval, const float* __restrict__ xc, float* __restrict__ x) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  AMG_GROUP_ROW(i, lane, n);
   float s = 0.f;
-  for (int e = pptr[i]; e < pptr[i + 1]; ++e) s += pval[e] * xc[pcol[e]];
-  x[i] += s;
+  if (i < n)
+    for (int e = pptr[i] + lane; e < pptr[i + 1]; e += G) s += pval[e] * xc[pcol[e]];
+  s = group_sum_f<G>(s);
+  if (lane == 0 && i < n) x[i] += s;
 }
 
 // coarsest: x = A^-1 b per problem (one CTA per problem)
@@ -900,6 +941,18 @@ __global__ void k_amg_coarse_solve(const int32_t* __restrict__ crow0, const int3
 }
 
 inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)std::max<int64_t>(1, (n + t - 1) / t); }
+
+// Lanes per row of a coarse level with n rows (see the coarse-level kernels).
+inline int amg_group(int n) { return n >= 16384 ? 4 : (n >= 2048 ? 8 : 32); }
+#define AMG_LAUNCH_G(KERNEL, ROWS, ST, ...)                                                        \
+  do {                                                                                             \
+    const int rows_ = (ROWS);                                                                      \
+    switch (amg_group(rows_)) {                                                                    \
+      case 4: KERNEL<4><<<nblk((int64_t)rows_ * 4), 256, 0, ST>>>(__VA_ARGS__); break;             \
+      case 8: KERNEL<8><<<nblk((int64_t)rows_ * 8), 256, 0, ST>>>(__VA_ARGS__); break;             \
+      default: KERNEL<32><<<nblk((int64_t)rows_ * 32), 256, 0, ST>>>(__VA_ARGS__); break;          \
+    }                                                                                              \
+  } while (0)
 
 template <int NT> void numeric_nt(hdg_system* s, const float* val0, cudaStream_t st) {
   AmgHierarchy* H = s->amg;
@@ -962,11 +1015,11 @@ template <int NT> void apply_nt(hdg_system* s, const float* val0, const float* b
   for (int l = 0; l + 1 < nl; ++l) {
     AmgLevel& L = H->lev[l];
     AmgLevel& C = H->lev[l + 1];
-    k_amg_l1_sweep<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.x.p, L.t.p);
-    k_amg_residual<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.b.p, L.t.p, L.r.p);
+    AMG_LAUNCH_G(k_amg_l1_sweep, L.n, st, L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.x.p, L.t.p);
+    AMG_LAUNCH_G(k_amg_residual, L.n, st, L.n, L.ptr.p, L.col.p, L.val.p, L.b.p, L.t.p, L.r.p);
     const bool coarsest = (l + 2 == nl);
-    k_amg_restrict<<<nblk(C.n), 256, 0, st>>>(C.n, L.rptr.p, L.rent.p, L.rrow.p, L.pval.p, L.r.p,
-                                              coarsest ? nullptr : C.dl1inv.p, C.b.p, C.x.p);
+    AMG_LAUNCH_G(k_amg_restrict, C.n, st, C.n, L.rptr.p, L.rent.p, L.rrow.p, L.pval.p, L.r.p,
+                 coarsest ? nullptr : C.dl1inv.p, C.b.p, C.x.p);
     launches += 3;
   }
   AmgLevel& C = H->lev.back();
@@ -977,9 +1030,9 @@ template <int NT> void apply_nt(hdg_system* s, const float* val0, const float* b
   for (int l = nl - 2; l >= 0; --l) {
     AmgLevel& L = H->lev[l];
     AmgLevel& Cn = H->lev[l + 1];
-    k_amg_prolong<<<nblk(L.n), 256, 0, st>>>(L.n, L.pptr.p, L.pcol.p, L.pval.p, Cn.x.p, L.t.p);
-    k_amg_l1_sweep<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.t.p, L.r.p);
-    k_amg_l1_sweep<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.r.p, L.x.p);
+    AMG_LAUNCH_G(k_amg_prolong, L.n, st, L.n, L.pptr.p, L.pcol.p, L.pval.p, Cn.x.p, L.t.p);
+    AMG_LAUNCH_G(k_amg_l1_sweep, L.n, st, L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.t.p, L.r.p);
+    AMG_LAUNCH_G(k_amg_l1_sweep, L.n, st, L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.r.p, L.x.p);
     launches += 3;
   }
   // level 0 up: prolongate, degree-2 Chebyshev from the corrected iterate

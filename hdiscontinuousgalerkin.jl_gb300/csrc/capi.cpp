@@ -43,6 +43,15 @@ void set_device(hdg_ctx* ctx) {
 }  // namespace
 
 thread_local cudaStream_t g_alloc_stream = nullptr;
+thread_local cudaStream_t g_use_stream = nullptr;
+
+void order_streams(cudaStream_t before, cudaStream_t after) {
+  cudaEvent_t e;
+  HDG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  HDG_CUDA(cudaEventRecord(e, before));
+  HDG_CUDA(cudaStreamWaitEvent(after, e, 0));
+  HDG_CUDA(cudaEventDestroy(e));
+}
 
 hdg_system::~hdg_system() {
   if (cg) destroy_cg(cg);
@@ -361,8 +370,7 @@ static void set_coefficients(hdg_system* s, double tau, const hdg_field* f, cons
   set_coefficients_many(s, ts.data(), fs.data(), kappa ? ks.data() : nullptr, kappa_cell);
 }
 
-static void assemble_now(hdg_system* s) {
-  cudaStream_t st = s->ctx->stream;
+extern "C++" void assemble_async(hdg_system* s, cudaStream_t st) {
   const bool prof = s->ctx->profiling;
   HDG_CUDA(cudaMemsetAsync(s->d_scal.p, 0, 4 * sizeof(double), st));
   if (prof) s->ev_element.start(st);
@@ -373,6 +381,12 @@ static void assemble_now(hdg_system* s) {
   }
   launch_gather(s, st);
   if (prof) s->ev_gather.stop(st);
+  s->applied = false;
+  s->have_solution = false;
+  s->have_recovery = false;
+}
+
+extern "C++" void assembly_check(hdg_system* s, cudaStream_t st) {
   double sc[2];
   HDG_CUDA(cudaMemcpyAsync(sc, s->d_scal.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
   HDG_CUDA(cudaStreamSynchronize(st));
@@ -380,9 +394,11 @@ static void assemble_now(hdg_system* s) {
   std::memcpy(&err, &sc[1], sizeof(int));
   if (err & 1) throw HdgError{HDG_ERR_NEG_DETJ, "det(J) is not positive on some cell"};
   if (err & 2) throw HdgError{HDG_ERR_SINGULAR, "a local system has a zero pivot (singular)"};
-  s->applied = false;
-  s->have_solution = false;
-  s->have_recovery = false;
+}
+
+static void assemble_now(hdg_system* s) {
+  assemble_async(s, s->ctx->stream);
+  assembly_check(s, s->ctx->stream);
 }
 
 static int assemble_condense_impl(hdg_space* space, double tau, const hdg_field* f, const hdg_field* kappa,
@@ -619,30 +635,63 @@ int hdg_dirichlet(const hdg_space* sp, const char* faceset, const hdg_field* g, 
   return HDG_OK;
 }
 
+// Validates a Dirichlet set, records its faces for the multigrid setup (a new set invalidates the
+// symbolic part) and scatters it on the device.
+static void set_dirichlet_now(hdg_system* s, const int32_t* dofs, const double* vals, int n) {
+  std::vector<int32_t> d0(n);
+  std::vector<double> v(vals, vals + n);
+  for (int k = 0; k < n; ++k) {
+    if (dofs[k] < 1 || dofs[k] > s->ndofs) throw HdgError{HDG_ERR_ARG, "prescribed dof out of range"};
+    d0[k] = dofs[k] - 1;
+  }
+  // prescribed faces (all their dofs are prescribed together): the multigrid setup leaves them
+  // out of its aggregates
+  std::vector<char> dir(s->nf, 0);
+  for (int k = 0; k < n; ++k) dir[d0[k] / s->nt] = 1;
+  if (dir != s->h_dir_face && s->amg) {
+    destroy_amg(s->amg);
+    s->amg = nullptr;
+  }
+  s->h_dir_face.swap(dir);
+  launch_dirichlet_scatter(s, d0, v, s->ctx->stream);
+}
+
 int hdg_apply_dirichlet(hdg_system* s, const int32_t* dofs, const double* vals, int n) {
   if (!s || n < 0 || (n > 0 && (!dofs || !vals))) return HDG_ERR_ARG;
   if (s->applied) return fail(s->ctx, HDG_ERR_ARG, "apply! was already called on this system");
   return guard(s->ctx, [&]() -> int {
     set_device(s->ctx);
-    std::vector<int32_t> d0(n);
-    std::vector<double> v(vals, vals + n);
-    for (int k = 0; k < n; ++k) {
-      if (dofs[k] < 1 || dofs[k] > s->ndofs) return fail(s->ctx, HDG_ERR_ARG, "prescribed dof out of range");
-      d0[k] = dofs[k] - 1;
-    }
-    // prescribed faces (all their dofs are prescribed together): the multigrid setup leaves them
-    // out of its aggregates; a new Dirichlet set invalidates the symbolic setup
-    std::vector<char> dir(s->nf, 0);
-    for (int k = 0; k < n; ++k) dir[d0[k] / s->nt] = 1;
-    if (dir != s->h_dir_face && s->amg) {
-      destroy_amg(s->amg);
-      s->amg = nullptr;
-    }
-    s->h_dir_face.swap(dir);
     if (s->ctx->profiling) s->ev_apply.start(s->ctx->stream);
-    launch_apply_dirichlet(s, d0, v, s->ctx->stream);
+    set_dirichlet_now(s, dofs, vals, n);
+    launch_dirichlet_apply(s, s->ctx->stream);
     if (s->ctx->profiling) s->ev_apply.stop(s->ctx->stream);
     s->applied = true;
+    return HDG_OK;
+  });
+}
+
+int hdg_system_set_dirichlet(hdg_system* s, const int32_t* dofs, const double* vals, int n) {
+  if (!s || n < 0 || (n > 0 && (!dofs || !vals))) return HDG_ERR_ARG;
+  // allowed on an applied system: the set takes effect at the next apply!, which needs a
+  // reassembly first (hdg_batch_step refuses HDG_STEP_APPLY without HDG_STEP_ASSEMBLE there)
+  return guard(s->ctx, [&]() -> int {
+    set_device(s->ctx);
+    set_dirichlet_now(s, dofs, vals, n);
+    return HDG_OK;
+  });
+}
+
+int hdg_system_set_coefficients_batch(hdg_system* s, const double* tau, const hdg_field* f, const hdg_field* kappa,
+                                      const double* kappa_cell) {
+  if (!s || !f) return HDG_ERR_ARG;
+  return guard(s->ctx, [&]() -> int {
+    set_device(s->ctx);
+    std::vector<const hdg_field*> fs(s->nprob), ks(s->nprob);
+    for (int P = 0; P < s->nprob; ++P) {
+      fs[P] = &f[P];
+      ks[P] = kappa ? &kappa[P] : nullptr;
+    }
+    set_coefficients_many(s, tau, fs.data(), kappa ? ks.data() : nullptr, kappa_cell);
     return HDG_OK;
   });
 }
@@ -721,6 +770,16 @@ int hdg_errornorm_l2sq(hdg_system* s, const hdg_field* uex, double* out) {
   });
 }
 
+int hdg_nodal_avg(hdg_system* s, double* out) {
+  if (!s || !out) return HDG_ERR_ARG;
+  if (!s->have_recovery) return fail(s->ctx, HDG_ERR_ARG, "recover first");
+  return guard(s->ctx, [&]() -> int {
+    set_device(s->ctx);
+    run_nodal_avg(s, out, s->ctx->stream);
+    return HDG_OK;
+  });
+}
+
 int hdg_system_timings(hdg_system* s, hdg_timings* out) {
   if (!s || !out) return HDG_ERR_ARG;
   return guard(s->ctx, [&]() -> int {
@@ -772,6 +831,45 @@ int hdg_solve_batch(int nsys, hdg_system* const* systems, const hdg_solver* opts
     size_t k = 0;
     for (int i = 0; i < nsys; ++i) {
       v[i]->have_solution = (rc == HDG_OK || rc == HDG_ERR_NO_CONVERGENCE);
+      for (auto& r : st[i]) {
+        if (stats) stats[k] = r;
+        ++k;
+      }
+    }
+    if (rc == HDG_ERR_NO_CONVERGENCE) return fail(ctx, rc, "some problem did not reach the tolerance within maxit");
+    if (rc == HDG_ERR_BREAKDOWN) return fail(ctx, rc, "CG breakdown in some problem");
+    return rc;
+  });
+}
+
+int hdg_batch_step(int nsys, hdg_system* const* systems, const hdg_solver* opts, int flags, hdg_stats* stats) {
+  if (nsys < 1 || !systems || (flags & ~(HDG_STEP_ASSEMBLE | HDG_STEP_APPLY | HDG_STEP_RECOVER))) return HDG_ERR_ARG;
+  hdg_ctx* ctx = systems[0] ? systems[0]->ctx : nullptr;
+  if (!ctx) return HDG_ERR_ARG;
+  for (int i = 0; i < nsys; ++i) {
+    hdg_system* s = systems[i];
+    if (!s || s->ctx != ctx) return fail(ctx, HDG_ERR_ARG, "the systems of a step must share one context");
+    for (int j = 0; j < i; ++j)
+      if (systems[j] == s) return fail(ctx, HDG_ERR_ARG, "a system appears twice in the step");
+    if (flags & HDG_STEP_APPLY) {
+      if (!s->dir_ready) return fail(ctx, HDG_ERR_ARG, "no Dirichlet set recorded (hdg_system_set_dirichlet)");
+      if (s->applied && !(flags & HDG_STEP_ASSEMBLE))
+        return fail(ctx, HDG_ERR_ARG, "apply! was already called on this system");
+    } else {
+      if (flags & HDG_STEP_ASSEMBLE) return fail(ctx, HDG_ERR_ARG, "assembly undoes apply!: add HDG_STEP_APPLY");
+      if (!s->applied) return fail(ctx, HDG_ERR_ARG, "apply the Dirichlet conditions first");
+    }
+  }
+  return guard(ctx, [&]() -> int {
+    set_device(ctx);
+    hdg_solver o = solver_defaults(opts);
+    std::vector<hdg_system*> v(systems, systems + nsys);
+    std::vector<std::vector<hdg_stats>> st;
+    int rc = run_batch_step(v, o, flags, &st);
+    size_t k = 0;
+    for (int i = 0; i < nsys; ++i) {
+      v[i]->have_solution = (rc == HDG_OK || rc == HDG_ERR_NO_CONVERGENCE);
+      v[i]->have_recovery = v[i]->have_solution && (flags & HDG_STEP_RECOVER);
       for (auto& r : st[i]) {
         if (stats) stats[k] = r;
         ++k;

@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <thread>
 
 #include "hdg_device.cuh"
 
@@ -50,6 +51,7 @@ struct CgState {
   cudaGraphExec_t graph64 = nullptr, graph32 = nullptr;
   int chunk64 = 0, chunk32 = 0;
   bool graph_mg = false;  // graph64 holds the multigrid iteration
+  int graph_amg_gen = -1; // ... of this multigrid setup (hdg_system::amg_gen)
   int32_t* h_st = nullptr;  // pinned mirrors
   double* h_sc = nullptr;
   std::vector<double> rr_best;
@@ -574,15 +576,12 @@ template <int NT> struct SolverNT : CgSolver {
     }
     s->ensure_reduction_buffers();
     s->d_x.alloc(nrow);
-    nseg_full = s->nseg;
-    full_prob.resize(nseg_full); full_r0.resize(nseg_full); full_r1.resize(nseg_full);
-    full_b0.resize(nprob); full_nb.resize(nprob);
-    s->d_seg_prob.download(full_prob.data(), nseg_full, st);
-    s->d_seg_row0.download(full_r0.data(), nseg_full, st);
-    s->d_seg_row1.download(full_r1.data(), nseg_full, st);
-    s->d_prob_blk0.download(full_b0.data(), nprob, st);
-    s->d_prob_nblk.download(full_nb.data(), nprob, st);
-    HDG_CUDA(cudaStreamSynchronize(st));
+    nseg_full = s->nseg;  // full tables (a solve restores them when it ends)
+    full_prob = s->h_seg_prob;
+    full_r0 = s->h_seg_row0;
+    full_r1 = s->h_seg_row1;
+    full_b0 = s->h_prob_blk0;
+    full_nb = s->h_prob_nblk;
     for (auto* e : s->ev_cg_a) delete e;
     for (auto* e : s->ev_cg_b) delete e;
     s->ev_cg_a.clear();
@@ -612,10 +611,14 @@ template <int NT> struct SolverNT : CgSolver {
       k_cg_init_mg<NT><<<s->nseg, CG_BLOCK, 0, st>>>(a64, c->r32.p);
       amg_apply(s, c->r32.p, c->z32.p, st);
       k_cg_c<NT><<<s->nseg, CG_BLOCK, 0, st>>>(a64, c->z32.p, 1, 0);
-      if (c->graph64) { cudaGraphExecDestroy(c->graph64); c->graph64 = nullptr; }  // Jacobi and multigrid differ
-      c->chunk64 = 0;
+      // the graph holds the hierarchy's buffers: rebuilt after a Jacobi solve or a new setup
+      if (c->graph64 && (!c->graph_mg || c->graph_amg_gen != s->amg_gen)) {
+        cudaGraphExecDestroy(c->graph64);
+        c->graph64 = nullptr;
+      }
       build_graph<double>(a64, &c->graph64, &c->chunk64);
       c->graph_mg = true;
+      c->graph_amg_gen = s->amg_gen;
     } else if (!mixed) {
       c->r.alloc(nrow); c->z.alloc(nrow); c->p.alloc(nrow); c->q.alloc(nrow); c->dinv.alloc(nrow);
       k_dinv<NT, double><<<(nrow + 255) / 256, 256, 0, st>>>(nrow, s->d_kdiag.p, s->d_val.p, c->dinv.p);
@@ -888,9 +891,7 @@ CgSolver* make_cg_solver(hdg_system* s) {
   throw HdgError{HDG_ERR_ARG, "degree not supported"};
 }
 
-// Solves every problem of every system; the systems' chunks are interleaved so that one host
-// loop drives a whole degree-binned batch.  stats[i] receives the per-problem results of sys[i].
-int run_solve_many(const std::vector<hdg_system*>& sys, const hdg_solver& o,
+int run_batch_step(const std::vector<hdg_system*>& sys, const hdg_solver& o, int flags,
                    std::vector<std::vector<hdg_stats>>* stats) {
   std::vector<CgSolver*> sv;
   struct Guard {
@@ -900,10 +901,14 @@ int run_solve_many(const std::vector<hdg_system*>& sys, const hdg_solver& o,
     }
   } guard{sv};
   for (auto* s : sys) sv.push_back(make_cg_solver(s));
-  for (auto* x : sv) x->prepare(o);
-  // Several systems (degree bins) iterate on streams of their own, forked from and joined back
-  // to the context's stream, so that one bin's reduction tails and chunk boundaries overlap
-  // with the other bins' work.  Every system allocated its buffers in prepare, before the fork.
+  // The multigrid's symbolic setup is host work (and synchronises): done for every system before
+  // any of them is queued, so that it never stalls the pipeline.  It runs once per system.
+  if (o.preconditioner == HDG_PRECOND_AMG)
+    for (auto* s : sys)
+      if (!s->amg) amg_setup_symbolic(s, s->h_dir_face);
+  // Several systems (degree bins) run on streams of their own, forked from and joined back to
+  // the context's stream: one system's assembly, reduction tails, chunk boundaries and recovery
+  // overlap the other systems' iterations.
   struct Fork {
     std::vector<cudaStream_t> streams;
     std::vector<cudaEvent_t> events;
@@ -917,7 +922,9 @@ int run_solve_many(const std::vector<hdg_system*>& sys, const hdg_solver& o,
       for (auto q : streams) cudaStreamDestroy(q);
     }
   } fork;
-  if (sv.size() > 1) {
+  const size_t ns = sv.size();
+  std::vector<cudaStream_t> q(ns, sys[0]->ctx->stream);
+  if (ns > 1) {
     fork.home = sys[0]->ctx->stream;
     cudaEvent_t start;
     HDG_CUDA(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
@@ -927,37 +934,88 @@ int run_solve_many(const std::vector<hdg_system*>& sys, const hdg_solver& o,
         HDG_CUDA(cudaStreamWaitEvent(fork.home, start, 0));
       }
     HDG_CUDA(cudaEventRecord(start, fork.home));
-    for (auto* x : sv) {
-      cudaStream_t q;
+    for (size_t i = 0; i < ns; ++i) {
+      cudaStream_t qs;
       cudaEvent_t e;
-      HDG_CUDA(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
-      fork.streams.push_back(q);
+      HDG_CUDA(cudaStreamCreateWithFlags(&qs, cudaStreamNonBlocking));
+      fork.streams.push_back(qs);
       HDG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
       fork.events.push_back(e);
-      HDG_CUDA(cudaStreamWaitEvent(q, start, 0));
-      x->set_stream(q);
+      HDG_CUDA(cudaStreamWaitEvent(qs, start, 0));
+      q[i] = qs;
     }
     HDG_CUDA(cudaEventDestroy(start));
+  } else {
+    q[0] = sys[0]->ctx->stream;
   }
-  std::vector<char> done(sv.size(), 0);
-  for (int rep = 0;; ++rep) {
-    bool all = true;
-    for (size_t i = 0; i < sv.size(); ++i)
-      if (!done[i]) {
-        sv[i]->launch_chunk(rep);
-        sv[i]->enqueue_status_copy();
-        all = false;
+  // per system: [assembly] -> [apply!] -> initialisation -> first chunk, queued system by system
+  std::vector<cudaEvent_t> ready(ns);
+  struct EvGuard {
+    std::vector<cudaEvent_t>& v;
+    ~EvGuard() {
+      for (auto e : v)
+        if (e) cudaEventDestroy(e);
+    }
+  } evguard{ready};
+  struct UseStream {  // buffers allocated while a system is queued are ordered before its stream
+    ~UseStream() { g_use_stream = nullptr; }
+  } use_stream;
+  for (size_t i = 0; i < ns; ++i) {
+    hdg_system* s = sys[i];
+    const bool prof = s->ctx->profiling;
+    g_use_stream = q[i];
+    HDG_CUDA(cudaEventCreateWithFlags(&ready[i], cudaEventDisableTiming));
+    if (flags & HDG_STEP_ASSEMBLE) assemble_async(s, q[i]);
+    if (flags & HDG_STEP_APPLY) {
+      if (prof) s->ev_apply.start(q[i]);
+      launch_dirichlet_apply(s, q[i]);
+      if (prof) s->ev_apply.stop(q[i]);
+      s->applied = true;
+    }
+    sv[i]->set_stream(q[i]);
+    sv[i]->prepare(o);
+    sv[i]->launch_chunk(0);
+    sv[i]->enqueue_status_copy();
+    HDG_CUDA(cudaEventRecord(ready[i], q[i]));
+  }
+  // Event-driven host loop: a system whose status read-back has landed is processed and given its
+  // next chunk at once, without waiting for the others.
+  stats->assign(ns, {});
+  std::vector<char> done(ns, 0);
+  std::vector<int> rep(ns, 0);
+  size_t left = ns;
+  while (left > 0) {
+    bool progressed = false;
+    for (size_t i = 0; i < ns; ++i) {
+      if (done[i]) continue;
+      const cudaError_t qe = cudaEventQuery(ready[i]);
+      if (qe == cudaErrorNotReady) continue;
+      HDG_CUDA(qe);
+      progressed = true;
+      g_use_stream = q[i];
+      if (sv[i]->process(o)) {
+        sv[i]->finish(o, &(*stats)[i]);
+        if (flags & HDG_STEP_RECOVER) {
+          hdg_system* s = sys[i];
+          if (s->ctx->profiling) s->ev_recover.start(q[i]);
+          launch_recover(s, q[i]);
+          if (s->ctx->profiling) s->ev_recover.stop(q[i]);
+        }
+        done[i] = 1;
+        --left;
+        continue;
       }
-    if (all) break;
-    for (size_t i = 0; i < sv.size(); ++i)
-      if (!done[i]) HDG_CUDA(cudaStreamSynchronize(fork.streams.empty() ? sv[i]->s->ctx->stream : fork.streams[i]));
-    for (size_t i = 0; i < sv.size(); ++i)
-      if (!done[i] && sv[i]->process(o)) done[i] = 1;
+      sv[i]->launch_chunk(++rep[i]);
+      sv[i]->enqueue_status_copy();
+      HDG_CUDA(cudaEventRecord(ready[i], q[i]));
+    }
+    if (!progressed) std::this_thread::yield();
   }
-  stats->resize(sv.size());
+  g_use_stream = nullptr;
+  if (flags & HDG_STEP_ASSEMBLE)  // element error flags (the step went on regardless)
+    for (size_t i = 0; i < ns; ++i) assembly_check(sys[i], q[i]);
   int rc = HDG_OK;
-  for (size_t i = 0; i < sv.size(); ++i) {
-    sv[i]->finish(o, &(*stats)[i]);
+  for (size_t i = 0; i < ns; ++i) {
     for (auto& r : (*stats)[i]) {
       if (r.converged < 0) {
         r.converged = 0;
@@ -968,6 +1026,13 @@ int run_solve_many(const std::vector<hdg_system*>& sys, const hdg_solver& o,
     }
   }
   return rc;
+}
+
+// Solves every problem of every system; the systems' chunks are interleaved so that one host
+// loop drives a whole degree-binned batch.  stats[i] receives the per-problem results of sys[i].
+int run_solve_many(const std::vector<hdg_system*>& sys, const hdg_solver& o,
+                   std::vector<std::vector<hdg_stats>>* stats) {
+  return run_batch_step(sys, o, 0, stats);
 }
 
 int run_solve(hdg_system* s, const hdg_solver& o, hdg_stats* stats) {

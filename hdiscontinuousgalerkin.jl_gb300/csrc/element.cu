@@ -33,6 +33,7 @@ struct ElemArgs {
   double* AB;
   double* KB;
   int* err;
+  int schur;  // 1: the Schur-complement path (invertible reference mass, kappa constant per cell)
 };
 
 // One warp per cell; EWARPS warps (cells) per CTA, picked per degree, quadrature size and mesh
@@ -57,6 +58,13 @@ template <int P, int EWARPS> __global__ void __launch_bounds__(EWARPS * 32) k_el
     l.NW = o; o += NW * nq;
     l.N = o; o += NW * nq;
     l.Q = o; o += 2 * nq;
+    l.SMD0 = o; o += NW * NW;
+    l.SMD1 = o; o += NW * NW;
+    l.SQ00 = o; o += NW * NW;
+    l.SQ01 = o; o += NW * NW;
+    l.SQ11 = o; o += NW * NW;
+    l.SMF = o; o += 6 * NW * NT;
+    l.SDMF = o; o += 12 * NW * NT;
     l.total = o;
     return l;
   }();
@@ -111,103 +119,209 @@ template <int P, int EWARPS> __global__ void __launch_bounds__(EWARPS * 32) k_el
       be[i] = s * detJ;
     }
     __syncwarp();
-    // ---- augmented local system ----------------------------------------------------------
-    for (int idx = lane; idx < N * NC; idx += 32) {
-      const int r = idx / NC, col = idx - (idx / NC) * NC;
-      double v;
-      if (r < NV) {
-        const int c = r / NW, ia = r - c * NW;
-        const double adl0 = c ? ad01 : ad00, adl1 = c ? ad11 : ad10;
-        if (col < NV) {
-          const int c2 = col / NW, ib = col - c2 * NW;
-          if (c2 != c) {
-            v = 0.0;
-          } else if (a.kappa_mode == 2) {
-            double s = 0.0;
-            for (int q = 0; q < nq; ++q) s += ref[L.NW + ia * nq + q] * sq[nq + q] * ref[L.N + ib * nq + q];
-            v = s * detJ;
-          } else {
-            v = smass * ref[L.M + ia * NW + ib];
-          }
-        } else if (col < N) {
-          const int j = col - NV;
-          v = -(adl0 * ref[L.D0 + ia * NW + j] + adl1 * ref[L.D1 + ia * NW + j]);
-        } else if (col < N + M) {
-          const int f = (col - N) / NT, j = (col - N) - f * NT;
-          const int o = (ob >> f) & 1;
-          v = -wn[f][c] * ref[L.F + ((f * 2 + o) * NW + ia) * NT + j];
-        } else {
-          v = 0.0;
-        }
-      } else {
-        const int ia = r - NV;
-        if (col < NV) {
-          const int c2 = col / NW, ib = col - c2 * NW;
-          const double adl0 = c2 ? ad01 : ad00, adl1 = c2 ? ad11 : ad10;
-          v = adl0 * ref[L.D0 + ib * NW + ia] + adl1 * ref[L.D1 + ib * NW + ia];
-        } else if (col < N) {
-          const int ib = col - NV;
+    if (a.schur) {
+      // ---- Schur-complement path ------------------------------------------------------------
+      // Me = [A -B; B' C] with A = (det J / kappa) diag(M, M), so with kf = kappa / det J:
+      //   S  = C + kf sum_c B_c' M^-1 B_c = C + kf (a00 Q00 + a01 (Q01 + Q01') + a11 Q11),
+      //   X2 = S^-1 (R2 - B' A^-1 R1),   B' A^-1 R1 = -kf sum_l b_l^f DMF_{l,f,o},
+      //   X1 = A^-1 (R1 + B X2) = kf (-wn_f,c MF_{f,o} + (adl0_c MD0 + adl1_c MD1) X2),
+      // where B_c = adl0_c D0 + adl1_c D1 and R = [-Ee ; Fe | 0 ; be] (the same right-hand sides
+      // as the full system).  S is nw x nw: eliminated with partial pivoting like the full LU.
+      constexpr int RC = NW + M + 1;  // reduced augmented columns [S | R2']
+      const double kf = 1.0 / smass;
+      const double a00 = ad00 * ad00 + ad01 * ad01, a11 = ad10 * ad10 + ad11 * ad11, a01 = ad00 * ad10 + ad01 * ad11;
+      double b0f[3], b1f[3];
+#pragma unroll
+      for (int f = 0; f < 3; ++f) {
+        b0f[f] = ad00 * wn[f][0] + ad01 * wn[f][1];
+        b1f[f] = ad10 * wn[f][0] + ad11 * wn[f][1];
+      }
+      for (int idx = lane; idx < NW * RC; idx += 32) {
+        const int ia = idx / RC, col = idx - ia * RC;
+        double v;
+        if (col < NW) {
+          const int ib = col;
           v = tau * (el[0] * ref[L.C + (0 * NW + ia) * NW + ib] + el[1] * ref[L.C + (1 * NW + ia) * NW + ib] +
-                     el[2] * ref[L.C + (2 * NW + ia) * NW + ib]);
-        } else if (col < N + M) {
-          const int f = (col - N) / NT, j = (col - N) - f * NT;
+                     el[2] * ref[L.C + (2 * NW + ia) * NW + ib]) +
+              kf * (a00 * ref[L.SQ00 + ia * NW + ib] + a01 * (ref[L.SQ01 + ia * NW + ib] + ref[L.SQ01 + ib * NW + ia]) +
+                    a11 * ref[L.SQ11 + ia * NW + ib]);
+        } else if (col < NW + M) {
+          const int f = (col - NW) / NT, j = (col - NW) - f * NT;
           const int o = (ob >> f) & 1;
-          v = tau * el[f] * ref[L.F + ((f * 2 + o) * NW + ia) * NT + j];
+          v = tau * el[f] * ref[L.F + ((f * 2 + o) * NW + ia) * NT + j] +
+              kf * (b0f[f] * ref[L.SDMF + ((0 * 6 + f * 2 + o) * NW + ia) * NT + j] +
+                    b1f[f] * ref[L.SDMF + ((1 * 6 + f * 2 + o) * NW + ia) * NT + j]);
         } else {
           v = be[ia];
         }
+        W[ia * LD + col] = v;
       }
-      W[r * LD + col] = v;
-    }
-    __syncwarp();
-    // ---- Gaussian elimination with partial pivoting --------------------------------------
-    // The pivot search compares |a_ik| through its bit pattern: for non-negative IEEE doubles
-    // the unsigned-integer order of the bits is the numeric order, so the search runs on the
-    // integer pipe instead of the (narrow) FP64 pipe.  Ties keep the smallest row, as idamax.
-    double* rinv = be + NW;  // reciprocals of the pivots, reused by the back substitution
-    for (int k = 0; k < N; ++k) {
-      unsigned long long best = 0ull;
-      int bi = N;
-      for (int i = k + lane; i < N; i += 32) {
-        const unsigned long long v = (unsigned long long)__double_as_longlong(W[i * LD + k]) & 0x7fffffffffffffffull;
-        if (v > best || (v == best && i < bi)) { best = v; bi = i; }
-      }
+      __syncwarp();
+      double* rinv = be + NW;
+      for (int k = 0; k < NW; ++k) {
+        unsigned long long best = 0ull;
+        int bi = NW;
+        for (int i = k + lane; i < NW; i += 32) {
+          const unsigned long long v = (unsigned long long)__double_as_longlong(W[i * LD + k]) & 0x7fffffffffffffffull;
+          if (v > best || (v == best && i < bi)) { best = v; bi = i; }
+        }
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long ov = __shfl_xor_sync(0xffffffffu, best, o);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
-      }
-      if (best == 0ull && lane == 0) atomicOr(a.err, 2);
-      if (bi != k) {
-        for (int j = k + lane; j < NC; j += 32) {
-          double t = W[k * LD + j];
-          W[k * LD + j] = W[bi * LD + j];
-          W[bi * LD + j] = t;
+        for (int o = 16; o > 0; o >>= 1) {
+          const unsigned long long ov = __shfl_xor_sync(0xffffffffu, best, o);
+          const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+          if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+        }
+        if (best == 0ull && lane == 0) atomicOr(a.err, 2);
+        if (bi != k) {
+          for (int j = k + lane; j < RC; j += 32) {
+            double t = W[k * LD + j];
+            W[k * LD + j] = W[bi * LD + j];
+            W[bi * LD + j] = t;
+          }
+          __syncwarp();
+        }
+        const double pinv = 1.0 / W[k * LD + k];
+        if (lane == 0) rinv[k] = pinv;
+        for (int i = k + 1 + lane; i < NW; i += 32) W[i * LD + k] *= pinv;
+        __syncwarp();
+        const int cols = RC - k - 1, rows = NW - k - 1;
+        for (int t = lane; t < rows * cols; t += 32) {
+          const int i = k + 1 + t / cols, j = k + 1 + (t - (t / cols) * cols);
+          W[i * LD + j] -= W[i * LD + k] * W[k * LD + j];
         }
         __syncwarp();
       }
-      const double pinv = 1.0 / W[k * LD + k];
-      if (lane == 0) rinv[k] = pinv;
-      for (int i = k + 1 + lane; i < N; i += 32) W[i * LD + k] *= pinv;
-      __syncwarp();
-      const int cols = NC - k - 1, rows = N - k - 1;
-      for (int t = lane; t < rows * cols; t += 32) {
-        const int i = k + 1 + t / cols, j = k + 1 + (t - (t / cols) * cols);
-        W[i * LD + j] -= W[i * LD + k] * W[k * LD + j];
+      for (int k = NW - 1; k >= 0; --k) {
+        const double dinv = rinv[k];
+        for (int j = lane; j <= M; j += 32) W[k * LD + NW + j] *= dinv;
+        __syncwarp();
+        for (int t = lane; t < k * (M + 1); t += 32) {
+          const int i = t / (M + 1), j = t - (t / (M + 1)) * (M + 1);
+          W[i * LD + NW + j] -= W[i * LD + k] * W[k * LD + NW + j];
+        }
+        __syncwarp();
+      }
+      // X2 -> the u rows of X (rows NV.., columns N..), clear of the reduced system's rows
+      for (int t = lane; t < NW * (M + 1); t += 32) {
+        const int ib = t / (M + 1), j = t - ib * (M + 1);
+        W[(NV + ib) * LD + N + j] = W[ib * LD + NW + j];
       }
       __syncwarp();
-    }
-    // ---- back substitution on the m+1 right-hand sides -----------------------------------
-    for (int k = N - 1; k >= 0; --k) {
-      const double dinv = rinv[k];
-      for (int j = lane; j <= M; j += 32) W[k * LD + N + j] *= dinv;
-      __syncwarp();
-      for (int t = lane; t < k * (M + 1); t += 32) {
-        const int i = t / (M + 1), j = t - (t / (M + 1)) * (M + 1);
-        W[i * LD + N + j] -= W[i * LD + k] * W[k * LD + N + j];
+      // X1 -> the q rows of X
+      for (int t = lane; t < NV * (M + 1); t += 32) {
+        const int r = t / (M + 1), j = t - r * (M + 1);
+        const int c = r / NW, ia = r - c * NW;
+        const double adl0 = c ? ad01 : ad00, adl1 = c ? ad11 : ad10;
+        double s = 0.0;
+        for (int ib = 0; ib < NW; ++ib)
+          s += (adl0 * ref[L.SMD0 + ia * NW + ib] + adl1 * ref[L.SMD1 + ia * NW + ib]) * W[(NV + ib) * LD + N + j];
+        if (j < M) {
+          const int f = j / NT, jj = j - f * NT;
+          const int o = (ob >> f) & 1;
+          s -= wn[f][c] * ref[L.SMF + ((f * 2 + o) * NW + ia) * NT + jj];
+        }
+        W[r * LD + N + j] = kf * s;
       }
       __syncwarp();
+    } else {
+      // ---- augmented local system ----------------------------------------------------------
+      for (int idx = lane; idx < N * NC; idx += 32) {
+        const int r = idx / NC, col = idx - (idx / NC) * NC;
+        double v;
+        if (r < NV) {
+          const int c = r / NW, ia = r - c * NW;
+          const double adl0 = c ? ad01 : ad00, adl1 = c ? ad11 : ad10;
+          if (col < NV) {
+            const int c2 = col / NW, ib = col - c2 * NW;
+            if (c2 != c) {
+              v = 0.0;
+            } else if (a.kappa_mode == 2) {
+              double s = 0.0;
+              for (int q = 0; q < nq; ++q) s += ref[L.NW + ia * nq + q] * sq[nq + q] * ref[L.N + ib * nq + q];
+              v = s * detJ;
+            } else {
+              v = smass * ref[L.M + ia * NW + ib];
+            }
+          } else if (col < N) {
+            const int j = col - NV;
+            v = -(adl0 * ref[L.D0 + ia * NW + j] + adl1 * ref[L.D1 + ia * NW + j]);
+          } else if (col < N + M) {
+            const int f = (col - N) / NT, j = (col - N) - f * NT;
+            const int o = (ob >> f) & 1;
+            v = -wn[f][c] * ref[L.F + ((f * 2 + o) * NW + ia) * NT + j];
+          } else {
+            v = 0.0;
+          }
+        } else {
+          const int ia = r - NV;
+          if (col < NV) {
+            const int c2 = col / NW, ib = col - c2 * NW;
+            const double adl0 = c2 ? ad01 : ad00, adl1 = c2 ? ad11 : ad10;
+            v = adl0 * ref[L.D0 + ib * NW + ia] + adl1 * ref[L.D1 + ib * NW + ia];
+          } else if (col < N) {
+            const int ib = col - NV;
+            v = tau * (el[0] * ref[L.C + (0 * NW + ia) * NW + ib] + el[1] * ref[L.C + (1 * NW + ia) * NW + ib] +
+                       el[2] * ref[L.C + (2 * NW + ia) * NW + ib]);
+          } else if (col < N + M) {
+            const int f = (col - N) / NT, j = (col - N) - f * NT;
+            const int o = (ob >> f) & 1;
+            v = tau * el[f] * ref[L.F + ((f * 2 + o) * NW + ia) * NT + j];
+          } else {
+            v = be[ia];
+          }
+        }
+        W[r * LD + col] = v;
+      }
+      __syncwarp();
+      // ---- Gaussian elimination with partial pivoting --------------------------------------
+      // The pivot search compares |a_ik| through its bit pattern: for non-negative IEEE doubles
+      // the unsigned-integer order of the bits is the numeric order, so the search runs on the
+      // integer pipe instead of the (narrow) FP64 pipe.  Ties keep the smallest row, as idamax.
+      double* rinv = be + NW;  // reciprocals of the pivots, reused by the back substitution
+      for (int k = 0; k < N; ++k) {
+        unsigned long long best = 0ull;
+        int bi = N;
+        for (int i = k + lane; i < N; i += 32) {
+          const unsigned long long v = (unsigned long long)__double_as_longlong(W[i * LD + k]) & 0x7fffffffffffffffull;
+          if (v > best || (v == best && i < bi)) { best = v; bi = i; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const unsigned long long ov = __shfl_xor_sync(0xffffffffu, best, o);
+          const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+          if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+        }
+        if (best == 0ull && lane == 0) atomicOr(a.err, 2);
+        if (bi != k) {
+          for (int j = k + lane; j < NC; j += 32) {
+            double t = W[k * LD + j];
+            W[k * LD + j] = W[bi * LD + j];
+            W[bi * LD + j] = t;
+          }
+          __syncwarp();
+        }
+        const double pinv = 1.0 / W[k * LD + k];
+        if (lane == 0) rinv[k] = pinv;
+        for (int i = k + 1 + lane; i < N; i += 32) W[i * LD + k] *= pinv;
+        __syncwarp();
+        const int cols = NC - k - 1, rows = N - k - 1;
+        for (int t = lane; t < rows * cols; t += 32) {
+          const int i = k + 1 + t / cols, j = k + 1 + (t - (t / cols) * cols);
+          W[i * LD + j] -= W[i * LD + k] * W[k * LD + j];
+        }
+        __syncwarp();
+      }
+      // ---- back substitution on the m+1 right-hand sides -----------------------------------
+      for (int k = N - 1; k >= 0; --k) {
+        const double dinv = rinv[k];
+        for (int j = lane; j <= M; j += 32) W[k * LD + N + j] *= dinv;
+        __syncwarp();
+        for (int t = lane; t < k * (M + 1); t += 32) {
+          const int i = t / (M + 1), j = t - (t / (M + 1)) * (M + 1);
+          W[i * LD + N + j] -= W[i * LD + k] * W[k * LD + N + j];
+        }
+        __syncwarp();
+      }
     }
     // ---- K_e, b_e out; Y_f = wn_f,x X_qx + wn_f,y X_qy + tau |e_f| X_u into the free columns --
     double* KB = a.KB + (size_t)e * N * (M + 1);
@@ -289,21 +403,21 @@ template <int P> bool launch_cfg(hdg_system* s, cudaStream_t st, const ElemArgs&
   return false;
 }
 
-// Autotuner: the first launch for a (device, degree, quadrature size, log2 of the cell count)
+// Autotuner: the first launch for a (device, degree, quadrature size, log2 of the cell count, path)
 // times every (warps per CTA, grid oversubscription) pair on the real inputs (the kernel only
 // writes its outputs from its inputs, and every configuration computes each cell with the same
 // instruction sequence, so the results are bit-identical) and keeps the fastest.  The choice is
 // cached for the process.  HDG_ELEMENT_WARPS=<1|2|4|8> fixes the warps per CTA instead.
 template <int P> void launch_p(hdg_system* s, cudaStream_t st, const ElemArgs& a) {
   static std::mutex mu;
-  static std::map<std::tuple<int, int, int>, std::pair<int, int>> best;
+  static std::map<std::tuple<int, int, int, int>, std::pair<int, int>> best;
   if (const char* env = std::getenv("HDG_ELEMENT_WARPS")) {
     if (!launch_cfg<P>(s, st, a, std::atoi(env), 4)) throw HdgError{HDG_ERR_ARG, "HDG_ELEMENT_WARPS does not fit"};
     return;
   }
   int lg = 0;
   while ((1L << (lg + 1)) <= (long)a.nc) ++lg;
-  const auto key = std::make_tuple(s->ctx->device, a.nq, lg);
+  const auto key = std::make_tuple(s->ctx->device, a.nq, lg, a.schur);
   {
     std::lock_guard<std::mutex> lk(mu);
     auto it = best.find(key);
@@ -333,6 +447,7 @@ template <int P> void launch_p(hdg_system* s, cudaStream_t st, const ElemArgs& a
     }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (best_ms == 1e30f) throw HdgError{HDG_ERR_ARG, "no element-kernel configuration fits in shared memory"};
   {
     std::lock_guard<std::mutex> lk(mu);
     best[key] = pick;
@@ -359,6 +474,11 @@ void launch_element_condense(hdg_system* s, cudaStream_t st) {
   a.AB = s->d_AB.p;
   a.KB = s->d_KB.p;
   a.err = reinterpret_cast<int*>(s->d_scal.p + 1);
+  // Schur path: invertible reference mass and kappa constant on each cell (a kappa field makes
+  // Ae a weighted mass matrix that is no multiple of the reference one)
+  a.schur = (sp->t.schur && a.kappa_mode != 2 && std::getenv("HDG_ELEMENT_FULL_LU") == nullptr) ? 1 : 0;
+  // the Schur tables sit at the end of the packed table: the full-LU path leaves them in HBM
+  if (!a.schur) a.ref_len = ref_layout(sp->t.nw, sp->t.nt, sp->t.nq).SMD0;
   switch (sp->t.p) {
     case 1: launch_p<1>(s, st, a); break;
     case 2: launch_p<2>(s, st, a); break;

@@ -30,6 +30,10 @@ struct HdgError {
 // owns the object (set by every C-ABI entry point): a batch or a served request allocates and
 // frees its buffers without synchronising the device, and freed memory stays in the pool.
 extern thread_local cudaStream_t g_alloc_stream;
+// Stream that will use buffers allocated now, when it is not the allocation stream (a forked
+// stream of a pipelined batch step): a new allocation is ordered before that stream's later work.
+extern thread_local cudaStream_t g_use_stream;
+void order_streams(cudaStream_t before, cudaStream_t after);  // `after` waits for `before`'s work so far
 template <class T> struct DevBuf {
   T* p = nullptr;
   size_t n = 0;
@@ -65,6 +69,7 @@ template <class T> struct DevBuf {
     s = g_alloc_stream;
     HDG_CUDA(cudaMallocAsync((void**)&p, count * sizeof(T), s));
     n = count;
+    if (g_use_stream && g_use_stream != s) order_streams(s, g_use_stream);
   }
   void upload(const T* h, size_t count, cudaStream_t s) {
     alloc(count);
@@ -182,6 +187,8 @@ struct RefTables {
   std::vector<double> N, dN;       // [nw][nq], [nw][nq][2]
   std::vector<double> E;           // [nw][nfq][3]
   std::vector<double> T;           // [nt][nfq]
+  std::vector<double> Nv;          // [nw][3] basis at the reference vertices (0,0), (1,0), (0,1)
+  bool schur = false;              // the reference mass matrix is invertible (see tables.cpp)
   // packed device tables (see tables.cpp: ref_layout)
   std::vector<double> packed;
 };
@@ -189,7 +196,10 @@ bool build_ref_tables(int p, int qd, RefTables* t);
 
 // Offsets of the packed table, in doubles.
 struct RefLayout {
-  int M, D0, D1, C, F, H, NW, N, Q, total;
+  int M, D0, D1, C, F, H, NW, N, Q;
+  // Schur-complement tables (valid when RefTables::schur): M^-1 D_l, Q_lm = D_l' M^-1 D_m,
+  // MF_{f,o} = M^-1 F_{f,o}, DMF_{l,f,o} = D_l' M^-1 F_{f,o}
+  int SMD0, SMD1, SQ00, SQ01, SQ11, SMF, SDMF, total;
 };
 RefLayout ref_layout(int nw, int nt, int nq);
 
@@ -221,13 +231,15 @@ struct hdg_system {
   DevBuf<double> d_mdiag;           // [nprob] mean |diag K| per problem
   DevBuf<int32_t> d_prob_row0;      // [nprob+1]
   DevBuf<int32_t>& d_prob_row0_dev() {
-    if (!d_prob_row0.p) d_prob_row0.upload(h_prob_row0.data(), h_prob_row0.size(), ctx->stream);
+    if (!d_prob_row0.p)
+      d_prob_row0.upload(h_prob_row0.data(), h_prob_row0.size(), g_use_stream ? g_use_stream : ctx->stream);
     return d_prob_row0;
   }
   // Segments: the CUDA blocks of the row-parallel kernels (CG, meandiag, residual); each block
   // covers a row range inside one problem, so per-problem reductions need no cross-problem sums.
   int nseg = 0;
   DevBuf<int32_t> d_seg_prob, d_seg_row0, d_seg_row1, d_prob_blk0, d_prob_nblk;
+  std::vector<int32_t> h_seg_prob, h_seg_row0, h_seg_row1, h_prob_blk0, h_prob_nblk;  // host copies
   CoefDev coef_dev() const {
     return CoefDev{space->mesh->d_cell_prob.p, d_fkind.p, d_foff.p, d_fprm.p, d_kkind.p, d_koff.p, d_kprm.p,
                    d_tau.p};
@@ -256,6 +268,8 @@ struct hdg_system {
   DevBuf<double> d_b;     // rhs
   // Dirichlet state
   bool applied = false;   // apply! done: d_val/d_b are in solver form (free rows negated)
+  bool dir_ready = false; // d_pres/d_gv hold a Dirichlet set (scattered; survives reassembly)
+  bool dir_lift = false;  // some prescribed value is nonzero
   DevBuf<uint8_t> d_pres;
   DevBuf<double> d_gv;    // prescribed values scattered to dofs
   DevBuf<int32_t> d_dofs; // prescribed dofs (0-based)
@@ -277,6 +291,7 @@ struct hdg_system {
   bool have_solution = false, have_recovery = false;
   CgState* cg = nullptr;
   AmgHierarchy* amg = nullptr;      // multigrid preconditioner (symbolic part kept across reassembly)
+  int amg_gen = 0;                  // count of symbolic setups (captured CG graphs hold their buffers)
   std::vector<char> h_dir_face;     // faces whose dofs apply! prescribed (set by hdg_apply_dirichlet)
   ~hdg_system();
   // partials: 2 per segment; tickets: 4 per problem (CG product, CG update, residual, meandiag)
@@ -285,7 +300,7 @@ struct hdg_system {
     if (d_part.n < np) d_part.alloc(np);
     if (d_cnt.n < nc) {
       d_cnt.alloc(nc);
-      HDG_CUDA(cudaMemsetAsync(d_cnt.p, 0, nc * sizeof(unsigned), ctx->stream));
+      HDG_CUDA(cudaMemsetAsync(d_cnt.p, 0, nc * sizeof(unsigned), g_use_stream ? g_use_stream : ctx->stream));
     }
   }
 };
@@ -294,7 +309,16 @@ struct hdg_system {
 void launch_element_condense(hdg_system* s, cudaStream_t st);
 void launch_gather(hdg_system* s, cudaStream_t st);
 void launch_apply_dirichlet(hdg_system* s, const std::vector<int32_t>& dofs0, const std::vector<double>& vals,
-                            cudaStream_t st);
+                            cudaStream_t st);  // scatter + apply
+void launch_dirichlet_scatter(hdg_system* s, const std::vector<int32_t>& dofs0, const std::vector<double>& vals,
+                              cudaStream_t st);
+void launch_dirichlet_apply(hdg_system* s, cudaStream_t st);  // apply! from the scattered set
+void assemble_async(hdg_system* s, cudaStream_t st);          // element + gather, errors left on the device
+void assembly_check(hdg_system* s, cudaStream_t st);          // read the element error flags (synchronises)
+// One pipelined step over several systems: each system's (assembly, apply!, CG, recovery) runs on a
+// stream of its own, so that one system's assembly overlaps the others' iterations.
+int run_batch_step(const std::vector<hdg_system*>& sys, const hdg_solver& o, int flags,
+                   std::vector<std::vector<hdg_stats>>* stats);
 int run_solve(hdg_system* s, const hdg_solver& o, hdg_stats* st);
 int run_solve_many(const std::vector<hdg_system*>& sys, const hdg_solver& o,
                    std::vector<std::vector<hdg_stats>>* stats);
@@ -315,6 +339,7 @@ CgSolver* make_cg_solver(hdg_system* s);
 void mesh_concat(hdg_mesh* out, const std::vector<const hdg_mesh*>& parts);
 void launch_recover(hdg_system* s, cudaStream_t st);
 double run_errornorm(hdg_system* s, const FieldSpec& uex, cudaStream_t st);
+void run_nodal_avg(hdg_system* s, double* host_out, cudaStream_t st);
 void destroy_cg(CgState* c);
 void destroy_amg(AmgHierarchy* h);
 void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face);

@@ -1,5 +1,7 @@
 // Local recovery of (q, u) from the trace solution (get_uσ!, examples/poisson2D_HDG.jl:197-212)
 // and the squared L2 error (errornorm, src/DiscreteFunctions.jl:97-120).
+#include <vector>
+
 #include "hdg_device.cuh"
 
 namespace {
@@ -106,7 +108,68 @@ template <int P> double errornorm_p(hdg_system* s, const FieldSpec& uex, cudaStr
   return h;
 }
 
+// u_h at the three vertices of every cell: uv[c][k] = sum_a u[c,a] N_a(vertex k)
+template <int P>
+__global__ void k_vertex_values(const int nc, const double* __restrict__ qu, const double* __restrict__ nv,
+                                double* __restrict__ uv) {
+  using D = Dims<P>;
+  constexpr int NW = D::NW, N = D::N, NV = D::NV;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)nc * 3) return;
+  const int c = (int)(t / 3), k = (int)(t - (int64_t)c * 3);
+  double s = 0.0;
+#pragma unroll
+  for (int a = 0; a < NW; ++a) s += qu[(int64_t)c * N + NV + a] * nv[a * 3 + k];
+  uv[t] = s;
+}
+
+// nodal_avg: every node averages the vertex values of its cells, summed in cell order
+__global__ void k_node_average(const int nn, const int32_t* __restrict__ ptr, const int32_t* __restrict__ ent,
+                               const double* __restrict__ uv, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nn) return;
+  double s = 0.0;
+  for (int e = ptr[i]; e < ptr[i + 1]; ++e) s += uv[ent[e]];
+  out[i] = (ptr[i + 1] > ptr[i]) ? s / (double)(ptr[i + 1] - ptr[i]) : 0.0;
+}
+
+template <int P> void nodal_avg_p(hdg_system* s, double* host_out, cudaStream_t st) {
+  hdg_space* sp = s->space;
+  hdg_mesh* m = sp->mesh;
+  // node -> (cell, vertex) entries in cell order
+  std::vector<int32_t> ptr(m->nn + 1, 0), ent((size_t)m->nc * 3);
+  for (int c = 0; c < m->nc; ++c)
+    for (int k = 0; k < 3; ++k) ++ptr[m->cells[3 * c + k] + 1];
+  for (int i = 0; i < m->nn; ++i) ptr[i + 1] += ptr[i];
+  std::vector<int32_t> fill(ptr.begin(), ptr.end() - 1);
+  for (int c = 0; c < m->nc; ++c)
+    for (int k = 0; k < 3; ++k) ent[fill[m->cells[3 * c + k]]++] = 3 * c + k;
+  DevBuf<int32_t> dptr, dent;
+  DevBuf<double> nv, uv, out;
+  dptr.upload(ptr.data(), ptr.size(), st);
+  dent.upload(ent.data(), ent.size(), st);
+  nv.upload(sp->t.Nv.data(), sp->t.Nv.size(), st);
+  uv.alloc((size_t)m->nc * 3);
+  out.alloc(m->nn);
+  const int64_t tot = (int64_t)m->nc * 3;
+  k_vertex_values<P><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(m->nc, s->d_qu.p, nv.p, uv.p);
+  k_node_average<<<(m->nn + 255) / 256, 256, 0, st>>>(m->nn, dptr.p, dent.p, uv.p, out.p);
+  HDG_CUDA(cudaGetLastError());
+  s->ctx->launches += 2;
+  out.download(host_out, m->nn, st);
+  HDG_CUDA(cudaStreamSynchronize(st));
+}
+
 }  // namespace
+
+void run_nodal_avg(hdg_system* s, double* host_out, cudaStream_t st) {
+  switch (s->space->t.p) {
+    case 1: nodal_avg_p<1>(s, host_out, st); break;
+    case 2: nodal_avg_p<2>(s, host_out, st); break;
+    case 3: nodal_avg_p<3>(s, host_out, st); break;
+    case 4: nodal_avg_p<4>(s, host_out, st); break;
+  }
+}
 
 void launch_recover(hdg_system* s, cudaStream_t st) {
   switch (s->space->t.p) {

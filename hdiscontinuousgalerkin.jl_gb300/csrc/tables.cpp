@@ -201,6 +201,13 @@ RefLayout ref_layout(int nw, int nt, int nq) {
   L.NW = o; o += nw * nq;
   L.N = o; o += nw * nq;
   L.Q = o; o += 2 * nq;
+  L.SMD0 = o; o += nw * nw;
+  L.SMD1 = o; o += nw * nw;
+  L.SQ00 = o; o += nw * nw;
+  L.SQ01 = o; o += nw * nw;
+  L.SQ11 = o; o += nw * nw;
+  L.SMF = o; o += 6 * nw * nt;
+  L.SDMF = o; o += 12 * nw * nt;
   L.total = o;
   return L;
 }
@@ -237,6 +244,13 @@ bool build_ref_tables(int p, int qd, RefTables* t) {
       t->dN[(a * nq + q) * 2] = v.gx;
       t->dN[(a * nq + q) * 2 + 1] = v.gy;
     }
+  }
+  t->Nv.assign(nw * 3, 0);
+  static const double VX[3] = {0.0, 1.0, 0.0}, VY[3] = {0.0, 0.0, 1.0};
+  for (int a = 0; a < nw; ++a) {
+    int n, m;
+    dubiner_index(a + 1, &n, &m);
+    for (int k = 0; k < 3; ++k) t->Nv[a * 3 + k] = dubiner_nm(Dd{VX[k], 0, 0}, Dd{VY[k], 0, 0}, n, m).v;
   }
   t->E.assign(nw * nfq * 3, 0);
   for (int f = 0; f < 3; ++f)
@@ -301,6 +315,79 @@ bool build_ref_tables(int p, int qd, RefTables* t) {
   for (int q = 0; q < nq; ++q) {
     P[L.Q + 2 * q] = t->qx[q];
     P[L.Q + 2 * q + 1] = t->qy[q];
+  }
+  // Schur-complement tables.  With the mass block Ae = (det J / kappa) diag(M, M) of an affine
+  // cell and constant kappa, Me^-1 follows from M^-1 and the Schur complement
+  // S = Ce + Be' Ae^-1 Be (nw x nw); every product of reference matrices it needs is tabulated
+  // here once.  They are used only when the volume rule makes M invertible (for p = 2 the
+  // default Strang(3) rule leaves M of rank 5, and the element kernel keeps its full LU).
+  {
+    std::vector<long double> a((size_t)nw * 2 * nw, 0.0L);
+    for (int i = 0; i < nw; ++i) {
+      for (int j = 0; j < nw; ++j) a[(size_t)i * 2 * nw + j] = P[L.M + i * nw + j];
+      a[(size_t)i * 2 * nw + nw + i] = 1.0L;
+    }
+    long double maxpiv = 0.0L, minpiv = 1e300L;
+    bool ok = true;
+    for (int c = 0; c < nw && ok; ++c) {
+      int piv = c;
+      for (int i = c + 1; i < nw; ++i)
+        if (std::fabs(a[(size_t)i * 2 * nw + c]) > std::fabs(a[(size_t)piv * 2 * nw + c])) piv = i;
+      if (piv != c)
+        for (int j = 0; j < 2 * nw; ++j) std::swap(a[(size_t)c * 2 * nw + j], a[(size_t)piv * 2 * nw + j]);
+      const long double d = a[(size_t)c * 2 * nw + c];
+      maxpiv = std::max(maxpiv, std::fabs(d));
+      minpiv = std::min(minpiv, std::fabs(d));
+      if (d == 0.0L) { ok = false; break; }
+      for (int j = 0; j < 2 * nw; ++j) a[(size_t)c * 2 * nw + j] /= d;
+      for (int i = 0; i < nw; ++i) {
+        if (i == c) continue;
+        const long double m = a[(size_t)i * 2 * nw + c];
+        for (int j = 0; j < 2 * nw; ++j) a[(size_t)i * 2 * nw + j] -= m * a[(size_t)c * 2 * nw + j];
+      }
+    }
+    t->schur = ok && minpiv > 1e-10L * maxpiv;
+    if (t->schur) {
+      auto Mi = [&](int i, int j) { return a[(size_t)i * 2 * nw + nw + j]; };
+      const double* D[2] = {&P[L.D0], &P[L.D1]};
+      std::vector<long double> MD[2];
+      for (int l = 0; l < 2; ++l) {
+        MD[l].assign((size_t)nw * nw, 0.0L);
+        for (int i = 0; i < nw; ++i)
+          for (int j = 0; j < nw; ++j) {
+            long double s = 0;
+            for (int k = 0; k < nw; ++k) s += Mi(i, k) * D[l][k * nw + j];
+            MD[l][(size_t)i * nw + j] = s;
+            P[(l ? L.SMD1 : L.SMD0) + i * nw + j] = (double)s;
+          }
+      }
+      const int QO[3] = {L.SQ00, L.SQ01, L.SQ11};
+      const int QL[3][2] = {{0, 0}, {0, 1}, {1, 1}};
+      for (int q = 0; q < 3; ++q)
+        for (int i = 0; i < nw; ++i)
+          for (int j = 0; j < nw; ++j) {
+            long double s = 0;  // (D_l' M^-1 D_m)[i][j] = sum_k D_l[k][i] (M^-1 D_m)[k][j]
+            for (int k = 0; k < nw; ++k) s += (long double)D[QL[q][0]][k * nw + i] * MD[QL[q][1]][(size_t)k * nw + j];
+            P[QO[q] + i * nw + j] = (double)s;
+          }
+      for (int fo = 0; fo < 6; ++fo) {
+        std::vector<long double> MF((size_t)nw * nt, 0.0L);
+        for (int i = 0; i < nw; ++i)
+          for (int j = 0; j < nt; ++j) {
+            long double s = 0;
+            for (int k = 0; k < nw; ++k) s += Mi(i, k) * P[L.F + (fo * nw + k) * nt + j];
+            MF[(size_t)i * nt + j] = s;
+            P[L.SMF + (fo * nw + i) * nt + j] = (double)s;
+          }
+        for (int l = 0; l < 2; ++l)
+          for (int i = 0; i < nw; ++i)
+            for (int j = 0; j < nt; ++j) {
+              long double s = 0;
+              for (int k = 0; k < nw; ++k) s += (long double)D[l][k * nw + i] * MF[(size_t)k * nt + j];
+              P[L.SDMF + ((l * 6 + fo) * nw + i) * nt + j] = (double)s;
+            }
+      }
+    }
   }
   return true;
 }

@@ -119,6 +119,11 @@ void build_segments(hdg_system* s) {
     for (int r = a; r < e; ++r) rowp[r] = P;
   }
   s->nseg = (int)sp.size();
+  s->h_seg_prob = sp;
+  s->h_seg_row0 = r0;
+  s->h_seg_row1 = r1;
+  s->h_prob_blk0 = b0;
+  s->h_prob_nblk = nb;
   cudaStream_t st = s->ctx->stream;
   s->d_seg_prob.upload(sp.data(), sp.size(), st);
   s->d_seg_row0.upload(r0.data(), r0.size(), st);
@@ -258,10 +263,11 @@ template <int NT> void gather_t(hdg_system* s, cudaStream_t st) {
   s->ctx->launches += 2;
 }
 
-template <int NT>
-void apply_t(hdg_system* s, const std::vector<int32_t>& dofs0, const std::vector<double>& vals, cudaStream_t st) {
-  hdg_mesh* m = s->space->mesh;
-  const int nrow = m->nf * NT;
+// Scatter of the prescribed dofs and values into per-row flags and values (d_pres, d_gv): the
+// part of apply! that depends only on the Dirichlet data, so it survives reassembly.
+void dirichlet_scatter(hdg_system* s, const std::vector<int32_t>& dofs0, const std::vector<double>& vals,
+                       cudaStream_t st) {
+  const int nrow = s->ndofs;
   bool lift = false;
   for (size_t k = 0; k < dofs0.size(); ++k)
     if (vals[k] != 0.0) lift = true;
@@ -279,12 +285,21 @@ void apply_t(hdg_system* s, const std::vector<int32_t>& dofs0, const std::vector
     s->ctx->launches++;
   }
   s->d_mdiag.alloc(s->nprob);
-  DevBuf<int32_t>& prow = s->d_prob_row0_dev();
+  s->d_prob_row0_dev();
+  s->dir_lift = lift;
+  s->dir_ready = true;
+}
+
+// apply! on the assembled system from the scattered Dirichlet data: per-problem mean |diag|,
+// lifting of the prescribed values into b, and the symmetric row/column elimination.
+template <int NT> void apply_t(hdg_system* s, cudaStream_t st) {
+  hdg_mesh* m = s->space->mesh;
+  const int nrow = m->nf * NT;
   const SegArgs g{s->d_seg_prob.p, s->d_seg_row0.p, s->d_seg_row1.p, s->d_prob_blk0.p, s->d_prob_nblk.p, s->d_part.p,
                   s->d_cnt.p};
-  k_meandiag<NT><<<s->nseg, 256, 0, st>>>(g, prow.p, m->nf, s->d_kdiag.p, s->d_val.p, s->d_mdiag.p);
+  k_meandiag<NT><<<s->nseg, 256, 0, st>>>(g, s->d_prob_row0.p, m->nf, s->d_kdiag.p, s->d_val.p, s->d_mdiag.p);
   HDG_CUDA(cudaGetLastError());
-  if (lift) {
+  if (s->dir_lift) {
     k_lift<NT><<<(nrow + 255) / 256, 256, 0, st>>>(m->nf, s->d_bcol5.p, s->d_val.p, s->d_gv.p, s->d_b.p);
     HDG_CUDA(cudaGetLastError());
     s->ctx->launches++;
@@ -307,13 +322,24 @@ void launch_gather(hdg_system* s, cudaStream_t st) {
   }
 }
 
-void launch_apply_dirichlet(hdg_system* s, const std::vector<int32_t>& dofs0, const std::vector<double>& vals,
-                            cudaStream_t st) {
+void launch_dirichlet_scatter(hdg_system* s, const std::vector<int32_t>& dofs0, const std::vector<double>& vals,
+                              cudaStream_t st) {
+  dirichlet_scatter(s, dofs0, vals, st);
+}
+
+void launch_dirichlet_apply(hdg_system* s, cudaStream_t st) {
+  if (!s->dir_ready) throw HdgError{HDG_ERR_ARG, "no Dirichlet set was given to this system"};
   switch (s->nt) {
-    case 2: apply_t<2>(s, dofs0, vals, st); break;
-    case 3: apply_t<3>(s, dofs0, vals, st); break;
-    case 4: apply_t<4>(s, dofs0, vals, st); break;
-    case 5: apply_t<5>(s, dofs0, vals, st); break;
+    case 2: apply_t<2>(s, st); break;
+    case 3: apply_t<3>(s, st); break;
+    case 4: apply_t<4>(s, st); break;
+    case 5: apply_t<5>(s, st); break;
     default: throw HdgError{HDG_ERR_ARG, "degree not supported"};
   }
+}
+
+void launch_apply_dirichlet(hdg_system* s, const std::vector<int32_t>& dofs0, const std::vector<double>& vals,
+                            cudaStream_t st) {
+  launch_dirichlet_scatter(s, dofs0, vals, st);
+  launch_dirichlet_apply(s, st);
 }

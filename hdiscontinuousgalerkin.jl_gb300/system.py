@@ -243,6 +243,17 @@ def get_usigma_(sigma_h: TrialFunction, u_h: TrialFunction, uhat_h: TrialFunctio
     u_h.system = sigma_h.system = uhat_h.system = K
 
 
+def nodal_avg(u_h: TrialFunction) -> np.ndarray:
+    """nodal_avg(u_h) (src/DiscreteFunctions.jl:81-95): per mesh node, the mean of the recovered u
+    over the node's cells, evaluated at the node."""
+    K = u_h.system
+    if K is None:
+        raise ValueError("u_h has no recovered values (call get_usigma_ first)")
+    out = np.zeros(K.sp.mesh.nnodes)
+    L.check(L.load().hdg_nodal_avg(K._h, L.dptr(out)), K.ctx)
+    return out
+
+
 def errornorm(u_h: TrialFunction, u_ex, norm_type: str = "L2") -> float:
     """errornorm(u_h, u_ex): the SQUARED L2 error (src/DiscreteFunctions.jl:97-120), on the device."""
     if norm_type != "L2":

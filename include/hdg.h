@@ -189,6 +189,10 @@ int hdg_recover(hdg_system* sys, double* q, double* u, double* uhat_cell);
 /* errornorm(u_h, u_ex), src/DiscreteFunctions.jl:97-120: the SQUARED L2 error of the last
  * recovery. */
 int hdg_errornorm_l2sq(hdg_system* sys, const hdg_field* u_exact, double* out);
+/* nodal_avg(u_h), src/DiscreteFunctions.jl:81-95: at every mesh node, the mean over the node's
+ * cells of the last recovered u evaluated at that node (host output, nnodes values).  The
+ * reference feeds it to its plotting; here it is a plain buffer. */
+int hdg_nodal_avg(hdg_system* sys, double* out);
 int hdg_system_destroy(hdg_system* sys);
 
 /* No counterpart in the reference.  The squared L2 error of hdg_errornorm_l2sq for callers that
@@ -239,6 +243,24 @@ int hdg_system_reassemble_batch(hdg_system* sys, const double* tau, const hdg_fi
 /* Solves every problem of several systems (for example one per degree) in one interleaved loop;
  * each problem stops independently.  stats: one entry per problem, systems in order. */
 int hdg_solve_batch(int nsys, hdg_system* const* systems, const hdg_solver* opts, hdg_stats* stats);
+/* Uploads new per-problem coefficients (as hdg_system_reassemble_batch) without assembling:
+ * the next hdg_batch_step with HDG_STEP_ASSEMBLE assembles from them. */
+int hdg_system_set_coefficients_batch(hdg_system* sys, const double* tau, const hdg_field* f,
+                                      const hdg_field* kappa, const double* kappa_cell);
+/* Records a Dirichlet set (the arguments of hdg_apply_dirichlet) without applying it: the next
+ * hdg_batch_step with HDG_STEP_APPLY applies it.  The set is kept across reassembly.  On a
+ * system that is already applied, the new set takes effect after the next reassembly. */
+int hdg_system_set_dirichlet(hdg_system* sys, const int32_t* dofs, const double* vals, int n);
+#define HDG_STEP_ASSEMBLE 1 /* assemble + condense from the coefficients on the device */
+#define HDG_STEP_APPLY 2    /* apply! the recorded Dirichlet set */
+#define HDG_STEP_RECOVER 4  /* local recovery of (q, u) after the solve */
+/* One pipelined step over several systems: per system, on a CUDA stream of its own,
+ * [assemble + condense] -> [apply!] -> CG -> [recovery], so that one system's assembly and
+ * recovery overlap the other systems' iterations.  The results equal those of
+ * hdg_system_reassemble_resident, hdg_apply_dirichlet, hdg_solve_batch and hdg_recover called
+ * in turn.  Without HDG_STEP_APPLY the systems must be applied already (and HDG_STEP_ASSEMBLE,
+ * which undoes apply!, is then refused).  stats: one entry per problem, systems in order. */
+int hdg_batch_step(int nsys, hdg_system* const* systems, const hdg_solver* opts, int flags, hdg_stats* stats);
 /* Device solution of a system: trace values (ndofs) and, after recovery, [q; u] per cell (ncells x n). */
 int hdg_system_get_solution(const hdg_system* sys, double* uhat, double* qu);
 

@@ -4,6 +4,7 @@ Tolerances (FP64 path): element blocks and global matrix entries within 1e-12 re
 largest entry; sparsity pattern and dof numbering bit-exact; trace solution within a tolerance
 derived from the CG stopping criterion (relative residual 1e-13 here)."""
 import math
+import os
 
 import numpy as np
 import pytest
@@ -311,3 +312,86 @@ def test_multigrid_batch_matches_single_problems(H, oracle):
         om.set_xy(H.batch.host_mesh(pr)._topology()[0])
         r = oracle.solve_poisson(om, pr.p, qd=pr.qd(), f=pr.f.as_oracle(), kappa_cell=pr.kappa_cell)
         assert rel(uh, r["uhat"]) < 1e-10, (pr.n, pr.p)
+
+
+@pytest.mark.parametrize("pc", ["jacobi", "amg"])
+def test_pipelined_step_equals_sequential_calls(H, pc):
+    """hdg_batch_step (per-bin streams: assembly, apply!, CG and recovery overlapped across bins)
+    gives bit-identical results to the same work done call by call: reassembly, apply!,
+    hdg_solve_batch and recovery of each bin in turn.  Repeated resident steps repeat the result."""
+    import ctypes as C
+    L = H._lib
+    rng = np.random.default_rng(21)
+    probs = []
+    for k, (n, p) in enumerate([(9, 1), (5, 2), (4, 3), (3, 4), (6, 2), (7, 4)]):
+        f = H.Field.bumps(rng.random((8, 2)), 0.1 + 0.1 * rng.random(8), rng.standard_normal(8))
+        kc = np.exp(rng.uniform(np.log(1e-2), np.log(1e2), 2 * n * n))
+        probs.append(H.Problem(n=n, p=p, f=f, kappa_cell=kc, jitter=0.2, seed=700 + k))
+    pcv = H.PRECOND_AMG if pc == "amg" else H.PRECOND_JACOBI
+    B = H.Batch(H.default_context(), probs, precision=H.PREC_MIXED)
+    st1 = B.solve(tol=1e-10, reassemble=True, preconditioner=pcv)
+    s1 = B.solutions()
+    st2 = B.solve(tol=1e-10, reassemble="resident", preconditioner=pcv)
+    s2 = B.solutions()
+    # call by call
+    for b in B.bins:
+        b.reassemble(resident=True)
+        b.apply()
+    o = L.hdg_solver(1e-10, 100000, int(H.PREC_MIXED), 32, 1e-5, int(pcv))
+    st = (L.hdg_stats * len(probs))()
+    arr = (C.c_void_p * len(B.bins))(*[b.h for b in B.bins])
+    assert L.load().hdg_solve_batch(len(B.bins), arr, C.byref(o), st) == 0
+    for b in B.bins:
+        b.recover()
+    s3 = B.solutions()
+    for a, b_, c in zip(s1, s2, s3):
+        for x, y, z in zip(a, b_, c):
+            assert np.array_equal(x, y) and np.array_equal(x, z)
+    assert [s.iterations for s in st1] == [s.iterations for s in st2]
+    # a solve without apply! is refused; assembly without apply! is refused
+    assert L.load().hdg_batch_step(len(B.bins), arr, C.byref(o), L.STEP_ASSEMBLE, st) == -1  # HDG_ERR_ARG
+
+
+@pytest.mark.parametrize("p,qd", [(1, None), (2, None), (3, 6)])
+def test_unstructured_figure1_parity(H, oracle, p, qd):
+    """The unstructured figure.1 mesh: trace matrix, solution and recovery equal the oracle's, and the
+    manufactured solution is approximated (squared L2 error small and shrinking with p)."""
+    root = os.path.join(os.path.dirname(__file__), "golden", "mesh", "figure.1")
+    mesh = H.parse_mesh_triangle(root)
+    omesh = oracle.parse_mesh_triangle(root)
+    K, S, (Vh, Wh, Mh) = compare_system(H, oracle, mesh, omesh, p, qd=qd)
+    uhat = H.solve(K, None, tol=1e-14)
+    ref = S.solve()
+    assert rel(uhat, ref) < 1e-11
+    q, u, _ = K.recover()
+    oq, ou, _ = S.recover(ref)
+    assert rel(u, ou) < 1e-10 and rel(q, oq) < 1e-10
+    e = K.errornorm(H.MANUFACTURED_U)
+    assert e == pytest.approx(oracle.errornorm(omesh, p, ou, oracle.MANUFACTURED_U, qd=qd), rel=1e-9)
+    assert e < {1: 1e-3, 2: 1e-4, 3: 1e-5}[p]
+
+
+def test_nodal_avg(H, oracle):
+    """nodal_avg(u_h) (src/DiscreteFunctions.jl:81-95): the per-node mean of the recovered u over
+    the node's cells equals the same average formed on the host from the oracle's Dubiner basis,
+    and approximates the exact solution at the nodes."""
+    n, p = 10, 2
+    mesh = H.rectangle_mesh(H.TriangleCell, (n, n), (0.0, 0.0), (1.0, 1.0))
+    Vh, Wh, Mh = spaces(H, mesh, p, None)
+    K, b, K_e, b_e = H.doassemble(Vh, Wh, Mh, 1.0, H.MANUFACTURED_F)
+    H.apply_(K, b, H.Dirichlet(H.TrialFunction(Mh), mesh, "boundary"))
+    uhat = H.solve(K, b, tol=1e-13)
+    sigma_h, u_h, uhat_h = H.TrialFunction(Vh), H.TrialFunction(Wh), H.TrialFunction(Mh)
+    H.get_usigma_(sigma_h, u_h, uhat_h, uhat, H.system._LocalView(K, "K"), None, mesh)
+    got = H.nodal_avg(u_h)
+    xy, cn = H.get_vertices_matrix(mesh), H.getcells_matrix(mesh)
+    nw = (p + 1) * (p + 2) // 2
+    vals = np.array([[oracle.dubiner(a + 1, vx, vy)[0] for vx, vy in ((0, 0), (1, 0), (0, 1))] for a in range(nw)])
+    acc, cnt = np.zeros(len(xy)), np.zeros(len(xy))
+    for c in range(mesh.ncells):
+        for k in range(3):
+            acc[cn[c, k] - 1] += u_h.m_values[c] @ vals[:, k]
+            cnt[cn[c, k] - 1] += 1
+    assert rel(got, acc / cnt) < 1e-12
+    exact = np.sin(np.pi * xy[:, 0]) * np.sin(np.pi * xy[:, 1])
+    assert np.max(np.abs(got - exact)) < 2e-3

@@ -195,3 +195,20 @@ def test_pattern_assembler_matches_triplets(H):
     assert np.allclose(f, g, rtol=0, atol=1e-13)
     with pytest.raises(H.HDGError):
         H.assemble_(A, np.array([1, H.ndofs(dh)]), np.ones((2, 2)))
+
+
+def test_unstructured_figure1_reader_matches_oracle(H, oracle):
+    """The 62-cell unstructured Triangle mesh test/mesh/figure.1.*: the reader's cells, cell faces,
+    face table, boundary set and orientations equal the oracle's restatement of
+    src/triangle_mesh.jl (first-visit face numbering, edge-marker boundary)."""
+    root = os.path.join(ROOT, "tests", "golden", "mesh", "figure.1")
+    m = H.parse_mesh_triangle(root, ctx=None)
+    om = oracle.parse_mesh_triangle(root)
+    assert (m.nnodes, m.ncells, m.nfaces) == (om.nnodes, om.ncells, om.nfaces) == (41, 62, 102)
+    xy, cn, cf, fc = m._topology()
+    assert np.array_equal(xy, om.xy)
+    assert np.array_equal(cn, om.cells) and np.array_equal(cf, om.cell_faces)
+    assert np.array_equal(fc, om.faces)
+    assert sorted(H.getfaceset(m, "boundary")) == sorted(om.faceset("boundary").tolist())
+    for c in range(m.ncells):
+        assert [H.face_orientation(m, c + 1, f + 1) for f in range(3)] == [om.orientation(c, f) for f in range(3)]
