@@ -549,8 +549,8 @@ def parse():
                     help="default: mixed for the batched and served workloads (c3, c4, c5), fp64 for c1, c2")
     ap.add_argument("--tol", type=float, default=1e-12)
     ap.add_argument("--preconditioner", default=None, choices=["jacobi", "amg"],
-                    help="trace CG preconditioner (default: amg for the batch c4, jacobi otherwise); the plain "
-                         "FP64 path of c4 uses the same one")
+                    help="trace CG preconditioner (default: amg for the batch c4 and the stream c5, jacobi "
+                         "otherwise); the plain FP64 paths of c4 and c5 use the same one")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n", type=int, default=None, help="c1/c2 only: cells per side (a profiling case, not a bench line)")
     ap.add_argument("--p", type=int, default=None, help="c1/c2 only: polynomial degree (a profiling case)")
@@ -558,7 +558,7 @@ def parse():
     if args.precision is None:
         args.precision = "mixed" if args.workload in ("c3", "c4", "c5") else "fp64"
     if args.preconditioner is None:
-        args.preconditioner = "amg" if args.workload == "c4" else "jacobi"
+        args.preconditioner = "amg" if args.workload in ("c4", "c5") else "jacobi"
     return args
 
 

@@ -146,6 +146,7 @@ struct AmgLevel {  // a scalar level l >= 1 (rows = aggregates of level l-1)
   DevBuf<float> b, x, t, r;           // cycle vectors: rhs, iterate, sweep target, residual
   // transfer to the next level (all empty on the coarsest)
   int nc = 0;
+  DevBuf<int32_t> prob;               // problem of each row (device copy of h_prob)
   DevBuf<int32_t> agg;                // aggregate of each row
   DevBuf<float> tent;                 // tentative weight of each row
   DevBuf<int32_t> pptr, pcol;         // P (CSR, sorted columns)
@@ -400,6 +401,7 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
   for (auto& L : H->lev) {
     L.ptr.upload(L.h_ptr.data(), L.h_ptr.size(), st);
     upload_min1(L.col, L.h_col, st);
+    upload_min1(L.prob, L.h_prob, st);
     L.val.alloc(std::max<size_t>(L.h_col.size(), 1));
     L.dl1inv.alloc(std::max(L.n, 1));
     L.b.alloc(std::max(L.n, 1));
@@ -749,7 +751,16 @@ __global__ void k_amg_coarse_inv(const int32_t* __restrict__ crow0, const int32_
 }
 
 // ------------------------------------------------------------------------------------------
-// Cycle kernels
+// Cycle kernels.  `st` is the CG's per-problem state (HDG_CG_ST ints per problem: status, ...,
+// refine flag): rows of a problem that has stopped iterating and waits for no refinement are
+// skipped, so the tail of a batch, where a few problems still iterate, does not pay for a
+// V-cycle over every problem.  Their outputs keep stale values, which the CG never reads.
+// st == NULL runs every row.
+__device__ __forceinline__ bool amg_live(const int32_t* __restrict__ st, int P) {
+  return !st || st[HDG_CG_ST * P] == 0 || st[HDG_CG_ST * P + 3] != 0;
+}
+
+
 // Level-0 smoother: step `step` of the Chebyshev iteration (Saad, Iterative Methods, 12.3) for
 // D^-1 A0 on [lambda / CHEB_RATIO, lambda], D the face-block diagonal and lambda the problem's
 // Gershgorin bound.  xin == NULL stands for x = 0 (no product); d holds the previous step's
@@ -760,9 +771,9 @@ __global__ void k_amg_face_cheb(int nf, const int32_t* __restrict__ bcol5, const
                                 const float* __restrict__ dinv, const float* __restrict__ lam,
                                 const int32_t* __restrict__ face_prob, const float* __restrict__ b,
                                 const float* __restrict__ xin, float* __restrict__ xout, float* __restrict__ d,
-                                int step) {
+                                int step, const int32_t* __restrict__ st) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= nf) return;
+  if (f >= nf || !amg_live(st, face_prob[f])) return;
   const int64_t nd = (int64_t)nf * NT;
   float res[NT];
   for (int i = 0; i < NT; ++i) res[i] = b[(int64_t)f * NT + i];
@@ -802,11 +813,13 @@ __global__ void k_amg_face_cheb(int nf, const int32_t* __restrict__ bcol5, const
 // r = b - A0 x (level 0)
 template <int NT>
 __global__ void k_amg_face_residual(int nf, const int32_t* __restrict__ bcol5, const float* __restrict__ val,
-                                    const float* __restrict__ b, const float* __restrict__ x, float* __restrict__ r) {
+                                    const float* __restrict__ b, const float* __restrict__ x, float* __restrict__ r,
+                                    const int32_t* __restrict__ face_prob, const int32_t* __restrict__ st) {
   const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t nd = (int64_t)nf * NT;
   if (row >= nd) return;
   const int f = (int)(row / NT);
+  if (!amg_live(st, face_prob[f])) return;
   float s = b[row];
   int seen[5];
   int ns = 0;
@@ -825,9 +838,10 @@ __global__ void k_amg_face_residual(int nf, const int32_t* __restrict__ bcol5, c
 template <int NT>
 __global__ void k_amg_restrict0(int na, const int32_t* __restrict__ rptr0, const int32_t* __restrict__ rent0,
                                 const float* __restrict__ pval0, const float* __restrict__ r0,
-                                const float* __restrict__ dl1inv, float* __restrict__ b1, float* __restrict__ x1) {
+                                const float* __restrict__ dl1inv, float* __restrict__ b1, float* __restrict__ x1,
+                                const int32_t* __restrict__ prob1, const int32_t* __restrict__ st) {
   const int J = blockIdx.x * blockDim.x + threadIdx.x;
-  if (J >= na) return;
+  if (J >= na || !amg_live(st, prob1[J])) return;
   float s = 0.f;
   for (int t = rptr0[J]; t < rptr0[J + 1]; ++t) {
     const int f = rent0[t] / PW, c = rent0[t] - f * PW;
@@ -840,10 +854,12 @@ __global__ void k_amg_restrict0(int na, const int32_t* __restrict__ rptr0, const
 // x0 += P0 x1
 template <int NT>
 __global__ void k_amg_prolong0(int nf, const int32_t* __restrict__ pcol0, const float* __restrict__ pval0,
-                               const float* __restrict__ x1, float* __restrict__ x0) {
+                               const float* __restrict__ x1, float* __restrict__ x0,
+                               const int32_t* __restrict__ face_prob, const int32_t* __restrict__ st) {
   const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (row >= (int64_t)nf * NT) return;
   const int f = (int)(row / NT);
+  if (!amg_live(st, face_prob[f])) return;
   float s = 0.f;
   for (int c = 0; c < PW; ++c) {
     const int J = pcol0[f * PW + c];
@@ -876,26 +892,30 @@ template <int G> __device__ __forceinline__ float group_sum_f(float v) {
 template <int G>
 __global__ void k_amg_l1_sweep(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
                                const float* __restrict__ val, const float* __restrict__ dl1inv,
-                               const float* __restrict__ b, const float* __restrict__ xin, float* __restrict__ xout) {
+                               const float* __restrict__ b, const float* __restrict__ xin, float* __restrict__ xout,
+                               const int32_t* __restrict__ prob, const int32_t* __restrict__ st) {
   AMG_GROUP_ROW(i, lane, n);
+  const bool on = i < n && amg_live(st, prob[i]);
   float s = 0.f;
-  if (i < n)
+  if (on)
     for (int e = ptr[i] + lane; e < ptr[i + 1]; e += G) s += val[e] * xin[col[e]];
   s = group_sum_f<G>(s);
-  if (lane == 0 && i < n) xout[i] = xin[i] + (b[i] - s) * dl1inv[i];
+  if (lane == 0 && on) xout[i] = xin[i] + (b[i] - s) * dl1inv[i];
 }
 
 // r = b - A x
 template <int G>
 __global__ void k_amg_residual(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
                                const float* __restrict__ val, const float* __restrict__ b, const float* __restrict__ x,
-                               float* __restrict__ r) {
+                               float* __restrict__ r, const int32_t* __restrict__ prob,
+                               const int32_t* __restrict__ st) {
   AMG_GROUP_ROW(i, lane, n);
+  const bool on = i < n && amg_live(st, prob[i]);
   float s = 0.f;
-  if (i < n)
+  if (on)
     for (int e = ptr[i] + lane; e < ptr[i + 1]; e += G) s += val[e] * x[col[e]];
   s = group_sum_f<G>(s);
-  if (lane == 0 && i < n) r[i] = b[i] - s;
+  if (lane == 0 && on) r[i] = b[i] - s;
 }
 
 // b_c = P' r and x_c = b_c / dl1_c (first sweep of the coarse level; dl1 NULL on the coarsest)
@@ -903,13 +923,15 @@ template <int G>
 __global__ void k_amg_restrict(int nc, const int32_t* __restrict__ rptr, const int32_t* __restrict__ rent,
                                const int32_t* __restrict__ rrow, const float* __restrict__ pval,
                                const float* __restrict__ r, const float* __restrict__ dl1inv, float* __restrict__ bc,
-                               float* __restrict__ xc) {
+                               float* __restrict__ xc, const int32_t* __restrict__ probc,
+                               const int32_t* __restrict__ st) {
   AMG_GROUP_ROW(J, lane, nc);
+  const bool on = J < nc && amg_live(st, probc[J]);
   float s = 0.f;
-  if (J < nc)
+  if (on)
     for (int k = rptr[J] + lane; k < rptr[J + 1]; k += G) s += pval[rent[k]] * r[rrow[k]];
   s = group_sum_f<G>(s);
-  if (lane == 0 && J < nc) {
+  if (lane == 0 && on) {
     bc[J] = s;
     if (dl1inv) xc[J] = s * dl1inv[J];
   }
@@ -918,19 +940,23 @@ __global__ void k_amg_restrict(int nc, const int32_t* __restrict__ rptr, const i
 // x += P x_c
 template <int G>
 __global__ void k_amg_prolong(int n, const int32_t* __restrict__ pptr, const int32_t* __restrict__ pcol,
-                              const float* __restrict__ pval, const float* __restrict__ xc, float* __restrict__ x) {
+                              const float* __restrict__ pval, const float* __restrict__ xc, float* __restrict__ x,
+                              const int32_t* __restrict__ prob, const int32_t* __restrict__ st) {
   AMG_GROUP_ROW(i, lane, n);
+  const bool on = i < n && amg_live(st, prob[i]);
   float s = 0.f;
-  if (i < n)
+  if (on)
     for (int e = pptr[i] + lane; e < pptr[i + 1]; e += G) s += pval[e] * xc[pcol[e]];
   s = group_sum_f<G>(s);
-  if (lane == 0 && i < n) x[i] += s;
+  if (lane == 0 && on) x[i] += s;
 }
 
 // coarsest: x = A^-1 b per problem (one CTA per problem)
 __global__ void k_amg_coarse_solve(const int32_t* __restrict__ crow0, const int32_t* __restrict__ coff,
-                                   const float* __restrict__ cinv, const float* __restrict__ b, float* __restrict__ x) {
+                                   const float* __restrict__ cinv, const float* __restrict__ b, float* __restrict__ x,
+                                   const int32_t* __restrict__ st) {
   const int P = blockIdx.x;
+  if (!amg_live(st, P)) return;
   const int r0 = crow0[P], m = crow0[P + 1] - r0;
   const float* A = cinv + coff[P];
   for (int i = threadIdx.x; i < m; i += blockDim.x) {
@@ -995,54 +1021,52 @@ template <int NT> void numeric_nt(hdg_system* s, const float* val0, cudaStream_t
   HDG_CUDA(cudaGetLastError());
 }
 
-template <int NT> void apply_nt(hdg_system* s, const float* val0, const float* b0, float* z0, cudaStream_t st) {
+template <int NT>
+void apply_nt(hdg_system* s, const float* val0, const float* b0, float* z0, const int32_t* cst, cudaStream_t st) {
   AmgHierarchy* H = s->amg;
   const int nf = H->nf;
   const int64_t n0 = (int64_t)nf * NT;
   const int nl = (int)H->lev.size();
   // level 0 pre-smoothing: degree-2 Chebyshev from x = 0 (x0, then z0)
   k_amg_face_cheb<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
-                                                nullptr, H->x0.p, H->d0.p, 0);
+                                                nullptr, H->x0.p, H->d0.p, 0, cst);
   k_amg_face_cheb<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
-                                                H->x0.p, z0, H->d0.p, 1);
-  k_amg_face_residual<NT><<<nblk(n0), 256, 0, st>>>(nf, s->d_bcol5.p, val0, b0, z0, H->r0.p);
+                                                H->x0.p, z0, H->d0.p, 1, cst);
+  k_amg_face_residual<NT><<<nblk(n0), 256, 0, st>>>(nf, s->d_bcol5.p, val0, b0, z0, H->r0.p, H->face_prob.p, cst);
   AmgLevel& L1 = H->lev[0];
   k_amg_restrict0<NT><<<nblk(L1.n), 256, 0, st>>>(L1.n, H->rptr0.p, H->rent0.p, H->pval0.p, H->r0.p, L1.dl1inv.p,
-                                                  L1.b.p, L1.x.p);
-  int launches = 4;
+                                                  L1.b.p, L1.x.p, L1.prob.p, cst);
   // coarse levels down: x holds the first sweep (from the restriction); the second sweep goes to
   // t, which then holds the level's iterate until the way up
   for (int l = 0; l + 1 < nl; ++l) {
     AmgLevel& L = H->lev[l];
     AmgLevel& C = H->lev[l + 1];
-    AMG_LAUNCH_G(k_amg_l1_sweep, L.n, st, L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.x.p, L.t.p);
-    AMG_LAUNCH_G(k_amg_residual, L.n, st, L.n, L.ptr.p, L.col.p, L.val.p, L.b.p, L.t.p, L.r.p);
+    AMG_LAUNCH_G(k_amg_l1_sweep, L.n, st, L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.x.p, L.t.p, L.prob.p,
+                 cst);
+    AMG_LAUNCH_G(k_amg_residual, L.n, st, L.n, L.ptr.p, L.col.p, L.val.p, L.b.p, L.t.p, L.r.p, L.prob.p, cst);
     const bool coarsest = (l + 2 == nl);
     AMG_LAUNCH_G(k_amg_restrict, C.n, st, C.n, L.rptr.p, L.rent.p, L.rrow.p, L.pval.p, L.r.p,
-                 coarsest ? nullptr : C.dl1inv.p, C.b.p, C.x.p);
-    launches += 3;
+                 coarsest ? nullptr : C.dl1inv.p, C.b.p, C.x.p, C.prob.p, cst);
   }
   AmgLevel& C = H->lev.back();
-  if (H->cmax > 0) k_amg_coarse_solve<<<s->nprob, 128, 0, st>>>(H->crow0.p, H->coff.p, H->cinv.p, C.b.p, C.x.p);
-  ++launches;
+  if (H->cmax > 0) k_amg_coarse_solve<<<s->nprob, 128, 0, st>>>(H->crow0.p, H->coff.p, H->cinv.p, C.b.p, C.x.p, cst);
   // coarse levels up: the coarser level's result is in its x; prolongate into this level's
   // iterate (t), then two sweeps t -> r -> x
   for (int l = nl - 2; l >= 0; --l) {
     AmgLevel& L = H->lev[l];
     AmgLevel& Cn = H->lev[l + 1];
-    AMG_LAUNCH_G(k_amg_prolong, L.n, st, L.n, L.pptr.p, L.pcol.p, L.pval.p, Cn.x.p, L.t.p);
-    AMG_LAUNCH_G(k_amg_l1_sweep, L.n, st, L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.t.p, L.r.p);
-    AMG_LAUNCH_G(k_amg_l1_sweep, L.n, st, L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.r.p, L.x.p);
-    launches += 3;
+    AMG_LAUNCH_G(k_amg_prolong, L.n, st, L.n, L.pptr.p, L.pcol.p, L.pval.p, Cn.x.p, L.t.p, L.prob.p, cst);
+    AMG_LAUNCH_G(k_amg_l1_sweep, L.n, st, L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.t.p, L.r.p, L.prob.p,
+                 cst);
+    AMG_LAUNCH_G(k_amg_l1_sweep, L.n, st, L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.r.p, L.x.p, L.prob.p,
+                 cst);
   }
   // level 0 up: prolongate, degree-2 Chebyshev from the corrected iterate
-  k_amg_prolong0<NT><<<nblk(n0), 256, 0, st>>>(nf, H->pcol0.p, H->pval0.p, L1.x.p, z0);
+  k_amg_prolong0<NT><<<nblk(n0), 256, 0, st>>>(nf, H->pcol0.p, H->pval0.p, L1.x.p, z0, H->face_prob.p, cst);
   k_amg_face_cheb<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
-                                                z0, H->x0.p, H->d0.p, 0);
+                                                z0, H->x0.p, H->d0.p, 0, cst);
   k_amg_face_cheb<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
-                                                H->x0.p, z0, H->d0.p, 1);
-  launches += 3;
-  (void)launches;  // counted by the caller per replay (amg_cycle_launches)
+                                                H->x0.p, z0, H->d0.p, 1, cst);
 }
 
 }  // namespace
@@ -1095,13 +1119,13 @@ int amg_cycle_launches(const hdg_system* s) {
   return 4 + 3 * (nl - 1) + 1 + 3 * (nl - 1) + 3;
 }
 
-void amg_apply(hdg_system* s, const float* r, float* z, cudaStream_t st) {
+void amg_apply(hdg_system* s, const float* r, float* z, const int32_t* cg_state, cudaStream_t st) {
   const float* v0 = s->amg->val0f.p ? s->amg->val0f.p : s->d_valf.p;
   switch (s->nt) {
-    case 2: apply_nt<2>(s, v0, r, z, st); break;
-    case 3: apply_nt<3>(s, v0, r, z, st); break;
-    case 4: apply_nt<4>(s, v0, r, z, st); break;
-    case 5: apply_nt<5>(s, v0, r, z, st); break;
+    case 2: apply_nt<2>(s, v0, r, z, cg_state, st); break;
+    case 3: apply_nt<3>(s, v0, r, z, cg_state, st); break;
+    case 4: apply_nt<4>(s, v0, r, z, cg_state, st); break;
+    case 5: apply_nt<5>(s, v0, r, z, cg_state, st); break;
   }
   HDG_CUDA(cudaGetLastError());
 }

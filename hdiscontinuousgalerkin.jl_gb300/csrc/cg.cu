@@ -35,7 +35,7 @@ constexpr int CG_BLOCK = 256;
 template <typename T> constexpr int cg_min_blocks() { return sizeof(T) == sizeof(float) ? 6 : 4; }
 constexpr int SAMPLE_EVERY = 8;  // with profiling on, every 8th chunk runs un-graphed and timed
 constexpr int SC = 10;           // per problem: rz, rz_old, pq, rr, bb, tol2, alpha, beta, rr_true, -
-constexpr int ST = 4;            // per problem: status, iterations, maxit, refine flag
+constexpr int ST = HDG_CG_ST;    // per problem: status, iterations, maxit, refine flag
 constexpr double DELTA = 0.1;    // refine once the recursive residual fell by this factor
 // status: 0 running, 1 converged (recursive, FP64), 2 iteration cap, 3 breakdown (p'Ap <= 0),
 //         4 converged (true residual, mixed), 5 stopped (mixed: cap or stagnation)
@@ -531,7 +531,7 @@ template <int NT> struct SolverNT : CgSolver {
       k_cg_a<NT, T><<<s->nseg, CG_BLOCK, 0, stream>>>(a);
       if (mg) {
         k_cg_b_mg<NT><<<s->nseg, CG_BLOCK, 0, stream>>>(a, c->r32.p);
-        amg_apply(s, c->r32.p, c->z32.p, stream);
+        amg_apply(s, c->r32.p, c->z32.p, c->st.p, stream);
         k_cg_c<NT><<<s->nseg, CG_BLOCK, 0, stream>>>(a, c->z32.p, 0, 0);
       } else {
         k_cg_b<NT, T><<<s->nseg, CG_BLOCK, 0, stream>>>(a, 0);
@@ -559,7 +559,11 @@ template <int NT> struct SolverNT : CgSolver {
 
   void prepare(const hdg_solver& o) override {
     mg = (o.preconditioner == HDG_PRECOND_AMG);
-    mixed = (o.precision == HDG_PREC_MIXED) && !mg;  // the multigrid iteration runs in FP64
+    // The multigrid iteration runs in FP64.  An FP32 multigrid iteration with FP64 reliable
+    // updates was built and measured: on the high-contrast batch it needed up to 1.5x the
+    // iterations (474 -> 726) and lost 25 % overall, and it did not reach 1e-12 on a
+    // 131072-cell p=2 problem.
+    mixed = (o.precision == HDG_PREC_MIXED) && !mg;
     chunk = o.chunk > 1 ? (o.chunk + 1) / 2 * 2 : 2;  // even: the FP32 iteration alternates p buffers
     if (mg) chunk = std::min(chunk, 8);  // a multigrid iteration is ~25 launches
     if (c->nprob != nprob || c->nrow != nrow) {
@@ -609,7 +613,7 @@ template <int NT> struct SolverNT : CgSolver {
       a64 = CgArgs<double>{seg(), s->d_bcol5.p, s->nf, s->d_val.p, s->d_b.p, c->dinv.p, s->d_x.p, c->r.p, c->z.p,
                            c->p.p, c->q.p, c->p.p, c->sc.p, c->st.p, nullptr, nullptr};
       k_cg_init_mg<NT><<<s->nseg, CG_BLOCK, 0, st>>>(a64, c->r32.p);
-      amg_apply(s, c->r32.p, c->z32.p, st);
+      amg_apply(s, c->r32.p, c->z32.p, c->st.p, st);
       k_cg_c<NT><<<s->nseg, CG_BLOCK, 0, st>>>(a64, c->z32.p, 1, 0);
       // the graph holds the hierarchy's buffers: rebuilt after a Jacobi solve or a new setup
       if (c->graph64 && (!c->graph_mg || c->graph_amg_gen != s->amg_gen)) {
@@ -665,7 +669,7 @@ template <int NT> struct SolverNT : CgSolver {
         if constexpr (sizeof(T) == sizeof(double)) {
           if (mg) {  // the update, the V-cycle and the r.z kernel are timed together
             k_cg_b_mg<NT><<<s->nseg, CG_BLOCK, 0, st>>>(a, c->r32.p);
-            amg_apply(s, c->r32.p, c->z32.p, st);
+            amg_apply(s, c->r32.p, c->z32.p, c->st.p, st);
             k_cg_c<NT><<<s->nseg, CG_BLOCK, 0, st>>>(a, c->z32.p, 0, 0);
           } else {
             k_cg_b<NT, T><<<s->nseg, CG_BLOCK, 0, st>>>(a, 0);
@@ -712,7 +716,7 @@ template <int NT> struct SolverNT : CgSolver {
     HDG_CUDA(cudaGetLastError());
     s->ctx->launches++;
     if (mg && replace) {  // z for the replaced residuals, and a restart (beta = 0) of those problems
-      amg_apply(s, c->r32.p, c->z32.p, st);
+      amg_apply(s, c->r32.p, c->z32.p, c->st.p, st);
       k_cg_c<NT><<<s->nseg, CG_BLOCK, 0, st>>>(a64, c->z32.p, 1, 1);
       HDG_CUDA(cudaGetLastError());
       s->ctx->launches++;

@@ -305,6 +305,9 @@ struct hdg_system {
   }
 };
 
+// Per-problem CG state: HDG_CG_ST ints (status, iterations, iteration cap, refine flag).
+constexpr int HDG_CG_ST = 4;
+
 // ------------------------------------------------------------------ kernel launchers
 void launch_element_condense(hdg_system* s, cudaStream_t st);
 void launch_gather(hdg_system* s, cudaStream_t st);
@@ -344,7 +347,9 @@ void destroy_cg(CgState* c);
 void destroy_amg(AmgHierarchy* h);
 void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face);
 void amg_setup_numeric(hdg_system* s, cudaStream_t st);
-void amg_apply(hdg_system* s, const float* r, float* z, cudaStream_t st);  // z = M^-1 r (FP32)
+// z = M^-1 r (FP32).  cg_state: the CG's per-problem state (HDG_CG_ST ints per problem; NULL: all
+// problems); problems that neither iterate nor wait for a refinement are skipped.
+void amg_apply(hdg_system* s, const float* r, float* z, const int32_t* cg_state, cudaStream_t st);
 int amg_cycle_launches(const hdg_system* s);                             // kernels per V-cycle
 double amg_cycle_bytes(const hdg_system* s);                             // algorithmic bytes per V-cycle
 
