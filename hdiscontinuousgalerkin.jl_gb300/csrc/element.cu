@@ -38,25 +38,30 @@ struct ElemArgs {
 
 // One warp per cell; EWARPS warps (cells) per CTA, picked per degree, quadrature size and mesh
 // size by the launch-time autotuner below.
-template <int P, int EWARPS> __global__ void __launch_bounds__(EWARPS * 32) k_element_condense(ElemArgs a) {
+template <int P, int EWARPS, bool SCHUR>
+__global__ void __launch_bounds__(EWARPS * 32) k_element_condense(ElemArgs a) {
   using D = Dims<P>;
-  constexpr int NW = D::NW, NT = D::NT, NV = D::NV, N = D::N, M = D::M, NC = D::NC, LD = D::LD;
+  constexpr int NW = D::NW, NT = D::NT, NV = D::NV, N = D::N, M = D::M, NC = D::NC;
+  // Per-warp scratch: the full path holds the augmented system [Me | EF | Bte] (row stride
+  // D::LD, solution X in columns N..N+M); the Schur path holds the reduced nw x (nw+m+1) system,
+  // then X in columns M+1..2M+1 and Y_f in columns 0..M (row stride 2(M+1), odd).
+  constexpr int LDW = SCHUR ? ((2 * (M + 1)) | 1) : D::LD;
+  constexpr int XO = SCHUR ? (M + 1) : N;  // first column of X
+  static_assert(!SCHUR || NW + M + 1 <= LDW, "reduced system must fit the scratch rows");
   extern __shared__ double smem[];
   double* ref = smem;
-  const int ref_len = a.ref_len;
-  for (int i = threadIdx.x; i < ref_len; i += blockDim.x) ref[i] = a.ref[i];
   const int nq = a.nq;
-  const RefLayout L = [&] {
+  RefLayout L = [&] {
     RefLayout l;
     int o = 0;
     l.M = o; o += NW * NW;
     l.D0 = o; o += NW * NW;
     l.D1 = o; o += NW * NW;
+    l.N = o; o += NW * nq;
     l.C = o; o += 3 * NW * NW;
     l.F = o; o += 6 * NW * NT;
     l.H = o; o += NT * NT;
     l.NW = o; o += NW * nq;
-    l.N = o; o += NW * nq;
     l.Q = o; o += 2 * nq;
     l.SMD0 = o; o += NW * NW;
     l.SMD1 = o; o += NW * NW;
@@ -68,10 +73,20 @@ template <int P, int EWARPS> __global__ void __launch_bounds__(EWARPS * 32) k_el
     l.total = o;
     return l;
   }();
+  // The tables a path reads sit in one contiguous range of the packed table: [M .. Q] for the
+  // full LU, [C .. end] for the Schur path; only that range is staged in shared memory.
+  const int stage0 = SCHUR ? L.C : 0;
+  const int ref_len = a.ref_len;
+  for (int i = threadIdx.x; i < ref_len; i += blockDim.x) ref[i] = a.ref[stage0 + i];
+  if (SCHUR) {
+    L.C -= stage0; L.F -= stage0; L.H -= stage0; L.NW -= stage0; L.Q -= stage0;
+    L.SMD0 -= stage0; L.SMD1 -= stage0; L.SQ00 -= stage0; L.SQ01 -= stage0; L.SQ11 -= stage0;
+    L.SMF -= stage0; L.SDMF -= stage0;
+  }
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int wstride = N * LD + 2 * nq + NW + N + 2;
+  const int wstride = N * LDW + 2 * nq + NW + N + 2;
   double* W = smem + ((ref_len + 1) & ~1) + warp * wstride;
-  double* sq = W + N * LD;  // per-warp scratch: f (or kappa^-1) at the quadrature points, be
+  double* sq = W + N * LDW;  // per-warp scratch: f (or kappa^-1) at the quadrature points, be
   __syncthreads();
 
   for (int e = blockIdx.x * EWARPS + warp; e < a.nc; e += gridDim.x * EWARPS) {
@@ -119,7 +134,7 @@ template <int P, int EWARPS> __global__ void __launch_bounds__(EWARPS * 32) k_el
       be[i] = s * detJ;
     }
     __syncwarp();
-    if (a.schur) {
+    if constexpr (SCHUR) {
       // ---- Schur-complement path ------------------------------------------------------------
       // Me = [A -B; B' C] with A = (det J / kappa) diag(M, M), so with kf = kappa / det J:
       //   S  = C + kf sum_c B_c' M^-1 B_c = C + kf (a00 Q00 + a01 (Q01 + Q01') + a11 Q11),
@@ -154,7 +169,7 @@ template <int P, int EWARPS> __global__ void __launch_bounds__(EWARPS * 32) k_el
         } else {
           v = be[ia];
         }
-        W[ia * LD + col] = v;
+        W[ia * LDW + col] = v;
       }
       __syncwarp();
       double* rinv = be + NW;
@@ -162,7 +177,7 @@ template <int P, int EWARPS> __global__ void __launch_bounds__(EWARPS * 32) k_el
         unsigned long long best = 0ull;
         int bi = NW;
         for (int i = k + lane; i < NW; i += 32) {
-          const unsigned long long v = (unsigned long long)__double_as_longlong(W[i * LD + k]) & 0x7fffffffffffffffull;
+          const unsigned long long v = (unsigned long long)__double_as_longlong(W[i * LDW + k]) & 0x7fffffffffffffffull;
           if (v > best || (v == best && i < bi)) { best = v; bi = i; }
         }
 #pragma unroll
@@ -174,37 +189,37 @@ template <int P, int EWARPS> __global__ void __launch_bounds__(EWARPS * 32) k_el
         if (best == 0ull && lane == 0) atomicOr(a.err, 2);
         if (bi != k) {
           for (int j = k + lane; j < RC; j += 32) {
-            double t = W[k * LD + j];
-            W[k * LD + j] = W[bi * LD + j];
-            W[bi * LD + j] = t;
+            double t = W[k * LDW + j];
+            W[k * LDW + j] = W[bi * LDW + j];
+            W[bi * LDW + j] = t;
           }
           __syncwarp();
         }
-        const double pinv = 1.0 / W[k * LD + k];
+        const double pinv = 1.0 / W[k * LDW + k];
         if (lane == 0) rinv[k] = pinv;
-        for (int i = k + 1 + lane; i < NW; i += 32) W[i * LD + k] *= pinv;
+        for (int i = k + 1 + lane; i < NW; i += 32) W[i * LDW + k] *= pinv;
         __syncwarp();
         const int cols = RC - k - 1, rows = NW - k - 1;
         for (int t = lane; t < rows * cols; t += 32) {
           const int i = k + 1 + t / cols, j = k + 1 + (t - (t / cols) * cols);
-          W[i * LD + j] -= W[i * LD + k] * W[k * LD + j];
+          W[i * LDW + j] -= W[i * LDW + k] * W[k * LDW + j];
         }
         __syncwarp();
       }
       for (int k = NW - 1; k >= 0; --k) {
         const double dinv = rinv[k];
-        for (int j = lane; j <= M; j += 32) W[k * LD + NW + j] *= dinv;
+        for (int j = lane; j <= M; j += 32) W[k * LDW + NW + j] *= dinv;
         __syncwarp();
         for (int t = lane; t < k * (M + 1); t += 32) {
           const int i = t / (M + 1), j = t - (t / (M + 1)) * (M + 1);
-          W[i * LD + NW + j] -= W[i * LD + k] * W[k * LD + NW + j];
+          W[i * LDW + NW + j] -= W[i * LDW + k] * W[k * LDW + NW + j];
         }
         __syncwarp();
       }
-      // X2 -> the u rows of X (rows NV.., columns N..), clear of the reduced system's rows
+      // X2 -> the u rows of X (rows NV.., columns XO..), clear of the reduced system's rows
       for (int t = lane; t < NW * (M + 1); t += 32) {
         const int ib = t / (M + 1), j = t - ib * (M + 1);
-        W[(NV + ib) * LD + N + j] = W[ib * LD + NW + j];
+        W[(NV + ib) * LDW + XO + j] = W[ib * LDW + NW + j];
       }
       __syncwarp();
       // X1 -> the q rows of X
@@ -214,13 +229,13 @@ template <int P, int EWARPS> __global__ void __launch_bounds__(EWARPS * 32) k_el
         const double adl0 = c ? ad01 : ad00, adl1 = c ? ad11 : ad10;
         double s = 0.0;
         for (int ib = 0; ib < NW; ++ib)
-          s += (adl0 * ref[L.SMD0 + ia * NW + ib] + adl1 * ref[L.SMD1 + ia * NW + ib]) * W[(NV + ib) * LD + N + j];
+          s += (adl0 * ref[L.SMD0 + ia * NW + ib] + adl1 * ref[L.SMD1 + ia * NW + ib]) * W[(NV + ib) * LDW + XO + j];
         if (j < M) {
           const int f = j / NT, jj = j - f * NT;
           const int o = (ob >> f) & 1;
           s -= wn[f][c] * ref[L.SMF + ((f * 2 + o) * NW + ia) * NT + jj];
         }
-        W[r * LD + N + j] = kf * s;
+        W[r * LDW + XO + j] = kf * s;
       }
       __syncwarp();
     } else {
@@ -270,7 +285,7 @@ template <int P, int EWARPS> __global__ void __launch_bounds__(EWARPS * 32) k_el
             v = be[ia];
           }
         }
-        W[r * LD + col] = v;
+        W[r * LDW + col] = v;
       }
       __syncwarp();
       // ---- Gaussian elimination with partial pivoting --------------------------------------
@@ -282,7 +297,7 @@ template <int P, int EWARPS> __global__ void __launch_bounds__(EWARPS * 32) k_el
         unsigned long long best = 0ull;
         int bi = N;
         for (int i = k + lane; i < N; i += 32) {
-          const unsigned long long v = (unsigned long long)__double_as_longlong(W[i * LD + k]) & 0x7fffffffffffffffull;
+          const unsigned long long v = (unsigned long long)__double_as_longlong(W[i * LDW + k]) & 0x7fffffffffffffffull;
           if (v > best || (v == best && i < bi)) { best = v; bi = i; }
         }
 #pragma unroll
@@ -294,31 +309,31 @@ template <int P, int EWARPS> __global__ void __launch_bounds__(EWARPS * 32) k_el
         if (best == 0ull && lane == 0) atomicOr(a.err, 2);
         if (bi != k) {
           for (int j = k + lane; j < NC; j += 32) {
-            double t = W[k * LD + j];
-            W[k * LD + j] = W[bi * LD + j];
-            W[bi * LD + j] = t;
+            double t = W[k * LDW + j];
+            W[k * LDW + j] = W[bi * LDW + j];
+            W[bi * LDW + j] = t;
           }
           __syncwarp();
         }
-        const double pinv = 1.0 / W[k * LD + k];
+        const double pinv = 1.0 / W[k * LDW + k];
         if (lane == 0) rinv[k] = pinv;
-        for (int i = k + 1 + lane; i < N; i += 32) W[i * LD + k] *= pinv;
+        for (int i = k + 1 + lane; i < N; i += 32) W[i * LDW + k] *= pinv;
         __syncwarp();
         const int cols = NC - k - 1, rows = N - k - 1;
         for (int t = lane; t < rows * cols; t += 32) {
           const int i = k + 1 + t / cols, j = k + 1 + (t - (t / cols) * cols);
-          W[i * LD + j] -= W[i * LD + k] * W[k * LD + j];
+          W[i * LDW + j] -= W[i * LDW + k] * W[k * LDW + j];
         }
         __syncwarp();
       }
       // ---- back substitution on the m+1 right-hand sides -----------------------------------
       for (int k = N - 1; k >= 0; --k) {
         const double dinv = rinv[k];
-        for (int j = lane; j <= M; j += 32) W[k * LD + N + j] *= dinv;
+        for (int j = lane; j <= M; j += 32) W[k * LDW + N + j] *= dinv;
         __syncwarp();
         for (int t = lane; t < k * (M + 1); t += 32) {
           const int i = t / (M + 1), j = t - (t / (M + 1)) * (M + 1);
-          W[i * LD + N + j] -= W[i * LD + k] * W[k * LD + N + j];
+          W[i * LDW + N + j] -= W[i * LDW + k] * W[k * LDW + N + j];
         }
         __syncwarp();
       }
@@ -327,13 +342,13 @@ template <int P, int EWARPS> __global__ void __launch_bounds__(EWARPS * 32) k_el
     double* KB = a.KB + (size_t)e * N * (M + 1);
     for (int t = lane; t < N * (M + 1); t += 32) {
       const int r = t / (M + 1), j = t - (t / (M + 1)) * (M + 1);
-      KB[t] = W[r * LD + N + j];
+      KB[t] = W[r * LDW + XO + j];
     }
     for (int t = lane; t < 3 * NW * (M + 1); t += 32) {
       const int fa = t / (M + 1), j = t - (t / (M + 1)) * (M + 1);
       const int f = fa / NW, ia = fa - f * NW;
-      W[fa * LD + j] = wn[f][0] * W[ia * LD + N + j] + wn[f][1] * W[(NW + ia) * LD + N + j] +
-                       tau * el[f] * W[(NV + ia) * LD + N + j];
+      W[fa * LDW + j] = wn[f][0] * W[ia * LDW + XO + j] + wn[f][1] * W[(NW + ia) * LDW + XO + j] +
+                       tau * el[f] * W[(NV + ia) * LDW + XO + j];
     }
     __syncwarp();
     // ---- [Ate | bte] ----------------------------------------------------------------------
@@ -345,7 +360,7 @@ template <int P, int EWARPS> __global__ void __launch_bounds__(EWARPS * 32) k_el
       const double* F = ref + L.F + (f * 2 + o) * NW * NT;
       double s = 0.0;
 #pragma unroll
-      for (int ia = 0; ia < NW; ++ia) s += F[ia * NT + i] * W[(f * NW + ia) * LD + col];
+      for (int ia = 0; ia < NW; ++ia) s += F[ia * NT + i] * W[(f * NW + ia) * LDW + col];
       double v;
       if (col < M) {
         const int g = col / NT, j = col - g * NT;
@@ -359,9 +374,10 @@ template <int P, int EWARPS> __global__ void __launch_bounds__(EWARPS * 32) k_el
   }
 }
 
-template <int P, int EWARPS> size_t smem_bytes(const ElemArgs& a) {
+template <int P, int EWARPS, bool SCHUR> size_t smem_bytes(const ElemArgs& a) {
   using D = Dims<P>;
-  const int wstride = D::N * D::LD + 2 * a.nq + D::NW + D::N + 2;
+  constexpr int LDW = SCHUR ? ((2 * (D::M + 1)) | 1) : D::LD;
+  const int wstride = D::N * LDW + 2 * a.nq + D::NW + D::N + 2;
   return (size_t)(((a.ref_len + 1) & ~1) + EWARPS * wstride) * sizeof(double);
 }
 
@@ -369,38 +385,49 @@ constexpr size_t ELEM_SMEM_MAX = 200 * 1024;
 
 // Launches the kernel with EWARPS warps per CTA and a grid of `oversub` x the resident CTAs
 // (a grid-stride loop covers the rest).  Returns false when the configuration does not fit.
-template <int P, int EWARPS> bool launch_pw(hdg_system* s, cudaStream_t st, const ElemArgs& a, int oversub) {
-  const size_t smem = smem_bytes<P, EWARPS>(a);
+template <int P, int EWARPS, bool SCHUR>
+bool launch_pw(hdg_system* s, cudaStream_t st, const ElemArgs& a, int oversub) {
+  const size_t smem = smem_bytes<P, EWARPS, SCHUR>(a);
   if (smem > ELEM_SMEM_MAX) return false;
   static bool attr_set = false;
   if (!attr_set) {
-    HDG_CUDA(cudaFuncSetAttribute(k_element_condense<P, EWARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    HDG_CUDA(cudaFuncSetAttribute(k_element_condense<P, EWARPS, SCHUR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)ELEM_SMEM_MAX));
     attr_set = true;
   }
   int dev_sms = 152;
   cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, s->ctx->device);
   int blocks_per_sm = 0;
-  HDG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_element_condense<P, EWARPS>, EWARPS * 32,
+  HDG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_element_condense<P, EWARPS, SCHUR>, EWARPS * 32,
                                                          smem));
   if (blocks_per_sm < 1) return false;
   const long need = (a.nc + EWARPS - 1) / EWARPS;
   long grid = std::min<long>(need, (long)dev_sms * blocks_per_sm * oversub);
   if (grid < 1) grid = 1;
-  k_element_condense<P, EWARPS><<<(unsigned)grid, EWARPS * 32, smem, st>>>(a);
+  k_element_condense<P, EWARPS, SCHUR><<<(unsigned)grid, EWARPS * 32, smem, st>>>(a);
   HDG_CUDA(cudaGetLastError());
   s->ctx->launches++;
   return true;
 }
 
-template <int P> bool launch_cfg(hdg_system* s, cudaStream_t st, const ElemArgs& a, int warps, int oversub) {
+template <int P, bool SCHUR>
+bool launch_cfg_path(hdg_system* s, cudaStream_t st, const ElemArgs& a, int warps, int oversub) {
   switch (warps) {
-    case 1: return launch_pw<P, 1>(s, st, a, oversub);
-    case 2: return launch_pw<P, 2>(s, st, a, oversub);
-    case 4: return launch_pw<P, 4>(s, st, a, oversub);
-    case 8: return launch_pw<P, 8>(s, st, a, oversub);
+    case 1: return launch_pw<P, 1, SCHUR>(s, st, a, oversub);
+    case 2: return launch_pw<P, 2, SCHUR>(s, st, a, oversub);
+    case 4: return launch_pw<P, 4, SCHUR>(s, st, a, oversub);
+    case 8: return launch_pw<P, 8, SCHUR>(s, st, a, oversub);
   }
   return false;
+}
+
+// P = 2 never takes the Schur path with the default rule (Strang(3) leaves M^ of rank 5), so its
+// Schur kernels are not built; launch_element_condense keeps it on the full LU.
+template <int P> bool launch_cfg(hdg_system* s, cudaStream_t st, const ElemArgs& a, int warps, int oversub) {
+  if constexpr (P != 2) {
+    if (a.schur) return launch_cfg_path<P, true>(s, st, a, warps, oversub);
+  }
+  return launch_cfg_path<P, false>(s, st, a, warps, oversub);
 }
 
 // Autotuner: the first launch for a (device, degree, quadrature size, log2 of the cell count, path)
@@ -476,9 +503,11 @@ void launch_element_condense(hdg_system* s, cudaStream_t st) {
   a.err = reinterpret_cast<int*>(s->d_scal.p + 1);
   // Schur path: invertible reference mass and kappa constant on each cell (a kappa field makes
   // Ae a weighted mass matrix that is no multiple of the reference one)
-  a.schur = (sp->t.schur && a.kappa_mode != 2 && std::getenv("HDG_ELEMENT_FULL_LU") == nullptr) ? 1 : 0;
-  // the Schur tables sit at the end of the packed table: the full-LU path leaves them in HBM
-  if (!a.schur) a.ref_len = ref_layout(sp->t.nw, sp->t.nt, sp->t.nq).SMD0;
+  a.schur = (sp->t.schur && a.kappa_mode != 2 && sp->t.p != 2 && std::getenv("HDG_ELEMENT_FULL_LU") == nullptr) ? 1
+                                                                                                                 : 0;
+  // each path stages only the range of the packed table it reads (see the kernel)
+  const RefLayout RL = ref_layout(sp->t.nw, sp->t.nt, sp->t.nq);
+  a.ref_len = a.schur ? RL.total - RL.C : RL.SMD0;
   switch (sp->t.p) {
     case 1: launch_p<1>(s, st, a); break;
     case 2: launch_p<2>(s, st, a); break;

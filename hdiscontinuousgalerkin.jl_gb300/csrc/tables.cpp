@@ -192,14 +192,15 @@ const double EDGE[3][4] = {{1, 0, 0, 1}, {0, 1, 0, 0}, {0, 0, 1, 0}};
 RefLayout ref_layout(int nw, int nt, int nq) {
   RefLayout L;
   int o = 0;
+  // the full-LU path reads [M .. Q], the Schur path [C .. SDMF]: each range is contiguous
   L.M = o; o += nw * nw;
   L.D0 = o; o += nw * nw;
   L.D1 = o; o += nw * nw;
+  L.N = o; o += nw * nq;
   L.C = o; o += 3 * nw * nw;
   L.F = o; o += 6 * nw * nt;
   L.H = o; o += nt * nt;
   L.NW = o; o += nw * nq;
-  L.N = o; o += nw * nq;
   L.Q = o; o += 2 * nq;
   L.SMD0 = o; o += nw * nw;
   L.SMD1 = o; o += nw * nw;
