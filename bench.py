@@ -220,8 +220,10 @@ def run_c4(args, ws, rank, local):
 
     # ---- end to end through the public API with host buffers ----
     def e2e_step():
-        res = B.solve(tol=tol, reassemble=True, preconditioner=pc)  # H2D: kappa, sources, tau, Dirichlet data
-        return res, B.solutions()                 # D2H: uhat, q, u of every problem
+        # H2D: kappa, sources, tau, Dirichlet data; D2H inside the step: uhat, q, u of every
+        # problem into page-locked host arrays, each bin as soon as it is recovered
+        res = B.solve(tol=tol, reassemble=True, preconditioner=pc, download=True)
+        return res, B.solutions(downloaded=True)
     e2e_step()
     torch.cuda.synchronize()
     barrier(ws)

@@ -22,7 +22,7 @@ ERRORS = {
 }
 PREC_FP64, PREC_MIXED = 0, 1
 PRECOND_JACOBI, PRECOND_AMG = 0, 1
-STEP_ASSEMBLE, STEP_APPLY, STEP_RECOVER = 1, 2, 4  # hdg_batch_step flags
+STEP_ASSEMBLE, STEP_APPLY, STEP_RECOVER, STEP_DOWNLOAD = 1, 2, 4, 8  # hdg_batch_step flags
 FIELD_CONST, FIELD_SINSIN, FIELD_BUMPS, FIELD_FOURIER, FIELD_EXP_FOURIER = 0, 1, 2, 3, 4
 
 
@@ -106,6 +106,9 @@ SIGNATURES = {
     "hdg_system_set_coefficients_batch": ([vp, dp, C.POINTER(hdg_field), C.POINTER(hdg_field), dp], ip),
     "hdg_system_set_dirichlet": ([vp, i32p, dp, ip], ip),
     "hdg_batch_step": ([ip, C.POINTER(vp), C.POINTER(hdg_solver), ip, C.POINTER(hdg_stats)], ip),
+    "hdg_host_alloc": ([C.c_size_t, C.POINTER(vp)], ip),
+    "hdg_host_free": ([vp], ip),
+    "hdg_system_set_download": ([vp, dp, dp], ip),
     "hdg_system_get_solution": ([vp, dp, dp], ip),
     "hdg_engine_create": ([vp, C.c_double, ip, ip, C.POINTER(hdg_solver), C.POINTER(vp)], ip),
     "hdg_engine_add_resident_mesh": ([vp, vp, ip, intp], ip),

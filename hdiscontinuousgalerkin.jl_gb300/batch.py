@@ -84,6 +84,8 @@ class Bin:
         self.ndofs, self.n = nd.value, n.value
         self._dirichlet()
         self._dir_set = False
+        self._dl = None
+        self._host_bufs = []
 
     def _coef_arrays(self):
         np_ = len(self.problems)
@@ -137,11 +139,30 @@ class Bin:
         L.check(L.load().hdg_system_timings(self.h, C.byref(t)), self.ctx.handle)
         return {k: getattr(t, k) for k, _ in L.hdg_timings._fields_}
 
-    def solution(self):
-        """Per problem (uhat, q, u) on the host."""
-        uh = np.zeros(self.ndofs)
-        qu = np.zeros(self.mesh.ncells * self.n)
-        L.check(L.load().hdg_system_get_solution(self.h, L.dptr(uh), L.dptr(qu)), self.ctx.handle)
+    def _pinned(self, count):
+        ptr = C.c_void_p()
+        L.check(L.load().hdg_host_alloc(C.c_size_t(8 * count), C.byref(ptr)), self.ctx.handle)
+        self._host_bufs.append(ptr)
+        return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_double)), shape=(count,))
+
+    def enable_download(self):
+        """Page-locked host arrays that each pipelined step fills with (uhat, [q; u])."""
+        if self._dl is None:
+            uh = self._pinned(self.ndofs)
+            qu = self._pinned(self.mesh.ncells * self.n)
+            L.check(L.load().hdg_system_set_download(self.h, L.dptr(uh), L.dptr(qu)), self.ctx.handle)
+            self._dl = (uh, qu)
+        return self._dl
+
+    def solution(self, downloaded=False):
+        """Per problem (uhat, q, u) on the host.  downloaded=True reads the page-locked arrays
+        that the last step filled (views, valid until the next step) instead of copying."""
+        if downloaded and self._dl is not None:
+            uh, qu = self._dl
+        else:
+            uh = np.zeros(self.ndofs)
+            qu = np.zeros(self.mesh.ncells * self.n)
+            L.check(L.load().hdg_system_get_solution(self.h, L.dptr(uh), L.dptr(qu)), self.ctx.handle)
         qu = qu.reshape(self.mesh.ncells, self.n)
         out = []
         for k in range(len(self.problems)):
@@ -155,6 +176,9 @@ class Bin:
             if self.h:
                 L.load().hdg_system_destroy(self.h)
                 self.h = None
+            for ptr in self._host_bufs:
+                L.load().hdg_host_free(ptr)
+            self._host_bufs = []
         except Exception:
             pass
 
@@ -170,14 +194,21 @@ class Batch:
             self.bins.append(Bin(ctx, [self.problems[i] for i in idx], idx, precision))
         self.stats = None
 
-    def solve(self, tol=1e-10, maxit=100000, chunk=32, reassemble=True, preconditioner=L.PRECOND_JACOBI):
+    def solve(self, tol=1e-10, maxit=100000, chunk=32, reassemble=True, preconditioner=L.PRECOND_JACOBI,
+              download=False):
         """assemble + condense, apply!, CG and recovery of every problem, as one pipelined step
         (hdg_batch_step): each degree bin runs on a stream of its own, so one bin's assembly and
         recovery overlap the other bins' iterations.
         reassemble: True (upload the coefficients and Dirichlet data, then assemble), "resident"
         (assemble from the coefficients and Dirichlet data already on the device) or False (keep
-        the assembled systems; they must not have been applied yet)."""
+        the assembled systems; they must not have been applied yet).
+        download: copy every problem's solution to page-locked host arrays inside the step, each
+        bin as soon as it is recovered (read them with solutions(downloaded=True))."""
         flags = L.STEP_APPLY | L.STEP_RECOVER
+        if download:
+            flags |= L.STEP_DOWNLOAD
+            for b in self.bins:
+                b.enable_download()
         for b in self.bins:
             if reassemble is True:
                 b.set_coefficients()
@@ -203,10 +234,12 @@ class Batch:
         self.stats = stats
         return stats
 
-    def solutions(self):
+    def solutions(self, downloaded=False):
+        """Per problem (uhat, q, u).  downloaded=True returns views of the page-locked arrays that
+        the last solve(download=True) filled (valid until the next solve)."""
         out = [None] * len(self.problems)
         for b in self.bins:
-            for i, sol in zip(b.idx, b.solution()):
+            for i, sol in zip(b.idx, b.solution(downloaded)):
                 out[i] = sol
         return out
 

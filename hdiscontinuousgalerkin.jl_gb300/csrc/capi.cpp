@@ -842,8 +842,29 @@ int hdg_solve_batch(int nsys, hdg_system* const* systems, const hdg_solver* opts
   });
 }
 
+int hdg_host_alloc(size_t bytes, void** out) {
+  if (!out) return HDG_ERR_ARG;
+  *out = nullptr;
+  if (bytes == 0) return HDG_OK;
+  return cudaMallocHost(out, bytes) == cudaSuccess ? HDG_OK : HDG_ERR_OOM;
+}
+
+int hdg_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+  return HDG_OK;
+}
+
+int hdg_system_set_download(hdg_system* s, double* uhat, double* qu) {
+  if (!s) return HDG_ERR_ARG;
+  s->h_dl_uhat = uhat;
+  s->h_dl_qu = qu;
+  return HDG_OK;
+}
+
 int hdg_batch_step(int nsys, hdg_system* const* systems, const hdg_solver* opts, int flags, hdg_stats* stats) {
-  if (nsys < 1 || !systems || (flags & ~(HDG_STEP_ASSEMBLE | HDG_STEP_APPLY | HDG_STEP_RECOVER))) return HDG_ERR_ARG;
+  if (nsys < 1 || !systems ||
+      (flags & ~(HDG_STEP_ASSEMBLE | HDG_STEP_APPLY | HDG_STEP_RECOVER | HDG_STEP_DOWNLOAD)))
+    return HDG_ERR_ARG;
   hdg_ctx* ctx = systems[0] ? systems[0]->ctx : nullptr;
   if (!ctx) return HDG_ERR_ARG;
   for (int i = 0; i < nsys; ++i) {
@@ -851,6 +872,8 @@ int hdg_batch_step(int nsys, hdg_system* const* systems, const hdg_solver* opts,
     if (!s || s->ctx != ctx) return fail(ctx, HDG_ERR_ARG, "the systems of a step must share one context");
     for (int j = 0; j < i; ++j)
       if (systems[j] == s) return fail(ctx, HDG_ERR_ARG, "a system appears twice in the step");
+    if ((flags & HDG_STEP_DOWNLOAD) && s->h_dl_qu && !(flags & HDG_STEP_RECOVER))
+      return fail(ctx, HDG_ERR_ARG, "downloading (q, u) needs HDG_STEP_RECOVER");
     if (flags & HDG_STEP_APPLY) {
       if (!s->dir_ready) return fail(ctx, HDG_ERR_ARG, "no Dirichlet set recorded (hdg_system_set_dirichlet)");
       if (s->applied && !(flags & HDG_STEP_ASSEMBLE))

@@ -999,11 +999,15 @@ int run_batch_step(const std::vector<hdg_system*>& sys, const hdg_solver& o, int
       g_use_stream = q[i];
       if (sv[i]->process(o)) {
         sv[i]->finish(o, &(*stats)[i]);
+        hdg_system* s = sys[i];
         if (flags & HDG_STEP_RECOVER) {
-          hdg_system* s = sys[i];
           if (s->ctx->profiling) s->ev_recover.start(q[i]);
           launch_recover(s, q[i]);
           if (s->ctx->profiling) s->ev_recover.stop(q[i]);
+        }
+        if (flags & HDG_STEP_DOWNLOAD) {  // on the system's stream: overlaps the others' iterations
+          if (s->h_dl_uhat) s->d_x.download(s->h_dl_uhat, (size_t)s->ndofs, q[i]);
+          if (s->h_dl_qu) s->d_qu.download(s->h_dl_qu, (size_t)s->nc * s->n, q[i]);
         }
         done[i] = 1;
         --left;
@@ -1018,6 +1022,8 @@ int run_batch_step(const std::vector<hdg_system*>& sys, const hdg_solver& o, int
   g_use_stream = nullptr;
   if (flags & HDG_STEP_ASSEMBLE)  // element error flags (the step went on regardless)
     for (size_t i = 0; i < ns; ++i) assembly_check(sys[i], q[i]);
+  if (flags & HDG_STEP_DOWNLOAD)  // the host arrays are complete on return
+    for (size_t i = 0; i < ns; ++i) HDG_CUDA(cudaStreamSynchronize(q[i]));
   int rc = HDG_OK;
   for (size_t i = 0; i < ns; ++i) {
     for (auto& r : (*stats)[i]) {

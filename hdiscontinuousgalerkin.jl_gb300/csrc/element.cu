@@ -222,20 +222,26 @@ __global__ void __launch_bounds__(EWARPS * 32) k_element_condense(ElemArgs a) {
         W[(NV + ib) * LDW + XO + j] = W[ib * LDW + NW + j];
       }
       __syncwarp();
-      // X1 -> the q rows of X
-      for (int t = lane; t < NV * (M + 1); t += 32) {
-        const int r = t / (M + 1), j = t - r * (M + 1);
-        const int c = r / NW, ia = r - c * NW;
-        const double adl0 = c ? ad01 : ad00, adl1 = c ? ad11 : ad10;
-        double s = 0.0;
-        for (int ib = 0; ib < NW; ++ib)
-          s += (adl0 * ref[L.SMD0 + ia * NW + ib] + adl1 * ref[L.SMD1 + ia * NW + ib]) * W[(NV + ib) * LDW + XO + j];
+      // X1 -> the q rows of X: G_l = (M^-1 D_l) X2 for l = 0, 1, then
+      // X1_c = kf (adl0_c G_0 + adl1_c G_1 - wn_f,c MF_{f,o}) for both components at once
+      for (int t = lane; t < NW * (M + 1); t += 32) {
+        const int ia = t / (M + 1), j = t - ia * (M + 1);
+        double g0 = 0.0, g1 = 0.0;
+        for (int ib = 0; ib < NW; ++ib) {
+          const double x2 = W[(NV + ib) * LDW + XO + j];
+          g0 += ref[L.SMD0 + ia * NW + ib] * x2;
+          g1 += ref[L.SMD1 + ia * NW + ib] * x2;
+        }
+        double v0 = ad00 * g0 + ad10 * g1, v1 = ad01 * g0 + ad11 * g1;
         if (j < M) {
           const int f = j / NT, jj = j - f * NT;
           const int o = (ob >> f) & 1;
-          s -= wn[f][c] * ref[L.SMF + ((f * 2 + o) * NW + ia) * NT + jj];
+          const double mf = ref[L.SMF + ((f * 2 + o) * NW + ia) * NT + jj];
+          v0 -= wn[f][0] * mf;
+          v1 -= wn[f][1] * mf;
         }
-        W[r * LDW + XO + j] = kf * s;
+        W[ia * LDW + XO + j] = kf * v0;
+        W[(NW + ia) * LDW + XO + j] = kf * v1;
       }
       __syncwarp();
     } else {

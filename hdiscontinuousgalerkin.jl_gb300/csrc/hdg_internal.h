@@ -270,6 +270,8 @@ struct hdg_system {
   bool applied = false;   // apply! done: d_val/d_b are in solver form (free rows negated)
   bool dir_ready = false; // d_pres/d_gv hold a Dirichlet set (scattered; survives reassembly)
   bool dir_lift = false;  // some prescribed value is nonzero
+  double* h_dl_uhat = nullptr;  // host destinations of HDG_STEP_DOWNLOAD (hdg_system_set_download)
+  double* h_dl_qu = nullptr;
   DevBuf<uint8_t> d_pres;
   DevBuf<double> d_gv;    // prescribed values scattered to dofs
   DevBuf<int32_t> d_dofs; // prescribed dofs (0-based)

@@ -254,12 +254,24 @@ int hdg_system_set_dirichlet(hdg_system* sys, const int32_t* dofs, const double*
 #define HDG_STEP_ASSEMBLE 1 /* assemble + condense from the coefficients on the device */
 #define HDG_STEP_APPLY 2    /* apply! the recorded Dirichlet set */
 #define HDG_STEP_RECOVER 4  /* local recovery of (q, u) after the solve */
+#define HDG_STEP_DOWNLOAD 8 /* copy each system's solution to its registered host arrays */
+/* Page-locked host memory (cudaMallocHost), for download destinations that the device writes
+ * directly and asynchronously. */
+int hdg_host_alloc(size_t bytes, void** out);
+int hdg_host_free(void* p);
+/* Registers host destinations for HDG_STEP_DOWNLOAD: uhat (ndofs) and, after recovery, qu
+ * (ncells x n, as hdg_system_get_solution); either may be NULL.  Page-locked memory
+ * (hdg_host_alloc) lets the copies overlap the other systems' work; pageable memory works but
+ * the copies then hold the host. */
+int hdg_system_set_download(hdg_system* sys, double* uhat, double* qu);
 /* One pipelined step over several systems: per system, on a CUDA stream of its own,
  * [assemble + condense] -> [apply!] -> CG -> [recovery], so that one system's assembly and
  * recovery overlap the other systems' iterations.  The results equal those of
  * hdg_system_reassemble_resident, hdg_apply_dirichlet, hdg_solve_batch and hdg_recover called
  * in turn.  Without HDG_STEP_APPLY the systems must be applied already (and HDG_STEP_ASSEMBLE,
- * which undoes apply!, is then refused).  stats: one entry per problem, systems in order. */
+ * which undoes apply!, is then refused).  With HDG_STEP_DOWNLOAD each system's solution is
+ * copied to its registered host arrays on its own stream as soon as it is recovered; the call
+ * returns once every copy has landed.  stats: one entry per problem, systems in order. */
 int hdg_batch_step(int nsys, hdg_system* const* systems, const hdg_solver* opts, int flags, hdg_stats* stats);
 /* Device solution of a system: trace values (ndofs) and, after recovery, [q; u] per cell (ncells x n). */
 int hdg_system_get_solution(const hdg_system* sys, double* uhat, double* qu);

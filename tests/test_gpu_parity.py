@@ -348,6 +348,15 @@ def test_pipelined_step_equals_sequential_calls(H, pc):
         for x, y, z in zip(a, b_, c):
             assert np.array_equal(x, y) and np.array_equal(x, z)
     assert [s.iterations for s in st1] == [s.iterations for s in st2]
+    # in-step downloads into page-locked arrays give the same arrays as the copies afterwards
+    B.solve(tol=1e-10, reassemble="resident", preconditioner=pcv, download=True)
+    s4 = [tuple(np.array(x) for x in t) for t in B.solutions(downloaded=True)]
+    for a, d in zip(s1, s4):
+        for x, y in zip(a, d):
+            assert np.array_equal(x, y)
+    for a, d in zip(B.solutions(), s4):
+        for x, y in zip(a, d):
+            assert np.array_equal(x, y)
     # a solve without apply! is refused; assembly without apply! is refused
     assert L.load().hdg_batch_step(len(B.bins), arr, C.byref(o), L.STEP_ASSEMBLE, st) == -1  # HDG_ERR_ARG
 
