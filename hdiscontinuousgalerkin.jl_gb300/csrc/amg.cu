@@ -171,8 +171,10 @@ struct AmgHierarchy {
   DevBuf<float> dinv0;       // [nf][nt][nt]
   DevBuf<float> lam0;        // [nprob] Gershgorin bound of D^-1 A0
   DevBuf<int32_t> face_prob; // [nf]
-  DevBuf<float> val0f;       // FP32 trace matrix (when the system has none)
-  DevBuf<float> x0, r0, d0;  // level-0 cycle vectors (iterate, residual, Chebyshev correction)
+  DevBuf<float> val0f;       // FP32 trace matrix; after the numeric set-up D^-1 A0 (block rows scaled)
+  DevBuf<float> x0, r0, d0;  // level-0 cycle vectors (iterate, scaled residual, Chebyshev correction)
+  DevBuf<float> bt0;         // D^-1 b of the current cycle
+  DevBuf<float> dpval0;      // [nf*nt][PW] D P0 (restriction of the scaled residual)
   std::vector<AmgLevel> lev; // lev[0] is level 1
   // coarsest (last level): per-problem dense inverses
   std::vector<int32_t> h_crow0;  // [nprob+1] first coarsest row of each problem
@@ -308,6 +310,8 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
   H->x0.alloc((size_t)nf * nt);
   H->r0.alloc((size_t)nf * nt);
   H->d0.alloc((size_t)nf * nt);
+  H->bt0.alloc((size_t)nf * nt);
+  H->dpval0.alloc((size_t)nf * nt * PW);
   H->lev.clear();
   H->lev.push_back(std::move(L1));
   // coarser levels
@@ -750,6 +754,45 @@ __global__ void k_amg_coarse_inv(const int32_t* __restrict__ crow0, const int32_
   }
 }
 
+// D P0 (D the face-block diagonal of A0), for the restriction of the scaled residual.
+template <int NT>
+__global__ void k_amg_dp0(int nf, const int8_t* __restrict__ kdiag, const float* __restrict__ val,
+                          const float* __restrict__ pval0, float* __restrict__ dpval0) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const int64_t nd = (int64_t)nf * NT;
+  const int kd = kdiag[f];
+  for (int i = 0; i < NT; ++i)
+    for (int c = 0; c < PW; ++c) {
+      float s = 0.f;
+      for (int l = 0; l < NT; ++l)
+        s += val[(kd * NT + l) * nd + (int64_t)f * NT + i] * pval0[((int64_t)f * NT + l) * PW + c];
+      dpval0[((int64_t)f * NT + i) * PW + c] = s;
+    }
+}
+
+// A0 -> D^-1 A0 in place, block row by block row (each face rewrites only its own rows).  Runs
+// after every set-up product that needs A0 itself; the cycle then needs no D^-1 per sweep.
+template <int NT>
+__global__ void k_amg_scale0(int nf, const float* __restrict__ dinv, float* __restrict__ val) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const int64_t nd = (int64_t)nf * NT;
+  float di[NT][NT];
+  for (int i = 0; i < NT; ++i)
+    for (int l = 0; l < NT; ++l) di[i][l] = dinv[((int64_t)f * NT + i) * NT + l];
+  for (int k = 0; k < 5; ++k)
+    for (int j = 0; j < NT; ++j) {
+      float col[NT];
+      for (int l = 0; l < NT; ++l) col[l] = val[(k * NT + j) * nd + (int64_t)f * NT + l];
+      for (int i = 0; i < NT; ++i) {
+        float s = 0.f;
+        for (int l = 0; l < NT; ++l) s += di[i][l] * col[l];
+        val[(k * NT + j) * nd + (int64_t)f * NT + i] = s;
+      }
+    }
+}
+
 // ------------------------------------------------------------------------------------------
 // Cycle kernels.  `st` is the CG's per-problem state (HDG_CG_ST ints per problem: status, ...,
 // refine flag): rows of a problem that has stopped iterating and waits for no refinement are
@@ -770,47 +813,56 @@ template <int NT>
 __global__ void k_amg_face_cheb(int nf, const int32_t* __restrict__ bcol5, const float* __restrict__ val,
                                 const float* __restrict__ dinv, const float* __restrict__ lam,
                                 const int32_t* __restrict__ face_prob, const float* __restrict__ b,
-                                const float* __restrict__ xin, float* __restrict__ xout, float* __restrict__ d,
-                                int step, const int32_t* __restrict__ st) {
+                                float* __restrict__ bt, const float* __restrict__ xin, float* __restrict__ xout,
+                                float* __restrict__ d, int step, const int32_t* __restrict__ st) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf || !amg_live(st, face_prob[f])) return;
   const int64_t nd = (int64_t)nf * NT;
-  float res[NT];
-  for (int i = 0; i < NT; ++i) res[i] = b[(int64_t)f * NT + i];
-  if (xin) {
+  // t = D^-1 (b - A x) = bt - (D^-1 A) x: val holds the block rows of A scaled by D^-1, and
+  // the first step (x = 0) forms bt = D^-1 b for the rest of the cycle
+  float t[NT];
+  if (!xin) {
+    float bv[NT];
+    for (int l = 0; l < NT; ++l) bv[l] = b[(int64_t)f * NT + l];
+    for (int i = 0; i < NT; ++i) {
+      float s = 0.f;
+      for (int l = 0; l < NT; ++l) s += dinv[((int64_t)f * NT + i) * NT + l] * bv[l];
+      t[i] = s;
+      bt[(int64_t)f * NT + i] = s;
+    }
+  } else {
+    for (int i = 0; i < NT; ++i) t[i] = bt[(int64_t)f * NT + i];
     int seen[5];
     int ns = 0;
     for (int k = 0; k < 5; ++k) {
       const int g = bcol5[k * nf + f];
       bool dup = false;
-      for (int t = 0; t < ns; ++t) dup |= (seen[t] == g);
+      for (int u = 0; u < ns; ++u) dup |= (seen[u] == g);
       if (dup) continue;
       seen[ns++] = g;
       for (int j = 0; j < NT; ++j) {
         const float xv = xin[(int64_t)g * NT + j];
-        for (int i = 0; i < NT; ++i) res[i] -= val[(k * NT + j) * nd + (int64_t)f * NT + i] * xv;
+        for (int i = 0; i < NT; ++i) t[i] -= val[(k * NT + j) * nd + (int64_t)f * NT + i] * xv;
       }
     }
   }
   const float hi = fmaxf(lam[face_prob[f]], 1e-30f), lo = hi / CHEB_RATIO;
   const float theta = 0.5f * (hi + lo), delta = 0.5f * (hi - lo), sigma = theta / delta;
   float rp = 1.f / sigma, rc = rp;  // rho_{step-1}, rho_step
-  for (int t = 1; t <= step; ++t) {
+  for (int u = 1; u <= step; ++u) {
     rc = 1.f / (2.f * sigma - rp);
-    if (t < step) rp = rc;
+    if (u < step) rp = rc;
   }
   const float cd = (step == 0) ? 0.f : rc * rp, cr = (step == 0) ? 1.f / theta : 2.f * rc / delta;
   for (int i = 0; i < NT; ++i) {
-    float t = 0.f;
-    for (int l = 0; l < NT; ++l) t += dinv[((int64_t)f * NT + i) * NT + l] * res[l];
     const int64_t row = (int64_t)f * NT + i;
-    const float dn = cr * t + (step == 0 ? 0.f : cd * d[row]);
+    const float dn = cr * t[i] + (step == 0 ? 0.f : cd * d[row]);
     d[row] = dn;
     xout[row] = (xin ? xin[row] : 0.f) + dn;
   }
 }
 
-// r = b - A0 x (level 0)
+// scaled residual r~ = D^-1 (b - A0 x) = bt - (D^-1 A0) x (level 0); the restriction uses D P0
 template <int NT>
 __global__ void k_amg_face_residual(int nf, const int32_t* __restrict__ bcol5, const float* __restrict__ val,
                                     const float* __restrict__ b, const float* __restrict__ x, float* __restrict__ r,
@@ -834,7 +886,7 @@ __global__ void k_amg_face_residual(int nf, const int32_t* __restrict__ bcol5, c
   r[row] = s;
 }
 
-// b1 = P0' r0 and the first l1-Jacobi sweep of level 1: x1 = b1 / dl1
+// b1 = P0' r0 = (D P0)' r~0 and the first l1-Jacobi sweep of level 1: x1 = b1 / dl1
 template <int NT>
 __global__ void k_amg_restrict0(int na, const int32_t* __restrict__ rptr0, const int32_t* __restrict__ rent0,
                                 const float* __restrict__ pval0, const float* __restrict__ r0,
@@ -1007,7 +1059,9 @@ template <int NT> void numeric_nt(hdg_system* s, const float* val0, cudaStream_t
   AmgLevel& L1 = H->lev[0];
   k_amg_rap0<NT><<<nblk(L1.n), 256, 0, st>>>(L1.n, H->wap, H->rptr0.p, H->rent0.p, H->pval0.p, H->apcol0.p,
                                              H->apval0.p, L1.ptr.p, L1.col.p, L1.val.p);
-  s->ctx->launches += 4;
+  k_amg_dp0<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_kdiag.p, val0, H->pval0.p, H->dpval0.p);
+  k_amg_scale0<NT><<<nblk(nf), 256, 0, st>>>(nf, H->dinv0.p, const_cast<float*>(val0));
+  s->ctx->launches += 6;
   for (size_t l = 0; l < H->lev.size(); ++l) {
     AmgLevel& L = H->lev[l];
     k_amg_dl1<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.val.p, L.dl1inv.p);
@@ -1048,11 +1102,12 @@ void apply_nt(hdg_system* s, const float* val0, const float* b0, float* z0, cons
     float* out = ((k - 1 - t) % 2 == 0) ? z0 : H->x0.p;
     const float* in = (t == 0) ? nullptr : (out == z0 ? H->x0.p : z0);
     k_amg_face_cheb<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
-                                                  in, out, H->d0.p, t, cst);
+                                                  H->bt0.p, in, out, H->d0.p, t, cst);
   }
-  k_amg_face_residual<NT><<<nblk(n0), 256, 0, st>>>(nf, s->d_bcol5.p, val0, b0, z0, H->r0.p, H->face_prob.p, cst);
+  k_amg_face_residual<NT><<<nblk(n0), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->bt0.p, z0, H->r0.p, H->face_prob.p,
+                                                    cst);
   AmgLevel& L1 = H->lev[0];
-  k_amg_restrict0<NT><<<nblk(L1.n), 256, 0, st>>>(L1.n, H->rptr0.p, H->rent0.p, H->pval0.p, H->r0.p, L1.dl1inv.p,
+  k_amg_restrict0<NT><<<nblk(L1.n), 256, 0, st>>>(L1.n, H->rptr0.p, H->rent0.p, H->dpval0.p, H->r0.p, L1.dl1inv.p,
                                                   L1.b.p, L1.x.p, L1.prob.p, cst);
   // coarse levels down: x holds the first sweep (from the restriction); the second sweep goes to
   // t, which then holds the level's iterate until the way up
@@ -1086,7 +1141,7 @@ void apply_nt(hdg_system* s, const float* val0, const float* b0, float* z0, cons
     const float* in = (t % 2 == 0) ? z0 : H->x0.p;
     float* out = (t % 2 == 0) ? H->x0.p : z0;
     k_amg_face_cheb<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
-                                                  in, out, H->d0.p, t, cst);
+                                                  H->bt0.p, in, out, H->d0.p, t, cst);
   }
   if (k % 2 == 1) HDG_CUDA(cudaMemcpyAsync(z0, H->x0.p, sizeof(float) * n0, cudaMemcpyDeviceToDevice, st));
 }
@@ -1117,10 +1172,10 @@ double amg_cycle_bytes(const hdg_system* s) {
   const double mat0 = 20.0 * nt * nt * nf + 20.0 * nf;  // FP32 values + block columns
   const double dinv = 4.0 * nt * nt * nf;
   const int k = amg_cheb_degree();
-  double b = 8.0 * n0 + dinv;                              // first sweep: b, dinv -> x
-  b += (2 * k - 1) * (mat0 + dinv + 12.0 * n0);            // k-1 pre-sweeps, k post-sweeps
+  double b = 16.0 * n0 + dinv;                             // first sweep: b, D^-1 -> bt, x, d
+  b += (2 * k - 1) * (mat0 + 20.0 * n0);                   // k-1 pre-sweeps, k post-sweeps (D^-1 A0, bt, x, d)
   if (k % 2 == 1) b += 8.0 * n0;                           // copy of the result
-  b += mat0 + 12.0 * n0;                                   // residual
+  b += mat0 + 12.0 * n0;                                   // residual (D^-1 A0, bt, x -> r~)
   b += 24.0 * n0 + 20.0 * nf + 8.0 * n1;                   // restriction (P0 values, r) + first coarse sweep
   b += 28.0 * n0 + 20.0 * nf + 4.0 * n1;                   // prolongation
   const int nl = (int)H->lev.size();

@@ -938,10 +938,19 @@ int run_batch_step(const std::vector<hdg_system*>& sys, const hdg_solver& o, int
         HDG_CUDA(cudaStreamWaitEvent(fork.home, start, 0));
       }
     HDG_CUDA(cudaEventRecord(start, fork.home));
+    // The system with the most element work (the FP64-bound condensation of the highest degree)
+    // heads the critical path: its stream gets the greatest priority, so its element kernel is
+    // not starved of SM slots by the other systems' iteration kernels.
+    int prio_lo = 0, prio_hi = 0;
+    HDG_CUDA(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
+    size_t crit = 0;
+    auto elem_work = [&](size_t i) { return (double)sys[i]->nc * sys[i]->n * sys[i]->n * (sys[i]->m + 1); };
+    for (size_t i = 1; i < ns; ++i)
+      if (elem_work(i) > elem_work(crit)) crit = i;
     for (size_t i = 0; i < ns; ++i) {
       cudaStream_t qs;
       cudaEvent_t e;
-      HDG_CUDA(cudaStreamCreateWithFlags(&qs, cudaStreamNonBlocking));
+      HDG_CUDA(cudaStreamCreateWithPriority(&qs, cudaStreamNonBlocking, i == crit ? prio_hi : prio_lo));
       fork.streams.push_back(qs);
       HDG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
       fork.events.push_back(e);
