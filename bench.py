@@ -482,6 +482,7 @@ def run_c5(args, ws, rank, local):
     wall = time.perf_counter() - t0
     clk = clocks.stop()
     launches = ctx.launches() - launches0
+    eng.close()
     first = reqs[0]["t"]
     served = nreq / (t_last - first)
     lat_ms = sorted(1e3 * x for x in lat)

@@ -13,6 +13,8 @@
 // is by memory and slots, not by waiting for the device to drain.  Meshes registered as
 // resident keep their host topology in the engine, so a request on a resident mesh costs no mesh
 // construction.  No reference counterpart: the reference is a single-problem script.
+#include <cstdio>
+#include <cstdlib>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -90,6 +92,10 @@ struct hdg_engine {
   size_t in_use = 0;
   int64_t next_id = 1;
   bool keep_results = true;
+  // host time spent per phase (s), reported on destroy when HDG_ENGINE_VERBOSE is set
+  double t_concat = 0, t_space = 0, t_assemble = 0, t_apply = 0, t_prepare = 0, t_complete = 0, t_wait = 0;
+  double t_steps = 0;
+  int64_t n_flights = 0, n_steps = 0;
 };
 
 namespace {
@@ -120,11 +126,16 @@ Flight* launch_flight(hdg_engine* e, std::vector<Request>&& reqs, int slot) {
   std::vector<const hdg_mesh*> parts;
   for (auto& r : fl->reqs) parts.push_back(request_mesh(e, r));
   hdg_ctx* c = &fl->ctx;
+  double t0 = now_s();
   int rc = hdg_mesh_concat(c, (int)parts.size(), parts.data(), &fl->mesh);
   if (rc != HDG_OK) throw HdgError{rc, c->err};
+  double t1 = now_s();
+  e->t_concat += t1 - t0;
   const int p = fl->reqs[0].p, qd = fl->reqs[0].qd;
   rc = hdg_space_create(fl->mesh, p, qd, &fl->space);
   if (rc != HDG_OK) throw HdgError{rc, c->err};
+  t0 = now_s();
+  e->t_space += t0 - t1;
   const int np = (int)fl->reqs.size();
   std::vector<hdg_field> fs(np);
   std::vector<double> taus(np), kappa;
@@ -143,6 +154,8 @@ Flight* launch_flight(hdg_engine* e, std::vector<Request>&& reqs, int slot) {
   rc = hdg_assemble_condense_batch(fl->space, taus.data(), fs.data(), nullptr, any_kappa ? kappa.data() : nullptr,
                                    e->solver.precision, &fl->sys);
   if (rc != HDG_OK) throw HdgError{rc, c->err};
+  t1 = now_s();
+  e->t_assemble += t1 - t0;
   int cnt = 0;
   hdg_field zero{HDG_FIELD_CONST, 0, nullptr};
   rc = hdg_dirichlet(fl->space, "boundary", &zero, nullptr, nullptr, &cnt);
@@ -152,9 +165,13 @@ Flight* launch_flight(hdg_engine* e, std::vector<Request>&& reqs, int slot) {
   rc = hdg_dirichlet(fl->space, "boundary", &zero, dofs.data(), vals.data(), &cnt);
   if (rc == HDG_OK) rc = hdg_apply_dirichlet(fl->sys, dofs.data(), vals.data(), cnt);
   if (rc != HDG_OK) throw HdgError{rc, c->err};
+  t0 = now_s();
+  e->t_apply += t0 - t1;
   g_alloc_stream = c->stream;
   fl->cg = make_cg_solver(fl->sys);
   fl->cg->prepare(e->solver);
+  e->t_prepare += now_s() - t0;
+  ++e->n_flights;
   return fl.release();
 }
 
@@ -256,6 +273,15 @@ int hdg_engine_submit(hdg_engine* e, int mesh_id, const hdg_mesh* mesh, int p, i
 // One engine step: admit, advance every flight by one chunk, complete finished flights.
 int hdg_engine_step(hdg_engine* e, int* n_inflight, int* n_pending) {
   if (!e) return HDG_ERR_ARG;
+  const double ts = now_s();
+  struct StepClock {
+    hdg_engine* e;
+    double t0;
+    ~StepClock() {
+      e->t_steps += now_s() - t0;
+      ++e->n_steps;
+    }
+  } clock{e, ts};
   try {
     HDG_CUDA(cudaSetDevice(e->ctx->device));
     // 1. admission: one flight per (degree, quadrature) group of the pending queue, FIFO order
@@ -288,12 +314,16 @@ int hdg_engine_step(hdg_engine* e, int* n_inflight, int* n_pending) {
       fl->cg->enqueue_status_copy();
     }
     // 3. status, completion
+    const double tw = now_s();
     for (auto& fl : e->flights) HDG_CUDA(cudaStreamSynchronize(fl->ctx.stream));
+    e->t_wait += now_s() - tw;
     for (size_t i = 0; i < e->flights.size();) {
       Flight* fl = e->flights[i].get();
       g_alloc_stream = fl->ctx.stream;
       if (fl->cg->process(e->solver)) {
+        const double tc = now_s();
         complete_flight(e, fl);
+        e->t_complete += now_s() - tc;
         e->ctx->launches += fl->ctx.launches;
         for (size_t k = 0; k < e->streams.size(); ++k)
           if (e->streams[k] == fl->ctx.stream) e->stream_busy[k] = 0;
@@ -367,6 +397,12 @@ int hdg_engine_set_keep_results(hdg_engine* e, int keep) {
 
 int hdg_engine_destroy(hdg_engine* e) {
   if (!e) return HDG_OK;
+  if (std::getenv("HDG_ENGINE_VERBOSE"))
+    std::fprintf(stderr,
+                 "engine: %lld steps %.3f s, %lld flights; host s: concat %.3f space %.3f assemble %.3f apply %.3f "
+                 "prepare %.3f complete %.3f wait %.3f\n",
+                 (long long)e->n_steps, e->t_steps, (long long)e->n_flights, e->t_concat, e->t_space, e->t_assemble,
+                 e->t_apply, e->t_prepare, e->t_complete, e->t_wait);
   cudaSetDevice(e->ctx->device);
   for (auto& fl : e->flights) cudaStreamSynchronize(fl->ctx.stream);
   e->flights.clear();

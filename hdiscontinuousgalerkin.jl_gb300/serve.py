@@ -30,11 +30,15 @@ class Engine:
         self.inflight = 0
         self.pending = 0
 
+    def close(self):
+        """Release the engine (its flights, streams and results)."""
+        if self.h:
+            L.load().hdg_engine_destroy(self.h)
+            self.h = None
+
     def __del__(self):
         try:
-            if self.h:
-                L.load().hdg_engine_destroy(self.h)
-                self.h = None
+            self.close()
         except Exception:
             pass
 
