@@ -106,23 +106,46 @@ int aggregate(int n, const std::vector<int32_t>& ptr, const std::vector<int32_t>
 // Quotient graph of (ptr, adj) by agg: J ~ K when some member of J neighbours some member of K.
 void quotient(int n, const std::vector<int32_t>& ptr, const std::vector<int32_t>& adj, const std::vector<int32_t>& agg,
               int na, std::vector<int32_t>* qptr, std::vector<int32_t>* qadj) {
-  std::vector<std::vector<int32_t>> nb(na);
-  for (int i = 0; i < n; ++i) {
-    if (agg[i] < 0) continue;
-    for (int e = ptr[i]; e < ptr[i + 1]; ++e) {
-      const int j = adj[e];
-      if (agg[j] >= 0 && agg[j] != agg[i]) nb[agg[i]].push_back(agg[j]);
-    }
+  // members of each aggregate (counting sort keeps them in node order)
+  std::vector<int32_t> mptr(na + 1, 0), mem;
+  for (int i = 0; i < n; ++i)
+    if (agg[i] >= 0) ++mptr[agg[i] + 1];
+  for (int J = 0; J < na; ++J) mptr[J + 1] += mptr[J];
+  mem.resize(mptr[na]);
+  {
+    std::vector<int32_t> fill(mptr.begin(), mptr.end() - 1);
+    for (int i = 0; i < n; ++i)
+      if (agg[i] >= 0) mem[fill[agg[i]]++] = i;
   }
   qptr->assign(na + 1, 0);
   qadj->clear();
+  std::vector<int32_t> v;
   for (int J = 0; J < na; ++J) {
-    auto& v = nb[J];
+    v.clear();
+    for (int t = mptr[J]; t < mptr[J + 1]; ++t) {
+      const int i = mem[t];
+      for (int e = ptr[i]; e < ptr[i + 1]; ++e) {
+        const int j = adj[e];
+        if (agg[j] >= 0 && agg[j] != J) v.push_back(agg[j]);
+      }
+    }
     std::sort(v.begin(), v.end());
     v.erase(std::unique(v.begin(), v.end()), v.end());
     qadj->insert(qadj->end(), v.begin(), v.end());
     (*qptr)[J + 1] = (int32_t)qadj->size();
   }
+}
+
+// Lists of entries per key, in entry order (counting sort): key[e] in [0, nk) or < 0 (skipped).
+void bucket(int nk, const std::vector<int32_t>& key, std::vector<int32_t>* bptr, std::vector<int32_t>* bent) {
+  bptr->assign(nk + 1, 0);
+  for (size_t e = 0; e < key.size(); ++e)
+    if (key[e] >= 0) ++(*bptr)[key[e] + 1];
+  for (int k = 0; k < nk; ++k) (*bptr)[k + 1] += (*bptr)[k];
+  bent->resize((*bptr)[nk]);
+  std::vector<int32_t> fill(bptr->begin(), bptr->end() - 1);
+  for (size_t e = 0; e < key.size(); ++e)
+    if (key[e] >= 0) (*bent)[fill[key[e]]++] = (int32_t)e;
 }
 
 // Device copy of a host array that may be empty (a one-element buffer is kept so that kernels get
@@ -235,52 +258,54 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
   std::vector<int32_t> bcol5((size_t)5 * nf);
   s->d_bcol5.download(bcol5.data(), bcol5.size(), st);
   HDG_CUDA(cudaStreamSynchronize(st));
-  std::vector<std::vector<int32_t>> apc(nf);
+  // (at most 5 slots x PW columns = 25 entries per face, kept in a fixed-width table)
+  constexpr int APW = 5 * PW;
+  std::vector<int32_t> apc((size_t)nf * APW);
+  std::vector<uint8_t> apn(nf);
   int wap = 1;
   for (int f = 0; f < nf; ++f) {
-    auto& v = apc[f];
+    int32_t* v = &apc[(size_t)f * APW];
+    int n = 0;
     for (int k = 0; k < 5; ++k) {
       const int g = bcol5[(size_t)k * nf + f];
       for (int c = 0; c < PW; ++c)
-        if (pcol0[(size_t)g * PW + c] >= 0) v.push_back(pcol0[(size_t)g * PW + c]);
+        if (pcol0[(size_t)g * PW + c] >= 0) v[n++] = pcol0[(size_t)g * PW + c];
     }
-    std::sort(v.begin(), v.end());
-    v.erase(std::unique(v.begin(), v.end()), v.end());
-    wap = std::max(wap, (int)v.size());
+    std::sort(v, v + n);
+    n = (int)(std::unique(v, v + n) - v);
+    apn[f] = (uint8_t)n;
+    wap = std::max(wap, n);
   }
   if (wap > 32) throw HdgError{HDG_ERR_ARG, "AMG: prolongator pattern wider than 32 (invalid trace mesh)"};
   std::vector<int32_t> apcol0((size_t)nf * wap, -1);
   std::vector<int8_t> apmap0((size_t)nf * 5 * PW, -1);
   for (int f = 0; f < nf; ++f) {
-    const auto& v = apc[f];
-    std::copy(v.begin(), v.end(), apcol0.begin() + (size_t)f * wap);
+    const int32_t* v = &apc[(size_t)f * APW];
+    const int n = apn[f];
+    std::copy(v, v + n, apcol0.begin() + (size_t)f * wap);
     for (int k = 0; k < 5; ++k) {
       const int g = bcol5[(size_t)k * nf + f];
       for (int c = 0; c < PW; ++c) {
         const int J = pcol0[(size_t)g * PW + c];
         if (J < 0) continue;
-        apmap0[((size_t)f * 5 + k) * PW + c] = (int8_t)(std::lower_bound(v.begin(), v.end(), J) - v.begin());
+        apmap0[((size_t)f * 5 + k) * PW + c] = (int8_t)(std::lower_bound(v, v + n, J) - v);
       }
     }
   }
   // P0' lists and the level-1 pattern (rows = aggregates)
-  std::vector<std::vector<int32_t>> rl(na0);
-  for (int f = 0; f < nf; ++f)
-    for (int c = 0; c < PW; ++c)
-      if (pcol0[(size_t)f * PW + c] >= 0) rl[pcol0[(size_t)f * PW + c]].push_back(f * PW + c);
-  std::vector<int32_t> rptr0(na0 + 1, 0), rent0;
+  std::vector<int32_t> rptr0, rent0;  // entries f * PW + c of P0 per column, in entry order
+  bucket(na0, pcol0, &rptr0, &rent0);
   AmgLevel L1;
   L1.n = na0;
   L1.h_ptr.assign(na0 + 1, 0);
   L1.h_prob.assign(na0, 0);
   L1.h_B.assign(na0, 0.0);
+  std::vector<int32_t> cols;
   for (int J = 0; J < na0; ++J) {
-    rent0.insert(rent0.end(), rl[J].begin(), rl[J].end());
-    rptr0[J + 1] = (int32_t)rent0.size();
-    std::vector<int32_t> cols;
-    for (int e : rl[J]) {
-      const auto& v = apc[e / PW];
-      cols.insert(cols.end(), v.begin(), v.end());
+    cols.clear();
+    for (int t = rptr0[J]; t < rptr0[J + 1]; ++t) {
+      const int f = rent0[t] / PW;
+      cols.insert(cols.end(), &apc[(size_t)f * APW], &apc[(size_t)f * APW] + apn[f]);
     }
     std::sort(cols.begin(), cols.end());
     cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
@@ -333,9 +358,9 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
     std::vector<float> tent(n);
     for (int i = 0; i < n; ++i) tent[i] = nrm[agg[i]] > 0 ? (float)(F.h_B[i] / nrm[agg[i]]) : 0.f;
     // P pattern row i: aggregates of the columns of A row i
-    std::vector<int32_t> pptr(n + 1, 0), pcol;
+    std::vector<int32_t> pptr(n + 1, 0), pcol, v;
     for (int i = 0; i < n; ++i) {
-      std::vector<int32_t> v;
+      v.clear();
       for (int e = F.h_ptr[i]; e < F.h_ptr[i + 1]; ++e) v.push_back(agg[F.h_col[e]]);
       std::sort(v.begin(), v.end());
       v.erase(std::unique(v.begin(), v.end()), v.end());
@@ -345,7 +370,7 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
     // A P pattern row i: union of the P rows of A row i's columns
     std::vector<int32_t> apptr(n + 1, 0), apcol;
     for (int i = 0; i < n; ++i) {
-      std::vector<int32_t> v;
+      v.clear();
       for (int e = F.h_ptr[i]; e < F.h_ptr[i + 1]; ++e) {
         const int k = F.h_col[e];
         v.insert(v.end(), pcol.begin() + pptr[k], pcol.begin() + pptr[k + 1]);
@@ -356,27 +381,24 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
       apptr[i + 1] = (int32_t)apcol.size();
     }
     // P' lists and the next level's pattern
-    std::vector<std::vector<int32_t>> r(na);
-    for (int i = 0; i < n; ++i)
-      for (int e = pptr[i]; e < pptr[i + 1]; ++e) r[pcol[e]].push_back(e);
     std::vector<int32_t> prow_of(pcol.size());
     for (int i = 0; i < n; ++i)
       for (int e = pptr[i]; e < pptr[i + 1]; ++e) prow_of[e] = i;
-    std::vector<int32_t> rptr(na + 1, 0), rent, rrow;
+    std::vector<int32_t> rptr, rent, rrow;  // entries of P per column, in entry order
+    bucket(na, pcol, &rptr, &rent);
+    rrow.resize(rent.size());
+    for (size_t t = 0; t < rent.size(); ++t) rrow[t] = prow_of[rent[t]];
     AmgLevel C;
     C.n = na;
     C.h_ptr.assign(na + 1, 0);
     C.h_prob.assign(na, 0);
     C.h_B = nrm;
     for (int J = 0; J < na; ++J) {
-      std::vector<int32_t> cols;
-      for (int e : r[J]) {
-        rent.push_back(e);
-        rrow.push_back(prow_of[e]);
-        const int i = prow_of[e];
+      cols.clear();
+      for (int t = rptr[J]; t < rptr[J + 1]; ++t) {
+        const int i = rrow[t];
         cols.insert(cols.end(), apcol.begin() + apptr[i], apcol.begin() + apptr[i + 1]);
       }
-      rptr[J + 1] = (int32_t)rent.size();
       std::sort(cols.begin(), cols.end());
       cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
       C.h_col.insert(C.h_col.end(), cols.begin(), cols.end());

@@ -5,10 +5,11 @@
 //   1. admits pending requests into new "flights" while the HBM budget allows: the requests of one
 //      degree form a disjoint union mesh with one space and one trace system, assembled,
 //      condensed and gathered by the same launches as a batch;
-//   2. enqueues one chunk of CG iterations for every flight in progress, each flight on its own
-//      CUDA stream so that flights overlap on the device;
-//   3. reads the flights' per-problem status and completes the flights whose problems are all done
-//      (recovery, result copy, latency stamp), freeing their memory for the next admissions.
+//   2. processes every flight whose last chunk of CG iterations has finished (its per-problem
+//      status read back): a flight whose problems are all done is completed (recovery, result
+//      copy, latency stamp) and its memory freed for the next admissions; any other is given its
+//      next chunk at once.  Each flight runs on its own CUDA stream, so flights overlap on the
+//      device and none waits for another.
 // So requests that arrive while others are on the GPU join at the next chunk boundary: admission
 // is by memory and slots, not by waiting for the device to drain.  Meshes registered as
 // resident keep their host topology in the engine, so a request on a resident mesh costs no mesh
@@ -20,6 +21,7 @@
 #include <cstring>
 #include <deque>
 #include <memory>
+#include <thread>
 #include <unordered_map>
 
 #include "hdg_internal.h"
@@ -68,7 +70,9 @@ struct Flight {
   CgSolver* cg = nullptr;
   int rep = 0;
   size_t bytes = 0;
+  cudaEvent_t ready = nullptr;  // recorded after each chunk's status read-back
   ~Flight() {
+    if (ready) cudaEventDestroy(ready);
     delete cg;
     if (sys) hdg_system_destroy(sys);
     if (space) hdg_space_destroy(space);
@@ -170,6 +174,7 @@ Flight* launch_flight(hdg_engine* e, std::vector<Request>&& reqs, int slot) {
   g_alloc_stream = c->stream;
   fl->cg = make_cg_solver(fl->sys);
   fl->cg->prepare(e->solver);
+  HDG_CUDA(cudaEventCreateWithFlags(&fl->ready, cudaEventDisableTiming));
   e->t_prepare += now_s() - t0;
   ++e->n_flights;
   return fl.release();
@@ -307,32 +312,46 @@ int hdg_engine_step(hdg_engine* e, int* n_inflight, int* n_pending) {
       e->in_use += bytes;
       e->flights.emplace_back(fl);
     }
-    // 2. one chunk for every flight, each on its own stream
-    for (auto& fl : e->flights) {
-      g_alloc_stream = fl->ctx.stream;
-      fl->cg->launch_chunk(fl->rep++);
-      fl->cg->enqueue_status_copy();
-    }
-    // 3. status, completion
+    // 2. every flight whose last status read-back has landed is processed at once: completed, or
+    //    given its next chunk.  Flights still iterating are left alone, so no flight waits for
+    //    another.  When none is ready the step polls for up to 0.2 ms before returning, so that
+    //    the caller can admit new arrivals.
     const double tw = now_s();
-    for (auto& fl : e->flights) HDG_CUDA(cudaStreamSynchronize(fl->ctx.stream));
-    e->t_wait += now_s() - tw;
-    for (size_t i = 0; i < e->flights.size();) {
-      Flight* fl = e->flights[i].get();
-      g_alloc_stream = fl->ctx.stream;
-      if (fl->cg->process(e->solver)) {
-        const double tc = now_s();
-        complete_flight(e, fl);
-        e->t_complete += now_s() - tc;
-        e->ctx->launches += fl->ctx.launches;
-        for (size_t k = 0; k < e->streams.size(); ++k)
-          if (e->streams[k] == fl->ctx.stream) e->stream_busy[k] = 0;
-        e->in_use -= fl->bytes;
-        e->flights.erase(e->flights.begin() + i);
-      } else {
+    bool progressed = false;
+    for (int spin = 0;; ++spin) {
+      for (size_t i = 0; i < e->flights.size();) {
+        Flight* fl = e->flights[i].get();
+        g_alloc_stream = fl->ctx.stream;
+        if (fl->rep > 0) {  // a chunk is queued: has its read-back landed?
+          const cudaError_t q = cudaEventQuery(fl->ready);
+          if (q == cudaErrorNotReady) {
+            ++i;
+            continue;
+          }
+          HDG_CUDA(q);
+          progressed = true;
+          if (fl->cg->process(e->solver)) {
+            const double tc = now_s();
+            complete_flight(e, fl);
+            e->t_complete += now_s() - tc;
+            e->ctx->launches += fl->ctx.launches;
+            for (size_t k = 0; k < e->streams.size(); ++k)
+              if (e->streams[k] == fl->ctx.stream) e->stream_busy[k] = 0;
+            e->in_use -= fl->bytes;
+            e->flights.erase(e->flights.begin() + i);
+            continue;
+          }
+        }
+        progressed = true;
+        fl->cg->launch_chunk(fl->rep++);
+        fl->cg->enqueue_status_copy();
+        HDG_CUDA(cudaEventRecord(fl->ready, fl->ctx.stream));
         ++i;
       }
+      if (progressed || e->flights.empty() || now_s() - tw > 2e-4) break;
+      std::this_thread::yield();
     }
+    if (!progressed) e->t_wait += now_s() - tw;
     if (n_inflight) {
       int n = 0;
       for (auto& fl : e->flights) n += (int)fl->reqs.size();
