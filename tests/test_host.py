@@ -212,3 +212,27 @@ def test_unstructured_figure1_reader_matches_oracle(H, oracle):
     assert sorted(H.getfaceset(m, "boundary")) == sorted(om.faceset("boundary").tolist())
     for c in range(m.ncells):
         assert [H.face_orientation(m, c + 1, f + 1) for f in range(3)] == [om.orientation(c, f) for f in range(3)]
+
+
+def test_write_vtk_roundtrip(H, tmp_path):
+    """The headless output that stands in for the reference's Makie plot: a legacy VTK file whose
+    points, triangles and fields read back as written."""
+    m = H.rectangle_mesh(H.TriangleCell, (3, 2), (0.0, 0.0), (1.0, 1.0), ctx=None)
+    xy, cn = m._topology()[0], m._topology()[1]
+    u = xy[:, 0] * 2.0 + xy[:, 1]
+    q = np.stack([xy[:, 1], -xy[:, 0]], axis=1)
+    k = np.arange(cn.shape[0], dtype=float)
+    path = tmp_path / "u.vtk"
+    H.write_vtk(str(path), m, point_data={"u": u, "q": q}, cell_data={"kappa": k})
+    lines = path.read_text().splitlines()
+    i = lines.index(f"POINTS {xy.shape[0]} double")
+    pts = np.array([[float(t) for t in ln.split()] for ln in lines[i + 1:i + 1 + xy.shape[0]]])
+    assert np.array_equal(pts[:, :2], xy) and not pts[:, 2].any()
+    i = lines.index(f"CELLS {cn.shape[0]} {4 * cn.shape[0]}")
+    cells = np.array([[int(t) for t in ln.split()] for ln in lines[i + 1:i + 1 + cn.shape[0]]])
+    assert (cells[:, 0] == 3).all() and np.array_equal(cells[:, 1:] + 1, cn)
+    i = lines.index("SCALARS u double 1")
+    assert np.array_equal(np.array([float(t) for t in lines[i + 2:i + 2 + xy.shape[0]]]), u)
+    i = lines.index("SCALARS kappa double 1")
+    assert np.array_equal(np.array([float(t) for t in lines[i + 2:i + 2 + cn.shape[0]]]), k)
+    assert "VECTORS q double" in lines
