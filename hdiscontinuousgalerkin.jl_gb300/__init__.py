@@ -10,6 +10,7 @@ from ._lib import HDGError, PREC_FP64, PREC_MIXED, PRECOND_AMG, PRECOND_JACOBI
 from .batch import Batch, Problem, concat_meshes, problem_offsets
 from .serve import Engine
 from .vtk import write_vtk
+from .lagrange import LagrangeSystem, doassemble_cg, reconstruct_
 from .assembler import Assembler, SparseMatrixCSC, assemble_, end_assemble, start_assemble
 from .context import Context, default_context
 from .fields import MANUFACTURED_F, MANUFACTURED_U, Field

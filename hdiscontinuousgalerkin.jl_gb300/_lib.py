@@ -107,6 +107,13 @@ SIGNATURES = {
     "hdg_system_set_dirichlet": ([vp, i32p, dp, ip], ip),
     "hdg_batch_step": ([ip, C.POINTER(vp), C.POINTER(hdg_solver), ip, C.POINTER(hdg_stats)], ip),
     "hdg_host_alloc": ([C.c_size_t, C.POINTER(vp)], ip),
+    "hdg_lagrange_create": ([vp, vp, ip, ip, ip, i32p, C.c_int64, i64p, i64p, C.POINTER(vp)], ip),
+    "hdg_lagrange_assemble": ([vp, C.POINTER(hdg_field), dp], ip),
+    "hdg_lagrange_get_csc": ([vp, dp, dp], ip),
+    "hdg_lagrange_apply_dirichlet": ([vp, i32p, dp, ip], ip),
+    "hdg_lagrange_solve": ([vp, C.POINTER(hdg_solver), dp, C.POINTER(hdg_stats)], ip),
+    "hdg_lagrange_errornorm_l2sq": ([vp, dp, C.POINTER(hdg_field), C.POINTER(C.c_double)], ip),
+    "hdg_lagrange_destroy": ([vp], ip),
     "hdg_host_free": ([vp], ip),
     "hdg_system_set_download": ([vp, dp, dp], ip),
     "hdg_system_get_solution": ([vp, dp, dp], ip),

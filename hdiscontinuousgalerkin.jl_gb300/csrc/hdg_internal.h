@@ -11,6 +11,7 @@
 #include "../../include/hdg.h"
 
 #define HDG_MAX_P 4
+#define HDG_LAGRANGE_MAX_NL 15  // nodal basis functions of the highest Lagrange order (4)
 
 // ------------------------------------------------------------------ errors
 struct HdgError {
@@ -193,6 +194,15 @@ struct RefTables {
   std::vector<double> packed;
 };
 bool build_ref_tables(int p, int qd, RefTables* t);
+
+// Nodal (continuous Lagrange) basis of order k on the reference triangle, at the volume points of
+// QuadratureRule{2}(qd): nodes in the order of get_nodal_points (vertices, edge points, interior
+// points); values N [nl][nq] and reference gradients dN [nl][nq][2].
+struct LagrangeTables {
+  int order = 0, nl = 0, nq = 0;
+  std::vector<double> qx, qy, qw, N, dN;
+};
+bool build_lagrange_tables(int order, int qd, LagrangeTables* t);
 
 // Offsets of the packed table, in doubles.
 struct RefLayout {

@@ -393,6 +393,79 @@ bool build_ref_tables(int p, int qd, RefTables* t) {
   return true;
 }
 
+// ------------------------------------------------------------------ continuous Lagrange
+// ContinuousLagrange{2,RefTetrahedron,k} (src/LagrangeFE.jl:17-39): the nodal basis is the dual
+// of the Dubiner basis at the nodal points, phi_k = sum_j C[j][k] D_j with C = V^-1 and
+// V[i][j] = D_j(node_i).  Nodal points as get_nodal_points (src/shapes.jl:46-77): the vertices
+// (0,0), (1,0), (0,1); the k-1 interior points of the edges (1,0)->(0,1), (0,1)->(0,0),
+// (0,0)->(1,0); then the interior grid (j/k, i/k).
+bool build_lagrange_tables(int order, int qd, LagrangeTables* t) {
+  if (order < 1 || order > HDG_MAX_P) return false;
+  RefTables r;
+  if (!build_ref_tables(order, qd, &r)) return false;  // the rule and the Dubiner tables
+  const int k = order, nl = (k + 1) * (k + 2) / 2, nq = r.nq;
+  std::vector<double> px, py;
+  const double V0[3][2] = {{0, 0}, {1, 0}, {0, 1}};
+  const double ED[3][4] = {{1, 0, 0, 1}, {0, 1, 0, 0}, {0, 0, 1, 0}};
+  for (int v = 0; v < 3; ++v) { px.push_back(V0[v][0]); py.push_back(V0[v][1]); }
+  for (int e = 0; e < 3; ++e)
+    for (int i = 1; i < k; ++i) {
+      px.push_back(ED[e][0] + i * (ED[e][2] - ED[e][0]) / k);
+      py.push_back(ED[e][1] + i * (ED[e][3] - ED[e][1]) / k);
+    }
+  for (int i = 1; i < k; ++i)
+    for (int j = 1; j < k - i; ++j) { px.push_back((double)j / k); py.push_back((double)i / k); }
+  if ((int)px.size() != nl) return false;
+  // [V | I] -> [I | V^-1] by Gauss-Jordan with partial pivoting in long double
+  std::vector<long double> a((size_t)nl * 2 * nl, 0.0L);
+  for (int i = 0; i < nl; ++i) {
+    for (int j = 0; j < nl; ++j) {
+      int n, m;
+      dubiner_index(j + 1, &n, &m);
+      a[(size_t)i * 2 * nl + j] = dubiner_nm(Dd{px[i], 0, 0}, Dd{py[i], 0, 0}, n, m).v;
+    }
+    a[(size_t)i * 2 * nl + nl + i] = 1.0L;
+  }
+  for (int c = 0; c < nl; ++c) {
+    int piv = c;
+    for (int i = c + 1; i < nl; ++i)
+      if (std::fabs(a[(size_t)i * 2 * nl + c]) > std::fabs(a[(size_t)piv * 2 * nl + c])) piv = i;
+    if (a[(size_t)piv * 2 * nl + c] == 0.0L) return false;
+    if (piv != c)
+      for (int j = 0; j < 2 * nl; ++j) std::swap(a[(size_t)c * 2 * nl + j], a[(size_t)piv * 2 * nl + j]);
+    const long double d = a[(size_t)c * 2 * nl + c];
+    for (int j = 0; j < 2 * nl; ++j) a[(size_t)c * 2 * nl + j] /= d;
+    for (int i = 0; i < nl; ++i) {
+      if (i == c) continue;
+      const long double f = a[(size_t)i * 2 * nl + c];
+      if (f != 0.0L)
+        for (int j = 0; j < 2 * nl; ++j) a[(size_t)i * 2 * nl + j] -= f * a[(size_t)c * 2 * nl + j];
+    }
+  }
+  t->order = k;
+  t->nl = nl;
+  t->nq = nq;
+  t->qx = r.qx;
+  t->qy = r.qy;
+  t->qw = r.qw;
+  t->N.assign((size_t)nl * nq, 0.0);
+  t->dN.assign((size_t)nl * nq * 2, 0.0);
+  for (int kk = 0; kk < nl; ++kk)
+    for (int q = 0; q < nq; ++q) {
+      long double v = 0, gx = 0, gy = 0;
+      for (int j = 0; j < nl; ++j) {
+        const long double cjk = a[(size_t)j * 2 * nl + nl + kk];  // (V^-1)[j][kk]
+        v += cjk * r.N[(size_t)j * nq + q];
+        gx += cjk * r.dN[((size_t)j * nq + q) * 2];
+        gy += cjk * r.dN[((size_t)j * nq + q) * 2 + 1];
+      }
+      t->N[(size_t)kk * nq + q] = (double)v;
+      t->dN[((size_t)kk * nq + q) * 2] = (double)gx;
+      t->dN[((size_t)kk * nq + q) * 2 + 1] = (double)gy;
+    }
+  return true;
+}
+
 // ------------------------------------------------------------------ fields (host side)
 FieldSpec field_from(const hdg_field* f, double default_const) {
   FieldSpec s;

@@ -205,15 +205,22 @@ class Dirichlet:
                                        L.dptr(self.values), C.byref(n)), mesh.ctx)
 
 
-def apply_(K: TraceSystem, b, dbc: Dirichlet):
-    """apply!(K, b, dbc) (src/boundary.jl:326-363) on the device system."""
+def apply_(K, b, dbc: Dirichlet):
+    """apply!(K, b, dbc) (src/boundary.jl:121-158, :326-363) on the device system: the HDG
+    TraceSystem of doassemble or the LagrangeSystem of doassemble_cg (b is refreshed in place)."""
+    from .lagrange import LagrangeSystem
+    if isinstance(K, LagrangeSystem):
+        K.apply_dirichlet(dbc.prescribed_dofs, dbc.values)
+        if b is not None and b is not K.b:
+            b[:] = K.b
+        return
     if not isinstance(K, TraceSystem):
-        raise TypeError("apply_ works on the TraceSystem returned by doassemble")
+        raise TypeError("apply_ works on the system returned by doassemble or doassemble_cg")
     K.apply_dirichlet(dbc.prescribed_dofs, dbc.values)
 
 
-def solve(K: TraceSystem, b=None, **opts) -> np.ndarray:
-    """û = K \\ b (examples/poisson2D_HDG.jl:195): Jacobi-PCG on the device."""
+def solve(K, b=None, **opts) -> np.ndarray:
+    """û = K \\ b (examples/poisson2D_HDG.jl:195, poisson2D_CG.jl:126): PCG on the device."""
     return K.solve(**opts)
 
 
@@ -259,7 +266,10 @@ def errornorm(u_h: TrialFunction, u_ex, norm_type: str = "L2") -> float:
     if norm_type != "L2":
         raise ValueError(f"Norm {norm_type} not available")
     if u_h.system is None:
-        raise ValueError("u_h has no recovered values (call get_usigma_ first)")
+        raise ValueError("u_h has no recovered values (call get_usigma_ or reconstruct_ first)")
+    from .lagrange import LagrangeSystem
+    if isinstance(u_h.system, LagrangeSystem):
+        return u_h.system.errornorm(u_h.dof_values, u_ex)
     return u_h.system.errornorm(u_ex)
 
 

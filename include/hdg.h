@@ -276,6 +276,34 @@ int hdg_batch_step(int nsys, hdg_system* const* systems, const hdg_solver* opts,
 /* Device solution of a system: trace values (ndofs) and, after recovery, [q; u] per cell (ncells x n). */
 int hdg_system_get_solution(const hdg_system* sys, double* uhat, double* qu);
 
+/* ---- continuous Galerkin (nodal Lagrange) Poisson path --------------------------------- */
+/* examples/poisson2D_CG.jl / test/test_CGExample.jl on the device: -div(kappa grad u) = f with a
+ * nodal ContinuousLagrange{2,RefTetrahedron,order} element (order 1..4, P1 geometry) whose dofs a
+ * DofHandler numbered.  The system is assembled straight into the caller's CSC pattern (the one
+ * create_sparsity_pattern returns), so K and b are those of start_assemble(K, f) + assemble! in
+ * the reference's element loop (src/assembler.jl:62-137). */
+typedef struct hdg_lagrange hdg_lagrange;
+/* mesh on the device (ctx); cell_dofs: ncells x nbasefuncs, 1-based, as DofHandler.cell_dofs of a
+ * one-field handler; colptr (ndofs+1) / rowval (nnz): 0-based CSC pattern with every element
+ * coupling stored (else HDG_ERR_ARG).  quad_degree <= 0: order + 1 (the reference default). */
+int hdg_lagrange_create(hdg_ctx* ctx, const hdg_mesh* mesh, int order, int quad_degree, int ndofs,
+                        const int32_t* cell_dofs, int64_t nnz, const int64_t* colptr, const int64_t* rowval,
+                        hdg_lagrange** out);
+/* doassemble: K = sum_cells int kappa grad v . grad u, b = sum_cells int f v (kappa_cell may be
+ * NULL: kappa = 1); HDG_ERR_NEG_DETJ for an inverted cell. */
+int hdg_lagrange_assemble(hdg_lagrange* sys, const hdg_field* f, const double* kappa_cell);
+/* K's stored values (nnz, in the pattern's order) and b (ndofs); either may be NULL. */
+int hdg_lagrange_get_csc(hdg_lagrange* sys, double* nzval, double* rhs);
+/* apply!(K, b, dbc), src/boundary.jl:121-158: dofs 1-based (sorted, as Dirichlet returns them). */
+int hdg_lagrange_apply_dirichlet(hdg_lagrange* sys, const int32_t* dofs, const double* vals, int n);
+/* u = K \ b by Jacobi-preconditioned CG in FP64 to opts->tol (relative residual); u (ndofs) may
+ * be NULL (the solution stays on the device for hdg_lagrange_errornorm_l2sq). */
+int hdg_lagrange_solve(hdg_lagrange* sys, const hdg_solver* opts, double* u, hdg_stats* stats);
+/* errornorm(u_h, u_exact) (squared L2, src/DiscreteFunctions.jl:97-120) of the dof values u
+ * (ndofs; NULL: the last solution). */
+int hdg_lagrange_errornorm_l2sq(hdg_lagrange* sys, const double* u, const hdg_field* u_exact, double* out);
+int hdg_lagrange_destroy(hdg_lagrange* sys);
+
 /* ---- serving: continuous batching of solve requests ----------------------------------- */
 /* No reference counterpart.  Requests queue on the host; every hdg_engine_step admits pending
  * requests into "flights" (one disjoint union system per degree, at most max_batch requests)

@@ -404,3 +404,49 @@ def test_nodal_avg(H, oracle):
     assert rel(got, acc / cnt) < 1e-12
     exact = np.sin(np.pi * xy[:, 0]) * np.sin(np.pi * xy[:, 1])
     assert np.max(np.abs(got - exact)) < 2e-3
+
+
+@pytest.mark.parametrize("n,order,var", [(10, 1, False), (12, 2, False), (9, 1, True), (7, 2, True)])
+def test_cg_poisson_path_matches_oracle(H, oracle, n, order, var):
+    """examples/poisson2D_CG.jl on the device: the stiffness values and load assembled into the
+    DofHandler's pattern, the system after apply!, the PCG solution and errornorm equal the CG
+    oracle's (jittered mesh and per-cell kappa in the variable cases); the 10 x 10 P1 example
+    meets the reference's bound errornorm <= 2e-4 (test/test_CGExample.jl:92-93)."""
+    import cgref
+    rng = np.random.default_rng(n * 3 + order)
+    mesh = H.rectangle_mesh(H.TriangleCell, (n, n), (0.0, 0.0), (1.0, 1.0))
+    om = oracle.rectangle_mesh(n, n)
+    kc = None
+    if var:
+        pr = H.Problem(n=n, p=order, f=H.MANUFACTURED_F, jitter=0.2, seed=17)
+        xy = H.batch.host_mesh(pr)._topology()[0]
+        mesh.set_coordinates(xy)
+        om.set_xy(xy)
+        kc = np.exp(rng.uniform(np.log(1e-2), np.log(1e2), 2 * n * n))
+    Wh = H.ScalarFunctionSpace(mesh, H.ContinuousLagrange(2, H.RefTetrahedron, order), update_face_data=False)
+    u_h = H.TrialFunction(Wh)
+    dh = H.DofHandler([u_h], mesh)
+    K0 = H.create_sparsity_pattern(dh)
+    dbc = H.Dirichlet(u_h, dh, "boundary", lambda x: 0.0)
+    K, b = H.doassemble_cg(Wh, K0, dh, H.MANUFACTURED_F, kappa_cell=kc)
+    Kref, bref, cd = cgref.assemble(om, order, oracle.MANUFACTURED_F, kappa_cell=kc)
+    assert np.array_equal(dh.cell_dofs.reshape(cd.shape), cd)
+    Kd = K.csc()
+    scale = abs(Kref).max()
+    assert abs(Kd - Kref).max() <= 1e-13 * scale
+    assert np.abs(b - bref).max() <= 1e-13 * np.abs(bref).max()
+    H.apply_(K, b, dbc)
+    Ka, ba = cgref.apply_dirichlet(Kref, bref, dbc.prescribed_dofs, dbc.values)
+    assert abs(K.csc() - Ka).max() <= 1e-13 * scale
+    assert np.abs(b - ba).max() <= 1e-13 * np.abs(ba).max()
+    u = H.solve(K, b, tol=1e-13)
+    assert K.stats.converged
+    uref = cgref.spla.spsolve(Ka.tocsc(), ba)
+    assert rel(u, uref) < 1e-10
+    H.reconstruct_(u_h, u, dh)
+    assert np.array_equal(u_h.m_values, u[cd - 1])
+    err = H.errornorm(u_h, H.MANUFACTURED_U)
+    eref = cgref.errornorm(om, order, uref, oracle.MANUFACTURED_U, cd)
+    assert abs(err - eref) <= 1e-8 * eref
+    if (n, order, var) == (10, 1, False):
+        assert err <= 2e-4

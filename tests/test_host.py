@@ -236,3 +236,33 @@ def test_write_vtk_roundtrip(H, tmp_path):
     i = lines.index("SCALARS kappa double 1")
     assert np.array_equal(np.array([float(t) for t in lines[i + 2:i + 2 + cn.shape[0]]]), k)
     assert "VECTORS q double" in lines
+
+
+def test_cg_oracle_pinned_by_reference_bound(oracle):
+    """The CG Poisson oracle reproduces the reference's own bound on its 10 x 10 P1 example
+    (test/test_CGExample.jl:92-93: squared L2 error <= 2e-4), and P2 converges further."""
+    import cgref
+    m = oracle.rectangle_mesh(10, 10)
+    r1 = cgref.solve_poisson_cg(m, 1)
+    assert r1["err"] <= 2e-4
+    r2 = cgref.solve_poisson_cg(m, 2)
+    assert r2["err"] < r1["err"] / 100
+    # nodal basis: a partition of unity with Kronecker values at the nodes
+    P = cgref.nodal_points(2)
+    N, _ = cgref.lagrange_tables(2, P[:, 0], P[:, 1])
+    assert np.allclose(N, np.eye(6), atol=1e-14)
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_dofhandler_and_dirichlet_match_cg_oracle(H, oracle, order):
+    """The library's DofHandler numbering and Dirichlet dofs equal the CG oracle's restatement of
+    src/dofhandler.jl and src/boundary.jl:44-95 on a 6 x 5 mesh."""
+    import cgref
+    m = H.rectangle_mesh(H.TriangleCell, (6, 5), (0.0, 0.0), (1.0, 1.0), ctx=None)
+    u = H.TrialFunction(H.ScalarFunctionSpace(m, H.ContinuousLagrange(2, H.RefTetrahedron, order)))
+    dh = H.DofHandler([u], m)
+    om = oracle.rectangle_mesh(6, 5)
+    cd = cgref.distribute_dofs(om, order)
+    assert np.array_equal(dh.cell_dofs.reshape(cd.shape), cd)
+    dbc = H.Dirichlet(u, dh, "boundary", lambda x: 0.0)
+    assert np.array_equal(dbc.prescribed_dofs, cgref.boundary_dofs(om, cd, order))
