@@ -537,13 +537,124 @@ def run_c5(args, ws, rank, local):
         print(json.dumps(line), flush=True)
 
 
+CG_DESC = ("cg: examples/poisson2D_CG.jl scaled: -div grad u = 2 pi^2 sin(pi x) sin(pi y) on 2*n*n triangles, "
+           "nodal ContinuousLagrange of order p, DofHandler numbering, homogeneous Dirichlet, Jacobi-PCG to 1e-12")
+
+
+def run_cg(args, ws, rank, local):
+    """The continuous-Galerkin Poisson path (the survey's next row): element loop and assemble!
+    into the DofHandler's CSC pattern, apply!, Jacobi-PCG and errornorm, on the device."""
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as g
+    g.build()
+    H = g.import_package()
+    torch.cuda.set_device(local)
+    ctx = H.Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    n = args.n or 256
+    order = args.p or 2
+    mesh = H.rectangle_mesh(H.TriangleCell, (n, n), (0.0, 0.0), (1.0, 1.0), ctx=ctx)
+    Wh = H.ScalarFunctionSpace(mesh, H.ContinuousLagrange(2, H.RefTetrahedron, order), update_face_data=False)
+    u_h = H.TrialFunction(Wh)
+    dh = H.DofHandler([u_h], mesh)
+    K0 = H.create_sparsity_pattern(dh)
+    dbc = H.Dirichlet(u_h, dh, "boundary", lambda x: 0.0)
+    K = H.LagrangeSystem(Wh, K0, dh)
+    dh._lagrange_system = K
+    tol = args.tol
+
+    def step():
+        t = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        t[0].record(stream)
+        K.assemble(H.MANUFACTURED_F)                         # element loop + assemble!
+        t[1].record(stream)
+        K.apply_dirichlet(dbc.prescribed_dofs, dbc.values)   # apply!
+        t[2].record(stream)
+        u = K.solve(tol=tol)                                 # K \ b, u to the host
+        t[3].record(stream)
+        return u, t
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = ctx.launches()
+    barrier(ws)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    phases = []
+    for _ in range(args.steps):
+        u, t = step()
+        phases.append(t)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(ws)
+    launches = ctx.launches() - launches0
+    clk = clocks.stop()
+    ms = max_over_ranks(e0.elapsed_time(e1), ws) / args.steps
+    value = ws * 1e3 / ms
+    asm_ms = statistics.mean(a.elapsed_time(b) for a, b, _, _ in phases)
+    apply_ms = statistics.mean(b.elapsed_time(c) for _, b, c, _ in phases)
+    solve_ms = statistics.mean(c.elapsed_time(d) for _, _, c, d in phases)
+    its = K.stats.iterations
+    H.reconstruct_(u_h, u, dh)
+    err = H.errornorm(u_h, H.MANUFACTURED_U)
+    # roofline of the PCG (two kernels per iteration): the CSC values and row indices, the column
+    # pointers, and the vectors (z, p_old gathered; p_new, q written; x, r read and written; z
+    # written; D^-1 read) once each
+    nd, nnz = K.ndofs, K.nnz
+    it_bytes = nnz * (8 + 4) + (nd + 1) * 4 + nd * 8 * (2 + 2 + 4 + 1 + 1)
+    peaks, peak_kind = measured_peaks()
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = it_bytes * its / (solve_ms / 1e3) / 1e9 if solve_ms > 0 else None
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": CG_DESC, "n": n, "order": order, "cells": mesh.ncells, "dofs": nd, "nnz": nnz,
+                   "tol": tol, "step": "assemble (element loop + assemble!) -> apply! -> PCG -> u to the host",
+                   "parallelism": f"{ws} independent replica(s), one per GPU"},
+        "cg_iterations": its, "errornorm_sq": err,
+        "phase_ms": {"assemble_ms": asm_ms, "apply_ms": apply_ms, "solve_ms": solve_ms},
+        "gpu_launches": launches,
+        "roofline": {"kernel": "k_lag_cg_a + k_lag_cg_b (one PCG iteration)", "bound": "hbm", "achieved": achieved,
+                     "peak": hbm, "unit": "GB/s", "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                     "algorithmic_bytes_per_iteration": it_bytes, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": int(dbc.prescribed_dofs.nbytes + dbc.values.nbytes),
+                "d2h_bytes_per_step": int(nd * 8)},
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import cgref
+        import hdgref
+        ns = min(n, 48)
+        om = hdgref.rectangle_mesh(ns, ns)
+        t0 = time.perf_counter()
+        r = cgref.solve_poisson_cg(om, order)
+        dt = time.perf_counter() - t0
+        scale = (ns * ns) / (n * n)
+        line["cpu_baseline"] = {"value": scale / dt, "unit": "solves/s", "cores": 1, "kind": "port",
+                                "sample": f"one complete solve of the {ns}x{ns} (2*{ns}^2 cells) order-{order} problem by "
+                                          f"the numpy/SuperLU CG oracle in {dt:.2f} s, rate scaled by the cell ratio "
+                                          f"{scale:.4f} (the direct solve grows faster than linearly, so this favours the CPU)"}
+        line["cpu_oracle_errornorm_sq"] = r["err"]
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c4", choices=sorted(WORKLOADS) + ["c3", "c4", "c5"])
+    ap.add_argument("--workload", default="c4", choices=sorted(WORKLOADS) + ["c3", "c4", "c5", "cg"])
     ap.add_argument("--requests", type=int, default=2000)
     ap.add_argument("--hbm-budget-gb", type=float, default=64.0)
     ap.add_argument("--max-batch", type=int, default=64)
@@ -911,6 +1022,8 @@ def main():
         run_c3(args, ws, rank, local)
     elif args.workload == "c5":
         run_c5(args, ws, rank, local)
+    elif args.workload == "cg":
+        run_cg(args, ws, rank, local)
     else:
         run_ours(args, ws, rank, local)
     if ws > 1:

@@ -884,6 +884,54 @@ __global__ void k_amg_face_cheb(int nf, const int32_t* __restrict__ bcol5, const
   }
 }
 
+template <int NT>
+__global__ void k_amg_row_cheb(int nf, const int32_t* __restrict__ bcol5, const float* __restrict__ val,
+                                const float* __restrict__ dinv, const float* __restrict__ lam,
+                                const int32_t* __restrict__ face_prob, const float* __restrict__ b,
+                                float* __restrict__ bt, const float* __restrict__ xin, float* __restrict__ xout,
+                                float* __restrict__ d, int step, const int32_t* __restrict__ st) {
+  // one thread per row (f, i): with the block rows scaled by D^-1 the rows of a face are
+  // independent.  For small systems (too few faces to fill the GPU) this runs nt times more
+  // threads than the face kernel; on large ones it re-reads each face's columns and neighbour
+  // values nt times and loses (amg_row_sweeps)
+  const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t nd = (int64_t)nf * NT;
+  if (row >= nd) return;
+  const int f = (int)(row / NT), i = (int)(row - (int64_t)f * NT);
+  if (!amg_live(st, face_prob[f])) return;
+  // t = D^-1 (b - A x) = bt - (D^-1 A) x: the first step (x = 0) forms bt = D^-1 b for the rest
+  // of the cycle
+  float t;
+  if (!xin) {
+    t = 0.f;
+    for (int l = 0; l < NT; ++l) t += dinv[((int64_t)f * NT + i) * NT + l] * b[(int64_t)f * NT + l];
+    bt[row] = t;
+  } else {
+    t = bt[row];
+    int seen[5];
+    int ns = 0;
+    for (int k = 0; k < 5; ++k) {
+      const int g = bcol5[k * nf + f];
+      bool dup = false;
+      for (int u = 0; u < ns; ++u) dup |= (seen[u] == g);
+      if (dup) continue;
+      seen[ns++] = g;
+      for (int j = 0; j < NT; ++j) t -= val[(k * NT + j) * nd + row] * xin[(int64_t)g * NT + j];
+    }
+  }
+  const float hi = fmaxf(lam[face_prob[f]], 1e-30f), lo = hi / CHEB_RATIO;
+  const float theta = 0.5f * (hi + lo), delta = 0.5f * (hi - lo), sigma = theta / delta;
+  float rp = 1.f / sigma, rc = rp;  // rho_{step-1}, rho_step
+  for (int u = 1; u <= step; ++u) {
+    rc = 1.f / (2.f * sigma - rp);
+    if (u < step) rp = rc;
+  }
+  const float cd = (step == 0) ? 0.f : rc * rp, cr = (step == 0) ? 1.f / theta : 2.f * rc / delta;
+  const float dn = cr * t + (step == 0 ? 0.f : cd * d[row]);
+  d[row] = dn;
+  xout[row] = (xin ? xin[row] : 0.f) + dn;
+}
+
 // scaled residual r~ = D^-1 (b - A0 x) = bt - (D^-1 A0) x (level 0); the restriction uses D P0
 template <int NT>
 __global__ void k_amg_face_residual(int nf, const int32_t* __restrict__ bcol5, const float* __restrict__ val,
@@ -1111,6 +1159,24 @@ template <int NT> void numeric_nt(hdg_system* s, const float* val0, cudaStream_t
   HDG_CUDA(cudaGetLastError());
 }
 
+// One level-0 Chebyshev step: a thread per row below AMG_ROW_SWEEP_FACES faces (latency-bound
+// sizes), a thread per face above.  Measured: 49 k faces (p = 4): rows 15 -> 10 us per sweep;
+// 197 k faces (p = 2) and the batch's bins (0.4-0.7 M faces): faces faster.
+constexpr int AMG_ROW_SWEEP_FACES = 100000;
+template <int NT>
+void cheb_sweep(hdg_system* s, const float* val0, const float* b0, const float* in, float* out, int step,
+                const int32_t* cst, cudaStream_t st) {
+  AmgHierarchy* H = s->amg;
+  const int nf = H->nf;
+  if (nf < AMG_ROW_SWEEP_FACES)
+    k_amg_row_cheb<NT><<<nblk((int64_t)nf * NT), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p,
+                                                              H->face_prob.p, b0, H->bt0.p, in, out, H->d0.p, step,
+                                                              cst);
+  else
+    k_amg_face_cheb<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
+                                                  H->bt0.p, in, out, H->d0.p, step, cst);
+}
+
 template <int NT>
 void apply_nt(hdg_system* s, const float* val0, const float* b0, float* z0, const int32_t* cst, cudaStream_t st) {
   AmgHierarchy* H = s->amg;
@@ -1123,8 +1189,7 @@ void apply_nt(hdg_system* s, const float* val0, const float* b0, float* z0, cons
   for (int t = 0; t < k; ++t) {
     float* out = ((k - 1 - t) % 2 == 0) ? z0 : H->x0.p;
     const float* in = (t == 0) ? nullptr : (out == z0 ? H->x0.p : z0);
-    k_amg_face_cheb<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
-                                                  H->bt0.p, in, out, H->d0.p, t, cst);
+    cheb_sweep<NT>(s, val0, b0, in, out, t, cst, st);
   }
   k_amg_face_residual<NT><<<nblk(n0), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->bt0.p, z0, H->r0.p, H->face_prob.p,
                                                     cst);
@@ -1162,8 +1227,7 @@ void apply_nt(hdg_system* s, const float* val0, const float* b0, float* z0, cons
   for (int t = 0; t < k; ++t) {
     const float* in = (t % 2 == 0) ? z0 : H->x0.p;
     float* out = (t % 2 == 0) ? H->x0.p : z0;
-    k_amg_face_cheb<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
-                                                  H->bt0.p, in, out, H->d0.p, t, cst);
+    cheb_sweep<NT>(s, val0, b0, in, out, t, cst, st);
   }
   if (k % 2 == 1) HDG_CUDA(cudaMemcpyAsync(z0, H->x0.p, sizeof(float) * n0, cudaMemcpyDeviceToDevice, st));
 }

@@ -165,10 +165,31 @@ __global__ void k_lag_scatter(int nd, const int32_t* __restrict__ dofs, const do
 // sc: [0] mean diag, [1] b.b, [2] rz of even iterations, [3] rz of odd ones, [4] status
 // (0 running, 1 converged, 2 iteration cap, 3 non-finite), [5] iterations, [6] final r.r
 // part: [3][nblocks] partial p.q, r.z, r.r
-__device__ __forceinline__ double sum_parts(const double* __restrict__ p, int nb) {
-  double s = 0.0;
-  for (int k = 0; k < nb; ++k) s += p[k];
-  return s;
+// The per-block partials of the previous kernel, added by warp 0 (lane-strided, then a fixed
+// shuffle tree) and handed to the block through shared memory: every block gets the same sums.
+// Also reads the status once per block, so that a whole block leaves together.  Contains a
+// barrier: call it from every thread of the block.
+__device__ __forceinline__ void block_inputs(const double* __restrict__ a, const double* __restrict__ b, int nb,
+                                             const double* __restrict__ sc, double* ra, double* rb, double* status) {
+  __shared__ double sh[3];
+  if (threadIdx.x < 32) {
+    double sa = 0.0, sb = 0.0;
+    for (int k = threadIdx.x; k < nb; k += 32) {
+      sa += a[k];
+      if (b) sb += b[k];
+    }
+    sa = warp_sum(sa);
+    sb = warp_sum(sb);
+    if (threadIdx.x == 0) {
+      sh[0] = sa;
+      sh[1] = sb;
+      sh[2] = sc[4];
+    }
+  }
+  __syncthreads();
+  *ra = sh[0];
+  *rb = sh[1];
+  *status = sh[2];
 }
 
 __device__ __forceinline__ double block_sum(double v) {
@@ -220,8 +241,9 @@ __global__ void __launch_bounds__(LB) k_lag_cg_a(int n, const int32_t* __restric
                                                  double* __restrict__ pnew, double* __restrict__ q,
                                                  double* __restrict__ part, double* __restrict__ sc, int nb, int it,
                                                  int maxit, double tol2) {
-  if (sc[4] != 0.0) return;
-  const double rz = sum_parts(part + nb, nb), rr = sum_parts(part + 2 * nb, nb);
+  double rz, rr, status;
+  block_inputs(part + nb, part + 2 * nb, nb, sc, &rz, &rr, &status);
+  if (status != 0.0) return;  // uniform in the block
   if (it == 0 && blockIdx.x == 0 && threadIdx.x == 0) sc[1] = rr;
   const double bb = (it == 0) ? rr : sc[1];
   if (rr <= tol2 * bb || !(rr == rr)) {
@@ -263,8 +285,9 @@ __global__ void __launch_bounds__(LB) k_lag_cg_b(int n, const double* __restrict
                                                  const double* __restrict__ dinv, double* __restrict__ x,
                                                  double* __restrict__ r, double* __restrict__ z,
                                                  double* __restrict__ part, double* __restrict__ sc, int nb, int it) {
-  if (sc[4] != 0.0) return;
-  const double pq = sum_parts(part, nb);
+  double pq, unused, status;
+  block_inputs(part, nullptr, nb, sc, &pq, &unused, &status);
+  if (status != 0.0) return;  // uniform in the block
   const double alpha = (pq > 0.0) ? sc[2 + (it & 1)] / pq : 0.0;
   double rz = 0.0, rr = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {

@@ -42,6 +42,11 @@ class LagrangeSystem:
         self.pattern.sort_indices()
         self.ndofs = dh.ndofs()
         nl = fe.getnbasefunctions()
+        if dh.cell_dofs.size != mesh.ncells * nl:
+            # src/dofhandler.jl:118-122 pushes one dof when it meets an entity with several dofs a
+            # second time, so from order 3 on the cells do not hold a full set of dofs
+            raise NotImplementedError("the DofHandler numbering of this order does not give every cell "
+                                      f"{nl} dofs (orders 1 and 2 do)")
         cd = np.ascontiguousarray(dh.cell_dofs.reshape(mesh.ncells, nl), dtype=np.int32)
         colptr = np.ascontiguousarray(self.pattern.indptr, dtype=np.int64)
         rowval = np.ascontiguousarray(self.pattern.indices, dtype=np.int64)
