@@ -1095,6 +1095,18 @@ inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)std::max<int64_t
 // 256-problem batch (kappa contrast 1e4, tol 1e-9): degree 1/2/3 took 754/474/359 iterations at
 // most and gave 302/367/398 solves/s; on the 131072-cell p=2 problem with kappa = 1, degree 2 was
 // 5 % faster than 3 (103 vs 99 iterations).
+// l1-Jacobi sweeps before and after the coarse correction on each coarse level
+// (HDG_AMG_COARSE_SWEEPS, 1..4, default 2).  On the 256-problem batch 1/2/3 sweeps gave
+// 406/418/415 solves/s (396/359/349 iterations for the hardest problem).
+int amg_coarse_sweeps() {
+  static const int k = [] {
+    const char* e = std::getenv("HDG_AMG_COARSE_SWEEPS");
+    const int v = e ? std::atoi(e) : 2;
+    return (v >= 1 && v <= 4) ? v : 2;
+  }();
+  return k;
+}
+
 int amg_cheb_degree() {
   static const int k = [] {
     const char* e = std::getenv("HDG_AMG_CHEB_DEGREE");
@@ -1196,34 +1208,46 @@ void apply_nt(hdg_system* s, const float* val0, const float* b0, float* z0, cons
   AmgLevel& L1 = H->lev[0];
   k_amg_restrict0<NT><<<nblk(L1.n), 256, 0, st>>>(L1.n, H->rptr0.p, H->rent0.p, H->dpval0.p, H->r0.p, L1.dl1inv.p,
                                                   L1.b.p, L1.x.p, L1.prob.p, cst);
-  // coarse levels down: x holds the first sweep (from the restriction); the second sweep goes to
-  // t, which then holds the level's iterate until the way up
+  // coarse levels down: x holds the first l1-Jacobi sweep (done by the restriction); the other
+  // nu - 1 sweeps alternate between x and t; the iterate then stays where it is until the way up
+  const int nu = amg_coarse_sweeps();
+  float* iter[AMG_MAX_LEVELS];
+  float* fin[AMG_MAX_LEVELS];
   for (int l = 0; l + 1 < nl; ++l) {
     AmgLevel& L = H->lev[l];
     AmgLevel& C = H->lev[l + 1];
-    AMG_LAUNCH_G(k_amg_l1_sweep, L.n, st, L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.x.p, L.t.p, L.prob.p,
-                 cst);
-    AMG_LAUNCH_G(k_amg_residual, L.n, st, L.n, L.ptr.p, L.col.p, L.val.p, L.b.p, L.t.p, L.r.p, L.prob.p, cst);
+    float* cur = L.x.p;
+    float* oth = L.t.p;
+    for (int sw = 1; sw < nu; ++sw) {
+      AMG_LAUNCH_G(k_amg_l1_sweep, L.n, st, L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, cur, oth, L.prob.p,
+                   cst);
+      std::swap(cur, oth);
+    }
+    iter[l] = cur;
+    AMG_LAUNCH_G(k_amg_residual, L.n, st, L.n, L.ptr.p, L.col.p, L.val.p, L.b.p, cur, L.r.p, L.prob.p, cst);
     const bool coarsest = (l + 2 == nl);
     AMG_LAUNCH_G(k_amg_restrict, C.n, st, C.n, L.rptr.p, L.rent.p, L.rrow.p, L.pval.p, L.r.p,
                  coarsest ? nullptr : C.dl1inv.p, C.b.p, C.x.p, C.prob.p, cst);
   }
   AmgLevel& C = H->lev.back();
   if (H->cmax > 0) k_amg_coarse_solve<<<s->nprob, 128, 0, st>>>(H->crow0.p, H->coff.p, H->cinv.p, C.b.p, C.x.p, cst);
-  // coarse levels up: the coarser level's result is in its x; prolongate into this level's
-  // iterate (t), then two sweeps t -> r -> x
+  fin[nl - 1] = C.x.p;
+  // coarse levels up: prolongate the coarser level's result into this level's iterate, then nu
+  // sweeps alternating with r (free again); the last one holds the level's result
   for (int l = nl - 2; l >= 0; --l) {
     AmgLevel& L = H->lev[l];
-    AmgLevel& Cn = H->lev[l + 1];
-    AMG_LAUNCH_G(k_amg_prolong, L.n, st, L.n, L.pptr.p, L.pcol.p, L.pval.p, Cn.x.p, L.t.p, L.prob.p, cst);
-    AMG_LAUNCH_G(k_amg_l1_sweep, L.n, st, L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.t.p, L.r.p, L.prob.p,
-                 cst);
-    AMG_LAUNCH_G(k_amg_l1_sweep, L.n, st, L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, L.r.p, L.x.p, L.prob.p,
-                 cst);
+    float* a = iter[l];
+    float* b = L.r.p;
+    AMG_LAUNCH_G(k_amg_prolong, L.n, st, L.n, L.pptr.p, L.pcol.p, L.pval.p, fin[l + 1], a, L.prob.p, cst);
+    for (int sw = 0; sw < nu; ++sw) {
+      AMG_LAUNCH_G(k_amg_l1_sweep, L.n, st, L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, a, b, L.prob.p, cst);
+      std::swap(a, b);
+    }
+    fin[l] = a;
   }
   // level 0 up: prolongate, then the same Chebyshev polynomial from the corrected iterate (z0,
   // x0, z0, ...); for odd k the result lands in x0 and is copied to z0
-  k_amg_prolong0<NT><<<nblk(n0), 256, 0, st>>>(nf, H->pcol0.p, H->pval0.p, L1.x.p, z0, H->face_prob.p, cst);
+  k_amg_prolong0<NT><<<nblk(n0), 256, 0, st>>>(nf, H->pcol0.p, H->pval0.p, fin[0], z0, H->face_prob.p, cst);
   for (int t = 0; t < k; ++t) {
     const float* in = (t % 2 == 0) ? z0 : H->x0.p;
     float* out = (t % 2 == 0) ? H->x0.p : z0;
@@ -1273,15 +1297,17 @@ double amg_cycle_bytes(const hdg_system* s) {
       break;
     }
     const double npc = (double)H->lev[l].h_col.size();      // P and P' sizes are comparable to A's
-    b += 3.0 * (spmv + 20.0 * n) + (spmv + 16.0 * n);      // three sweeps, one residual
+    b += (2 * amg_coarse_sweeps() - 1) * (spmv + 20.0 * n) + (spmv + 16.0 * n);  // sweeps, one residual
     b += 2.0 * (8.0 * npc + 12.0 * n);                      // restriction and prolongation
   }
   return b;
 }
 
 int amg_cycle_launches(const hdg_system* s) {
-  const int nl = (int)s->amg->lev.size(), k = amg_cheb_degree();
-  return (k + 2) + 3 * (nl - 1) + 1 + 3 * (nl - 1) + (1 + k);  // the D2D copy of odd k is no kernel
+  const int nl = (int)s->amg->lev.size(), k = amg_cheb_degree(), nu = amg_coarse_sweeps();
+  // level 0 down, coarse levels down, coarsest, coarse levels up, level 0 up (the D2D copy of an
+  // odd degree is no kernel)
+  return (k + 2) + (nu + 1) * (nl - 1) + 1 + (nu + 1) * (nl - 1) + (1 + k);
 }
 
 void amg_apply(hdg_system* s, const float* r, float* z, const int32_t* cg_state, cudaStream_t st) {

@@ -262,8 +262,6 @@ int hdg_space_create(hdg_mesh* mesh, int p, int qd, hdg_space** out) {
       return fail(ctx, HDG_ERR_BAD_ORDER, "Quadrature rule of order " + std::to_string(qd) + " not available");
     }
     s->d_ref.upload(s->t.packed.data(), s->t.packed.size(), ctx->stream);
-    std::vector<float> pf(s->t.packed.begin(), s->t.packed.end());
-    s->d_reff.upload(pf.data(), pf.size(), ctx->stream);
     HDG_CUDA(cudaStreamSynchronize(ctx->stream));
     *out = s;
     return HDG_OK;

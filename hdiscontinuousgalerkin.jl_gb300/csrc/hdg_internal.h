@@ -217,7 +217,6 @@ struct hdg_space {
   hdg_mesh* mesh = nullptr;
   RefTables t;
   DevBuf<double> d_ref;
-  DevBuf<float> d_reff;
 };
 
 struct CgState;       // cg.cu

@@ -244,26 +244,29 @@ __global__ void __launch_bounds__(LB) k_lag_cg_a(int n, const int32_t* __restric
   double rz, rr, status;
   block_inputs(part + nb, part + 2 * nb, nb, sc, &rz, &rr, &status);
   if (status != 0.0) return;  // uniform in the block
-  if (it == 0 && blockIdx.x == 0 && threadIdx.x == 0) sc[1] = rr;
-  const double bb = (it == 0) ? rr : sc[1];
-  if (rr <= tol2 * bb || !(rr == rr)) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-      sc[4] = (rr == rr) ? 1.0 : 3.0;
-      sc[5] = it;
-      sc[6] = rr;
+  // the scalar decisions once per block (thread 0), handed out through shared memory: on this
+  // part a division per thread costs more FP64 issue than the whole row loop
+  __shared__ double sh_beta;
+  __shared__ int sh_go;
+  if (threadIdx.x == 0) {
+    if (it == 0 && blockIdx.x == 0) sc[1] = rr;
+    const double bb = (it == 0) ? rr : sc[1];
+    int go = 1;
+    if (rr <= tol2 * bb || !(rr == rr) || it >= maxit) {
+      go = 0;
+      if (blockIdx.x == 0) {
+        sc[4] = (it >= maxit && rr == rr && !(rr <= tol2 * bb)) ? 2.0 : ((rr == rr) ? 1.0 : 3.0);
+        sc[5] = it;
+        sc[6] = rr;
+      }
     }
-    return;
+    sh_go = go;
+    sh_beta = (it == 0) ? 0.0 : rz / sc[2 + ((it - 1) & 1)];
+    if (go && blockIdx.x == 0) sc[2 + (it & 1)] = rz;
   }
-  if (it >= maxit) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-      sc[4] = 2.0;
-      sc[5] = it;
-      sc[6] = rr;
-    }
-    return;
-  }
-  const double beta = (it == 0) ? 0.0 : rz / sc[2 + ((it - 1) & 1)];
-  if (blockIdx.x == 0 && threadIdx.x == 0) sc[2 + (it & 1)] = rz;
+  __syncthreads();
+  if (!sh_go) return;  // uniform in the block
+  const double beta = sh_beta;
   double pq = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     double s = 0.0;
@@ -288,7 +291,10 @@ __global__ void __launch_bounds__(LB) k_lag_cg_b(int n, const double* __restrict
   double pq, unused, status;
   block_inputs(part, nullptr, nb, sc, &pq, &unused, &status);
   if (status != 0.0) return;  // uniform in the block
-  const double alpha = (pq > 0.0) ? sc[2 + (it & 1)] / pq : 0.0;
+  __shared__ double sh_alpha;
+  if (threadIdx.x == 0) sh_alpha = (pq > 0.0) ? sc[2 + (it & 1)] / pq : 0.0;
+  __syncthreads();
+  const double alpha = sh_alpha;
   double rz = 0.0, rr = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     x[i] += alpha * p[i];
