@@ -331,10 +331,10 @@ def run_c3(args, ws, rank, local):
     dbc = H.Dirichlet(H.TrialFunction(Mh), mesh, "boundary")
     tol = args.tol if args.tol != 1e-12 else 1e-10
 
-    def run(prec, tol_, keep):
+    def run(prec, tol_, keep, pc=H.PRECOND_JACOBI):
         K.reassemble(resident=True)
         K.apply_dirichlet(dbc.prescribed_dofs, dbc.values)
-        uh = K.solve(tol=tol_, precision=prec, to_host=keep)
+        uh = K.solve(tol=tol_, precision=prec, to_host=keep, preconditioner=pc)
         r = K.recover(to_host=keep)
         return (uh, r[0], r[1]) if keep else None
 
@@ -362,6 +362,15 @@ def run_c3(args, ws, rank, local):
     run(H.PREC_FP64, tol, False)
     f1.record(stream)
     torch.cuda.synchronize()
+    # the same solve with the multigrid preconditioner: FP64 CG around an FP32 V-cycle
+    gmg = run(H.PREC_MIXED, tol, True, H.PRECOND_AMG)
+    itg = K.stats.iterations
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record(stream)
+    for _ in range(args.steps):
+        run(H.PREC_MIXED, tol, False, H.PRECOND_AMG)
+    g1.record(stream)
+    torch.cuda.synchronize()
     line = {
         "metric": METRIC, "value": ws * 1e3 / ms, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -372,6 +381,10 @@ def run_c3(args, ws, rank, local):
         "rel_l2_vs_fp64": {"uhat": rel_l2(got[0], ref[0]), "q": rel_l2(got[1].ravel(), ref[1].ravel()),
                            "u": rel_l2(got[2].ravel(), ref[2].ravel())},
         "fp64_solves_per_s": 1e3 / f0.elapsed_time(f1), "cg_iterations_mixed": itm, "cg_iterations_fp64": it64,
+        "multigrid": {"solves_per_s": args.steps * 1e3 / g0.elapsed_time(g1), "cg_iterations": itg,
+                      "what": "FP64 CG preconditioned by the FP32 smoothed-aggregation V-cycle, same tolerance",
+                      "rel_l2_vs_fp64": {"uhat": rel_l2(gmg[0], ref[0]), "q": rel_l2(gmg[1].ravel(), ref[1].ravel()),
+                                         "u": rel_l2(gmg[2].ravel(), ref[2].ravel())}},
         "gpu_launches": launches, "clocks": clk,
         "cpu_baseline": None,
         "cpu_baseline_note": "not measured for this workload: the oracle's sparse direct solve of 3.1 M trace dofs "

@@ -89,6 +89,8 @@ SIGNATURES = {
     "hdg_system_get_element_blocks": ([vp, dp, dp, dp, dp], ip),
     "hdg_dirichlet": ([vp, C.c_char_p, C.POINTER(hdg_field), i32p, dp, intp], ip),
     "hdg_apply_dirichlet": ([vp, i32p, dp, ip], ip),
+    "hdg_dirichlet_l2": ([vp, C.c_char_p, C.POINTER(hdg_field), i32p, dp, intp], ip),
+    "hdg_space_set_he_tau": ([vp, ip], ip),
     "hdg_solve": ([vp, C.POINTER(hdg_solver), dp, C.POINTER(hdg_stats)], ip),
     "hdg_recover": ([vp, dp, dp, dp], ip),
     "hdg_errornorm_l2sq": ([vp, C.POINTER(hdg_field), dp], ip),

@@ -414,6 +414,7 @@ static int assemble_condense_impl(hdg_space* space, double tau, const hdg_field*
       s->space = space;
       s->ctx = ctx;
       s->precision = precision;
+      s->he_tau = space->he_tau;
       const RefTables& t = space->t;
       s->nw = t.nw;
       s->nt = t.nt;
@@ -630,6 +631,56 @@ int hdg_dirichlet(const hdg_space* sp, const char* faceset, const hdg_field* g, 
       ++k;
     }
   }
+  return HDG_OK;
+}
+
+int hdg_dirichlet_l2(const hdg_space* sp, const char* faceset, const hdg_field* g, int32_t* dofs, double* vals,
+                     int* count) {
+  if (!sp || !faceset || !count) return HDG_ERR_ARG;
+  const hdg_mesh* m = sp->mesh;
+  auto it = m->facesets.find(faceset);
+  if (it == m->facesets.end()) return fail(m->ctx, HDG_ERR_UNKNOWN_SET, std::string("no face set ") + faceset);
+  const RefTables& t = sp->t;
+  const int nt = t.nt, nfq = t.nfq;
+  *count = (int)it->second.size() * nt;
+  if (!dofs && !vals) return HDG_OK;
+  FieldSpec gs = field_from(g, 0.0);
+  static const double EDGE[3][4] = {{1, 0, 0, 1}, {0, 1, 0, 0}, {0, 0, 1, 0}};
+  static const int EN[3][2] = {{1, 2}, {2, 0}, {0, 1}};
+  int k = 0;
+  for (int32_t f : it->second) {
+    if (m->faces[4 * f + 3] >= 0) return fail(m->ctx, HDG_ERR_NOT_BOUNDARY, "Face " + std::to_string(f + 1) + " is not in boundary");
+    const int c = m->faces[4 * f + 2];
+    int fl = 0;
+    while (m->cfaces[3 * c + fl] != f) ++fl;
+    const bool o = m->cells[3 * c + EN[fl][1]] > m->cells[3 * c + EN[fl][0]];
+    // L2 projection onto the face's orthonormal Legendre basis: u_i = int_0^1 g mu_i ds (the
+    // face length cancels against the trace mass matrix |e| I), with the face rule's weights
+    for (int i = 0; i < nt; ++i) {
+      double acc = 0.0;
+      for (int q = 0; q < nfq; ++q) {
+        const int oq = o ? q : nfq - 1 - q;
+        const double s = t.fx[oq];
+        const double ex = (1.0 - s) * EDGE[fl][0] + s * EDGE[fl][2], ey = (1.0 - s) * EDGE[fl][1] + s * EDGE[fl][3];
+        const double L[3] = {1.0 - ex - ey, ex, ey};
+        double xq = 0, yq = 0;
+        for (int a = 0; a < 3; ++a) {
+          xq += L[a] * m->xy[2 * m->cells[3 * c + a]];
+          yq += L[a] * m->xy[2 * m->cells[3 * c + a] + 1];
+        }
+        acc += t.fw[q] * eval_field_host(gs, xq, yq) * t.T[i * nfq + q];
+      }
+      if (vals) vals[k] = acc;
+      if (dofs) dofs[k] = f * nt + i + 1;
+      ++k;
+    }
+  }
+  return HDG_OK;
+}
+
+int hdg_space_set_he_tau(hdg_space* sp, int on) {
+  if (!sp) return HDG_ERR_ARG;
+  sp->he_tau = on != 0;
   return HDG_OK;
 }
 

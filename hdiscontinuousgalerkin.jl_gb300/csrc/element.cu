@@ -34,6 +34,7 @@ struct ElemArgs {
   double* KB;
   int* err;
   int schur;  // 1: the Schur-complement path (invertible reference mass, kappa constant per cell)
+  int he_tau; // 1: He carries tau
 };
 
 // One warp per cell; EWARPS warps (cells) per CTA, picked per degree, quadrature size and mesh
@@ -370,7 +371,7 @@ __global__ void __launch_bounds__(EWARPS * 32) k_element_condense(ElemArgs a) {
       double v;
       if (col < M) {
         const int g = col / NT, j = col - g * NT;
-        v = (g == f) ? s - el[f] * ref[L.H + i * NT + j] : s;
+        v = (g == f) ? s - (a.he_tau ? tau : 1.0) * el[f] * ref[L.H + i * NT + j] : s;
       } else {
         v = -s;
       }
@@ -503,6 +504,7 @@ void launch_element_condense(hdg_system* s, cudaStream_t st) {
   a.nc = m->nc;
   a.co = s->coef_dev();
   a.kappa_mode = s->kappa_cells ? 1 : (s->kappa_field ? 2 : 0);
+  a.he_tau = s->he_tau ? 1 : 0;
   a.kcell = s->d_kappa.p;
   a.AB = s->d_AB.p;
   a.KB = s->d_KB.p;

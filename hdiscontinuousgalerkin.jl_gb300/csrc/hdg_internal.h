@@ -217,6 +217,7 @@ struct hdg_space {
   hdg_mesh* mesh = nullptr;
   RefTables t;
   DevBuf<double> d_ref;
+  bool he_tau = false;  // He = tau int mu mu dS (off: the reference's He without tau)
 };
 
 struct CgState;       // cg.cu
@@ -229,6 +230,7 @@ struct hdg_system {
   int nw, nt, n, m, nc, nf, ndofs;
   int64_t nblocks, nnz;
   double tau = 1.0;
+  bool he_tau = false;  // He carries tau (copied from the space at creation)
   // Problems held by this system (several when batched; all share the degree).  Problem P owns
   // trace rows [h_prob_row0[P], h_prob_row0[P+1]).
   int nprob = 1;

@@ -36,14 +36,22 @@ class SolveStats:
 class TraceSystem:
     """Assembled + condensed HDG trace system on the device (hdg_system)."""
 
-    def __init__(self, space_handle, tau=1.0, f=None, kappa=None, kappa_cell=None, precision=L.PREC_FP64):
+    def __init__(self, space_handle, tau=1.0, f=None, kappa=None, kappa_cell=None, precision=L.PREC_FP64,
+                 he_tau=False):
         self.sp = space_handle
         self.ctx = space_handle.mesh.ctx
         self.precision = precision
         h = C.c_void_p()
         fc, kc, kcell = self._coef(f, kappa, kappa_cell)
-        L.check(L.load().hdg_assemble_condense(self.sp.h, float(tau), fc, kc, kcell, int(precision), C.byref(h)),
-                self.ctx)
+        lib = L.load()
+        if he_tau:  # the choice is taken by the system at creation; the shared space is reset
+            L.check(lib.hdg_space_set_he_tau(self.sp.h, 1))
+        try:
+            L.check(lib.hdg_assemble_condense(self.sp.h, float(tau), fc, kc, kcell, int(precision), C.byref(h)),
+                    self.ctx)
+        finally:
+            if he_tau:
+                lib.hdg_space_set_he_tau(self.sp.h, 0)
         self._h = h
         nd, nnz, n, m = C.c_int(), C.c_int64(), C.c_int(), C.c_int()
         L.check(L.load().hdg_system_sizes(self._h, C.byref(nd), C.byref(nnz), C.byref(n), C.byref(m)))
@@ -173,12 +181,13 @@ class _LocalView:
 
 
 def doassemble(Vh: VectorFunctionSpace, Wh: ScalarFunctionSpace, Mh: ScalarTraceFunctionSpace, tau: float = 1.0,
-               f=None, kappa=None, kappa_cell=None, precision=L.PREC_FP64):
+               f=None, kappa=None, kappa_cell=None, precision=L.PREC_FP64, he_tau=False):
     """doassemble(Vh, Wh, Mh, τ) of examples/poisson2D_HDG.jl:58-186 on the device.
-    Returns (K, b, K_e, b_e); K is the TraceSystem, the others are views of it."""
+    Returns (K, b, K_e, b_e); K is the TraceSystem, the others are views of it.
+    he_tau=True puts τ into He (the reference's He has none, :149; they agree for τ = 1)."""
     if not (Vh.sp is Wh.sp is Mh.sp):
         raise ValueError("Vh, Wh and Mh must be built on the same mesh with the same degree and quadrature")
-    K = TraceSystem(Wh.sp, tau, f, kappa, kappa_cell, precision)
+    K = TraceSystem(Wh.sp, tau, f, kappa, kappa_cell, precision, he_tau)
     return K, _RhsView(K), _LocalView(K, "K"), _LocalView(K, "b")
 
 
@@ -186,7 +195,9 @@ class Dirichlet:
     """Dirichlet(û_h, mesh, faceset, g) on the trace space (src/boundary.jl:212-247), or
     Dirichlet(u, dh, faceset, g) on a nodal field of a DofHandler (src/boundary.jl:44-95)."""
 
-    def __init__(self, u, mesh, faceset: str, g=None):
+    def __init__(self, u, mesh, faceset: str, g=None, projection: str = "reference"):
+        """projection="l2" takes the L2 projection of g onto the trace basis (hdg_dirichlet_l2)
+        instead of the reference's accumulation (src/boundary.jl:232-242)."""
         from .dofhandler import DofHandler, DirichletDH
         if isinstance(mesh, DofHandler):
             d = DirichletDH(u, mesh, faceset, g if g is not None else (lambda x: 0.0))
@@ -198,11 +209,14 @@ class Dirichlet:
         g = as_field(g if g is not None else 0.0)
         gc = g.as_c()
         n = C.c_int()
-        L.check(L.load().hdg_dirichlet(fs.sp.h, faceset.encode(), C.byref(gc), None, None, C.byref(n)), mesh.ctx)
+        if projection not in ("reference", "l2"):
+            raise ValueError("projection is 'reference' or 'l2'")
+        fn = L.load().hdg_dirichlet_l2 if projection == "l2" else L.load().hdg_dirichlet
+        L.check(fn(fs.sp.h, faceset.encode(), C.byref(gc), None, None, C.byref(n)), mesh.ctx)
         self.prescribed_dofs = np.zeros(n.value, np.int32)
         self.values = np.zeros(n.value)
-        L.check(L.load().hdg_dirichlet(fs.sp.h, faceset.encode(), C.byref(gc), L.i32ptr(self.prescribed_dofs),
-                                       L.dptr(self.values), C.byref(n)), mesh.ctx)
+        L.check(fn(fs.sp.h, faceset.encode(), C.byref(gc), L.i32ptr(self.prescribed_dofs), L.dptr(self.values),
+                   C.byref(n)), mesh.ctx)
 
 
 def apply_(K, b, dbc: Dirichlet):

@@ -154,6 +154,15 @@ int hdg_system_get_element_blocks(const hdg_system* sys, double* Ate, double* bt
  * dofs/vals may be NULL to query count. */
 int hdg_dirichlet(const hdg_space* space, const char* faceset, const hdg_field* g, int32_t* dofs, double* vals,
                   int* count);
+/* The corrected trace projection: u_i = int_0^1 g mu_i ds on every face of the set, the L2
+ * projection onto the orthonormal Legendre basis (same arguments and dof order as hdg_dirichlet,
+ * which keeps the reference's projection, src/boundary.jl:232-242, for parity). */
+int hdg_dirichlet_l2(const hdg_space* space, const char* faceset, const hdg_field* g, int32_t* dofs, double* vals,
+                     int* count);
+/* on != 0: systems assembled from this space from now on use He = tau int mu mu dS in the
+ * condensation (each system keeps the choice it was created with, also when reassembled).  The
+ * reference's He carries no tau (examples/poisson2D_HDG.jl:149), consistent only for tau = 1. */
+int hdg_space_set_he_tau(hdg_space* space, int on);
 /* apply!(K, b, dbc), src/boundary.jl:326-363 (APPLY_TRANSPOSE): b -= v K[:,d]; zero rows and
  * columns of the prescribed dofs; K[d,d] = mean|diag K|; b[d] = v * mean|diag K|. */
 int hdg_apply_dirichlet(hdg_system* sys, const int32_t* dofs, const double* vals, int n);

@@ -823,8 +823,11 @@ int hr_element_blocks(const void* mv, int c, int p, int qd, double tau, int fkin
 // end_assemble's COO->CSC with duplicates summed (src/assembler.jl:47-49); rhs scatter-add
 // (src/assembler.jl:55-60).  kappa: per-cell array (or null) or a field (kkind >= 0).
 // Returns an opaque system, or null with *status set (-1 det(J)<=0, -2 bad rule, -3 singular).
-void* hr_assemble(const void* mv, int p, int qd, double tau, int fkind, int fnp, const double* fprm, int kkind,
-                  int knp, const double* kprm, const double* kappa_cell, int nthreads, int* status) {
+// he_tau != 0 subtracts τ·He instead of He: the hybridised flux is q̂·n = q·n + τ(u - û), so the
+// trace equation's He term carries τ; the reference leaves it out (:149), which agrees for τ = 1.
+void* hr_assemble_ex(const void* mv, int p, int qd, double tau, int fkind, int fnp, const double* fprm, int kkind,
+                     int knp, const double* kprm, const double* kappa_cell, int nthreads, int he_tau, int* status) {
+  const double hs = he_tau ? tau : 1.0;
   const Mesh& m = *(const Mesh*)mv;
   Tables t;
   *status = 0;
@@ -883,7 +886,7 @@ void* hr_assemble(const void* mv, int p, int qd, double tau, int fkind, int fnp,
         double s = 0;
         for (int k = 0; k < nv; ++k) s += b.E[k * mm + i] * K[k * mm + j];
         for (int k = 0; k < nw; ++k) s += b.F[k * mm + i] * K[(nv + k) * mm + j];
-        At[i * mm + j] = s - b.H[i * mm + j];
+        At[i * mm + j] = s - hs * b.H[i * mm + j];
       }
       double s = 0;
       for (int k = 0; k < nv; ++k) s += b.E[k * mm + i] * bl[k];
@@ -934,6 +937,11 @@ void* hr_assemble(const void* mv, int p, int qd, double tau, int fkind, int fnp,
     S->colptr[j + 1] = (int64_t)S->rowval.size();
   }
   return S;
+}
+
+void* hr_assemble(const void* mv, int p, int qd, double tau, int fkind, int fnp, const double* fprm, int kkind,
+                  int knp, const double* kprm, const double* kappa_cell, int nthreads, int* status) {
+  return hr_assemble_ex(mv, p, qd, tau, fkind, fnp, fprm, kkind, knp, kprm, kappa_cell, nthreads, 0, status);
 }
 
 void hr_system_free(void* s) { delete (System*)s; }
@@ -1002,6 +1010,52 @@ int hr_dirichlet(const void* mv, int p, int qd, const char* faceset, int gkind, 
         N += t.vol.w[q] * eval_field(g, xq, yq) * t.T[i * nfq + q];
       }
       vals[k] = N;
+      dofs[k] = fidx * nt - nt + (i + 1);
+      ++k;
+    }
+  }
+  return k;
+}
+
+// The L2 projection of g onto the trace basis of each boundary face: û_i = ∫₀¹ g μ_i ds with the
+// face rule's weights (the trace basis is orthonormal on [0, 1], and |e| cancels against the
+// trace mass matrix |e|·I).  Same dofs and order as hr_dirichlet; returns the count.
+int hr_dirichlet_l2(const void* mv, int p, int qd, const char* faceset, int gkind, int gnp, const double* gprm,
+                    int* dofs, double* vals) {
+  const Mesh& m = *(const Mesh*)mv;
+  Tables t;
+  if (!build_tables(p, qd, &t)) return -2;
+  auto it = m.facesets.find(faceset);
+  if (it == m.facesets.end()) return -1;
+  std::vector<char> in(m.nf() + 1, 0);
+  for (int f : it->second) in[f] = 1;
+  Field g = make_field(gkind, gnp, gprm);
+  const int nt = t.nt, nfq = t.nfq;
+  int k = 0;
+  for (int fidx = 1; fidx <= m.nf(); ++fidx) {
+    if (!in[fidx]) continue;
+    if (m.faces[4 * (fidx - 1) + 3] != 0) return -3;
+    int c = m.faces[4 * (fidx - 1) + 2] - 1;
+    int fl = 0;
+    while (m.cfaces[3 * c + fl] != fidx) ++fl;
+    bool o = orientation(m, c, fl);
+    const int* nd = &m.cells[3 * c];
+    for (int i = 0; i < nt; ++i) {
+      double u = 0.0;
+      for (int q = 0; q < nfq; ++q) {
+        int oq = o ? q : nfq - 1 - q;
+        double s = t.face.x[oq];
+        double ex = (1.0 - s) * REF_EDGE[fl][0][0] + s * REF_EDGE[fl][1][0];
+        double ey = (1.0 - s) * REF_EDGE[fl][0][1] + s * REF_EDGE[fl][1][1];
+        double L[3] = {1.0 - ex - ey, ex, ey};
+        double xq = 0, yq = 0;
+        for (int a = 0; a < 3; ++a) {
+          xq += L[a] * m.xy[2 * (nd[a] - 1)];
+          yq += L[a] * m.xy[2 * (nd[a] - 1) + 1];
+        }
+        u += t.face.w[q] * eval_field(g, xq, yq) * t.T[i * nfq + q];
+      }
+      vals[k] = u;
       dofs[k] = fidx * nt - nt + (i + 1);
       ++k;
     }

@@ -63,6 +63,10 @@ def lib():
             L.hr_assemble.restype = vp
             L.hr_assemble.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, dp, C.c_int, C.c_int, dp,
                                       dp, C.c_int, ip]
+            L.hr_assemble_ex.restype = vp
+            L.hr_assemble_ex.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, dp, C.c_int, C.c_int,
+                                         dp, dp, C.c_int, C.c_int, ip]
+            L.hr_dirichlet_l2.argtypes = [vp, C.c_int, C.c_int, C.c_char_p, C.c_int, C.c_int, dp, ip, dp]
             L.hr_system_free.argtypes = [vp]
             L.hr_system_sizes.argtypes = [vp, ip, i64p, ip, ip]
             L.hr_system_csc.argtypes = [vp, i64p, i64p, dp, dp]
@@ -230,7 +234,8 @@ def element_blocks(mesh: Mesh, c: int, p: int, qd=None, tau=1.0, f=None):
 class System:
     """Assembled (condensed) trace system of the oracle: CSC K, rhs b, local K_e, b_e."""
 
-    def __init__(self, mesh: Mesh, p: int, qd=None, tau=1.0, f=None, kappa=None, kappa_cell=None, threads=1):
+    def __init__(self, mesh: Mesh, p: int, qd=None, tau=1.0, f=None, kappa=None, kappa_cell=None, threads=1,
+                 he_tau=False):
         self.mesh, self.p = mesh, p
         self.qd = p + 1 if qd is None else qd
         fk, fp = _field(f)
@@ -240,8 +245,8 @@ class System:
             kk, kp = -1, np.zeros(1)
         kc = None if kappa_cell is None else np.ascontiguousarray(kappa_cell, dtype=np.float64)
         st = C.c_int()
-        self.h = lib().hr_assemble(mesh.h, p, self.qd, tau, fk, fp.size, _dp(fp), kk, kp.size, _dp(kp), _dp(kc),
-                                   threads, C.byref(st))
+        self.h = lib().hr_assemble_ex(mesh.h, p, self.qd, tau, fk, fp.size, _dp(fp), kk, kp.size, _dp(kp), _dp(kc),
+                                      threads, 1 if he_tau else 0, C.byref(st))
         if not self.h:
             raise ValueError(f"oracle assembly failed ({st.value})")
         nd, nnz, n, m = C.c_int(), C.c_int64(), C.c_int(), C.c_int()
@@ -272,13 +277,15 @@ class System:
         lib().hr_system_local(self.h, _dp(Ke), _dp(be))
         return Ke, be
 
-    def dirichlet(self, faceset="boundary", g=None):
+    def dirichlet(self, faceset="boundary", g=None, projection="reference"):
+        """Trace Dirichlet dofs and values: the reference's accumulation, or (projection="l2") the
+        L2 projection of g onto the trace basis."""
         gk, gp = _field(g)
         n = len(self.mesh.faceset(faceset)) * self.nt
         dofs = np.zeros(max(n, 1), np.int32)
         vals = np.zeros(max(n, 1))
-        k = lib().hr_dirichlet(self.mesh.h, self.p, self.qd, faceset.encode(), gk, gp.size, _dp(gp), _ip(dofs),
-                               _dp(vals))
+        fn = lib().hr_dirichlet_l2 if projection == "l2" else lib().hr_dirichlet
+        k = fn(self.mesh.h, self.p, self.qd, faceset.encode(), gk, gp.size, _dp(gp), _ip(dofs), _dp(vals))
         if k < 0:
             raise ValueError(f"Dirichlet failed ({k})")
         return dofs[:k], vals[:k]

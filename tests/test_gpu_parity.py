@@ -33,18 +33,20 @@ def rel(a, b):
     return np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(np.asarray(b)).max(), 1e-300)
 
 
-def compare_system(H, oracle, mesh, omesh, p, qd=None, f=None, kappa=None, kappa_cell=None, tau=1.0, apply=True):
+def compare_system(H, oracle, mesh, omesh, p, qd=None, f=None, kappa=None, kappa_cell=None, tau=1.0, apply=True,
+                   g=None, projection="reference", he_tau=False):
     f = f or H.MANUFACTURED_F
     Vh, Wh, Mh = spaces(H, mesh, p, qd)
-    K, b, K_e, b_e = H.doassemble(Vh, Wh, Mh, tau, f, kappa=kappa, kappa_cell=kappa_cell)
-    S = oracle.System(omesh, p, qd, tau, f.as_oracle(), kappa.as_oracle() if kappa is not None else None, kappa_cell)
+    K, b, K_e, b_e = H.doassemble(Vh, Wh, Mh, tau, f, kappa=kappa, kappa_cell=kappa_cell, he_tau=he_tau)
+    S = oracle.System(omesh, p, qd, tau, f.as_oracle(), kappa.as_oracle() if kappa is not None else None, kappa_cell,
+                      he_tau=he_tau)
     Ate, bte, Ke, be = K.element_blocks()
     oKe, obe = S.local()
     assert rel(Ke, oKe) < RTOL_BLOCK
     assert rel(be, obe) < RTOL_BLOCK
     if apply:
-        dbc = H.Dirichlet(H.TrialFunction(Mh), mesh, "boundary")
-        od, ov = S.dirichlet()
+        dbc = H.Dirichlet(H.TrialFunction(Mh), mesh, "boundary", g, projection=projection)
+        od, ov = S.dirichlet("boundary", g.as_oracle() if g is not None else None, projection=projection)
         np.testing.assert_array_equal(dbc.prescribed_dofs, od)
         np.testing.assert_allclose(dbc.values, ov, atol=1e-15)
         H.apply_(K, b, dbc)
@@ -137,6 +139,49 @@ def test_convergence_rates(H):
             errs.append(math.sqrt(K.errornorm(H.MANUFACTURED_U)))
         rate = math.log2(errs[0] / errs[1])
         assert rate > p + 0.7, (p, errs, rate)
+
+
+def _half_sin(H):
+    """u = sin(pi x / 2) sin(pi y / 2), nonzero on x = 1 and y = 1, and f = -lap u."""
+    return H.Field.sinsin(1.0, 0.5, 0.5), H.Field.sinsin(0.5 * math.pi ** 2, 0.5, 0.5)
+
+
+@pytest.mark.parametrize("n,p,qd,tau", [(6, 1, None, 4.0), (5, 2, None, 0.25), (4, 3, 6, 10.0)])
+@pytest.mark.parametrize("projection,he_tau", [("l2", True), ("l2", False), ("reference", True)])
+def test_dirichlet_projection_and_he_tau_match_oracle(H, oracle, n, p, qd, tau, projection, he_tau):
+    """The corrected trace Dirichlet projection and tau in He against the oracle's same options,
+    with tau != 1 and nonzero boundary data."""
+    u_ex, f = _half_sin(H)
+    mesh = H.rectangle_mesh(H.TriangleCell, (n, n), (0.0, 0.0), (1.0, 1.0))
+    omesh = oracle.rectangle_mesh(n, n)
+    K, S, _ = compare_system(H, oracle, mesh, omesh, p, qd, f=f, tau=tau, g=u_ex, projection=projection,
+                             he_tau=he_tau)
+    if not he_tau and tau > 1:
+        # He without tau and tau > 1: the trace matrix is indefinite on the free dofs (the oracle's
+        # eigenvalues show positive ones), a system for a direct solver, not for CG
+        return
+    uhat = H.solve(K, None, tol=1e-14)
+    assert K.stats.converged
+    assert rel(uhat, S.solve()) < 1e-11
+
+
+def test_corrected_options_converge_with_boundary_data(H):
+    """tau = 4 and u != 0 on the boundary: with the L2 trace projection and tau in He the error
+    falls at rate p + 1, on the device.  (The reference's formulation gives an indefinite trace
+    matrix at this tau and no convergence; the oracle's tests show both.)"""
+    u_ex, f = _half_sin(H)
+    for p, qd in ((1, None), (2, None)):
+        e = []
+        for n in (8, 16):
+            mesh = H.rectangle_mesh(H.TriangleCell, (n, n), (0.0, 0.0), (1.0, 1.0))
+            Vh, Wh, Mh = spaces(H, mesh, p, qd)
+            K, b, _, _ = H.doassemble(Vh, Wh, Mh, 4.0, f, he_tau=True)
+            H.apply_(K, b, H.Dirichlet(H.TrialFunction(Mh), mesh, "boundary", u_ex, projection="l2"))
+            H.solve(K, b, tol=1e-13)
+            K.recover()
+            e.append(math.sqrt(K.errornorm(u_ex)))
+        assert math.log2(e[0] / e[1]) > p + 0.7, e
+        assert e[1] < 1e-3, e
 
 
 def test_deterministic(H):
@@ -450,3 +495,30 @@ def test_cg_poisson_path_matches_oracle(H, oracle, n, order, var):
     assert abs(err - eref) <= 1e-8 * eref
     if (n, order, var) == (10, 1, False):
         assert err <= 2e-4
+
+
+def test_cg_poisson_path_refuses_bad_inputs(H):
+    """doassemble_cg refuses a pattern that lacks an element coupling (HDG_ERR_ARG from
+    hdg_lagrange_create), an order whose DofHandler numbering is incomplete, and an inverted cell
+    (HDG_ERR_NEG_DETJ)."""
+    import scipy.sparse as sp
+    mesh = H.rectangle_mesh(H.TriangleCell, (4, 4), (0.0, 0.0), (1.0, 1.0))
+    Wh = H.ScalarFunctionSpace(mesh, H.ContinuousLagrange(2, H.RefTetrahedron, 1), update_face_data=False)
+    u_h = H.TrialFunction(Wh)
+    dh = H.DofHandler([u_h], mesh)
+    K = H.create_sparsity_pattern(dh)
+    diag_only = sp.identity(K.shape[0], format="csc")
+    with pytest.raises(H.HDGError):
+        H.doassemble_cg(Wh, diag_only, dh, H.MANUFACTURED_F)
+    W3 = H.ScalarFunctionSpace(mesh, H.ContinuousLagrange(2, H.RefTetrahedron, 3), update_face_data=False)
+    u3 = H.TrialFunction(W3)
+    dh3 = H.DofHandler([u3], mesh)
+    with pytest.raises(NotImplementedError):
+        H.doassemble_cg(W3, H.create_sparsity_pattern(dh3), dh3, H.MANUFACTURED_F)
+    xy = mesh._topology()[0].copy()
+    cn = mesh._topology()[1]
+    a, b = cn[0, 1] - 1, cn[0, 2] - 1
+    xy[[a, b]] = xy[[b, a]]          # swap two vertices of the first cell: it turns inside out
+    mesh.set_coordinates(xy)
+    with pytest.raises(H.HDGError):
+        H.doassemble_cg(Wh, K, dh, H.MANUFACTURED_F)

@@ -135,3 +135,41 @@ def test_trace_system_structure(oracle):
     free = np.setdiff1d(np.arange(S.ndofs), dofs - 1)
     ev = np.linalg.eigvalsh(A[np.ix_(free, free)])
     assert ev.max() < 0
+
+
+def test_l2_trace_projection_is_exact_for_polynomials(oracle):
+    """projection="l2" reproduces a constant g on every boundary face (the trace basis is orthonormal
+    on [0, 1] with a constant first function); the reference's accumulation does not."""
+    m = oracle.rectangle_mesh(3, 2, (0.0, 0.0), (2.0, 1.0))
+    for p in (1, 2, 3):
+        S = oracle.System(m, p, f=oracle.MANUFACTURED_F)
+        d, v = S.dirichlet("boundary", (oracle.F_CONST, [0.7]), projection="l2")
+        v = v.reshape(-1, p + 1)
+        # a constant on the face is 0.7 times the first (constant, unit) basis function
+        np.testing.assert_allclose(v[:, 0], 0.7, rtol=1e-14)
+        np.testing.assert_allclose(v[:, 1:], 0.0, atol=1e-14)
+        d0, v0 = S.dirichlet("boundary", (oracle.F_CONST, [0.7]))
+        np.testing.assert_array_equal(d, d0)
+        assert np.abs(v0.reshape(-1, p + 1) - v).max() > 1e-3
+
+
+def test_corrected_formulation_converges_with_boundary_data(oracle):
+    """tau = 4, u = sin(pi x / 2) sin(pi y / 2) (nonzero on x = 1, y = 1): the reference's trace
+    projection (src/boundary.jl:232-242) and He without tau (examples/poisson2D_HDG.jl:149) give no
+    convergence; the L2 projection with tau in He gives rate p + 1."""
+    u = (oracle.F_SINSIN, [1.0, 0.5, 0.5])
+    f = (oracle.F_SINSIN, [0.5 * np.pi ** 2, 0.5, 0.5])
+    for p in (1, 2):
+        err = {}
+        for fixed in (False, True):
+            e = []
+            for n in (4, 8):
+                m = oracle.rectangle_mesh(n, n)
+                S = oracle.System(m, p, None, 4.0, f, he_tau=fixed)
+                d, v = S.dirichlet("boundary", u, projection="l2" if fixed else "reference")
+                S.apply(d, v)
+                _, uu, _ = S.recover(S.solve())
+                e.append(np.sqrt(oracle.errornorm(m, p, uu, u)))
+            err[fixed] = e
+        assert np.log2(err[True][0] / err[True][1]) > p + 0.7, err
+        assert min(err[False]) > 0.2, err
