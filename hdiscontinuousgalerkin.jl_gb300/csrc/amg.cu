@@ -36,6 +36,8 @@
 #include <cstdlib>
 #include <numeric>
 
+#include <cuda_fp16.h>
+
 #include "hdg_device.cuh"
 
 namespace {
@@ -194,7 +196,8 @@ struct AmgHierarchy {
   DevBuf<float> dinv0;       // [nf][nt][nt]
   DevBuf<float> lam0;        // [nprob] Gershgorin bound of D^-1 A0
   DevBuf<int32_t> face_prob; // [nf]
-  DevBuf<float> val0f;       // FP32 trace matrix; after the numeric set-up D^-1 A0 (block rows scaled)
+  DevBuf<float> val0f;       // FP32 trace matrix (set-up products); with FP32 cycle storage, D^-1 A0 afterwards
+  DevBuf<__half> val0h;      // D^-1 A0 in FP16, read by the cycle's level-0 sweeps (default storage)
   DevBuf<float> x0, r0, d0;  // level-0 cycle vectors (iterate, scaled residual, Chebyshev correction)
   DevBuf<float> bt0;         // D^-1 b of the current cycle
   DevBuf<float> dpval0;      // [nf*nt][PW] D P0 (restriction of the scaled residual)
@@ -793,10 +796,20 @@ __global__ void k_amg_dp0(int nf, const int8_t* __restrict__ kdiag, const float*
     }
 }
 
-// A0 -> D^-1 A0 in place, block row by block row (each face rewrites only its own rows).  Runs
-// after every set-up product that needs A0 itself; the cycle then needs no D^-1 per sweep.
-template <int NT>
-__global__ void k_amg_scale0(int nf, const float* __restrict__ dinv, float* __restrict__ val) {
+// Level-0 value storage of the cycle: FP32 or FP16, read as FP32.
+template <typename VT> __device__ __forceinline__ VT to_vt(float v);
+template <> __device__ __forceinline__ float to_vt<float>(float v) { return v; }
+template <> __device__ __forceinline__ __half to_vt<__half>(float v) { return __float2half_rn(v); }
+__device__ __forceinline__ float ldv(const float* p) { return *p; }
+__device__ __forceinline__ float ldv(const __half* p) { return __half2float(*p); }
+
+// A0 -> D^-1 A0, block row by block row, into `out` (FP32, which may be `val` itself: each face
+// reads and rewrites only its own rows, or FP16).  Runs after every set-up product that needs A0
+// itself; the cycle then needs no D^-1 per sweep.  The scaled diagonal block is I and the
+// off-diagonal entries are of order one, well inside FP16's range; the rounding (2^-11 relative)
+// changes the preconditioner, not the FP64 Krylov iteration around it.
+template <int NT, typename VT>
+__global__ void k_amg_scale0(int nf, const float* __restrict__ dinv, const float* val, VT* out) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
   const int64_t nd = (int64_t)nf * NT;
@@ -810,7 +823,7 @@ __global__ void k_amg_scale0(int nf, const float* __restrict__ dinv, float* __re
       for (int i = 0; i < NT; ++i) {
         float s = 0.f;
         for (int l = 0; l < NT; ++l) s += di[i][l] * col[l];
-        val[(k * NT + j) * nd + (int64_t)f * NT + i] = s;
+        out[(k * NT + j) * nd + (int64_t)f * NT + i] = to_vt<VT>(s);
       }
     }
 }
@@ -831,8 +844,8 @@ __device__ __forceinline__ bool amg_live(const int32_t* __restrict__ st, int P) 
 // Gershgorin bound.  xin == NULL stands for x = 0 (no product); d holds the previous step's
 // correction and is updated in place (each face reads and writes only its own rows of d).
 constexpr float CHEB_RATIO = 30.f;
-template <int NT>
-__global__ void k_amg_face_cheb(int nf, const int32_t* __restrict__ bcol5, const float* __restrict__ val,
+template <int NT, typename VT>
+__global__ void k_amg_face_cheb(int nf, const int32_t* __restrict__ bcol5, const VT* __restrict__ val,
                                 const float* __restrict__ dinv, const float* __restrict__ lam,
                                 const int32_t* __restrict__ face_prob, const float* __restrict__ b,
                                 float* __restrict__ bt, const float* __restrict__ xin, float* __restrict__ xout,
@@ -864,7 +877,7 @@ __global__ void k_amg_face_cheb(int nf, const int32_t* __restrict__ bcol5, const
       seen[ns++] = g;
       for (int j = 0; j < NT; ++j) {
         const float xv = xin[(int64_t)g * NT + j];
-        for (int i = 0; i < NT; ++i) t[i] -= val[(k * NT + j) * nd + (int64_t)f * NT + i] * xv;
+        for (int i = 0; i < NT; ++i) t[i] -= ldv(&val[(k * NT + j) * nd + (int64_t)f * NT + i]) * xv;
       }
     }
   }
@@ -884,8 +897,8 @@ __global__ void k_amg_face_cheb(int nf, const int32_t* __restrict__ bcol5, const
   }
 }
 
-template <int NT>
-__global__ void k_amg_row_cheb(int nf, const int32_t* __restrict__ bcol5, const float* __restrict__ val,
+template <int NT, typename VT>
+__global__ void k_amg_row_cheb(int nf, const int32_t* __restrict__ bcol5, const VT* __restrict__ val,
                                 const float* __restrict__ dinv, const float* __restrict__ lam,
                                 const int32_t* __restrict__ face_prob, const float* __restrict__ b,
                                 float* __restrict__ bt, const float* __restrict__ xin, float* __restrict__ xout,
@@ -916,7 +929,7 @@ __global__ void k_amg_row_cheb(int nf, const int32_t* __restrict__ bcol5, const 
       for (int u = 0; u < ns; ++u) dup |= (seen[u] == g);
       if (dup) continue;
       seen[ns++] = g;
-      for (int j = 0; j < NT; ++j) t -= val[(k * NT + j) * nd + row] * xin[(int64_t)g * NT + j];
+      for (int j = 0; j < NT; ++j) t -= ldv(&val[(k * NT + j) * nd + row]) * xin[(int64_t)g * NT + j];
     }
   }
   const float hi = fmaxf(lam[face_prob[f]], 1e-30f), lo = hi / CHEB_RATIO;
@@ -933,8 +946,8 @@ __global__ void k_amg_row_cheb(int nf, const int32_t* __restrict__ bcol5, const 
 }
 
 // scaled residual r~ = D^-1 (b - A0 x) = bt - (D^-1 A0) x (level 0); the restriction uses D P0
-template <int NT>
-__global__ void k_amg_face_residual(int nf, const int32_t* __restrict__ bcol5, const float* __restrict__ val,
+template <int NT, typename VT>
+__global__ void k_amg_face_residual(int nf, const int32_t* __restrict__ bcol5, const VT* __restrict__ val,
                                     const float* __restrict__ b, const float* __restrict__ x, float* __restrict__ r,
                                     const int32_t* __restrict__ face_prob, const int32_t* __restrict__ st) {
   const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -951,7 +964,7 @@ __global__ void k_amg_face_residual(int nf, const int32_t* __restrict__ bcol5, c
     for (int t = 0; t < ns; ++t) dup |= (seen[t] == g);
     if (dup) continue;
     seen[ns++] = g;
-    for (int j = 0; j < NT; ++j) s -= val[(k * NT + j) * nd + row] * x[(int64_t)g * NT + j];
+    for (int j = 0; j < NT; ++j) s -= ldv(&val[(k * NT + j) * nd + row]) * x[(int64_t)g * NT + j];
   }
   r[row] = s;
 }
@@ -1107,6 +1120,16 @@ int amg_coarse_sweeps() {
   return k;
 }
 
+// Storage of the scaled level-0 matrix that the cycle reads: FP16 (default; half the bytes of
+// the dominant sweeps) or FP32 (HDG_AMG_LEVEL0_FP32=1).
+bool amg_level0_fp32() {
+  static const bool v = [] {
+    const char* e = std::getenv("HDG_AMG_LEVEL0_FP32");
+    return e && std::atoi(e) != 0;
+  }();
+  return v;
+}
+
 int amg_cheb_degree() {
   static const int k = [] {
     const char* e = std::getenv("HDG_AMG_CHEB_DEGREE");
@@ -1142,7 +1165,12 @@ template <int NT> void numeric_nt(hdg_system* s, const float* val0, cudaStream_t
   k_amg_rap0<NT><<<nblk(L1.n), 256, 0, st>>>(L1.n, H->wap, H->rptr0.p, H->rent0.p, H->pval0.p, H->apcol0.p,
                                              H->apval0.p, L1.ptr.p, L1.col.p, L1.val.p);
   k_amg_dp0<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_kdiag.p, val0, H->pval0.p, H->dpval0.p);
-  k_amg_scale0<NT><<<nblk(nf), 256, 0, st>>>(nf, H->dinv0.p, const_cast<float*>(val0));
+  if (amg_level0_fp32()) {
+    k_amg_scale0<NT, float><<<nblk(nf), 256, 0, st>>>(nf, H->dinv0.p, val0, const_cast<float*>(val0));
+  } else {
+    H->val0h.alloc((size_t)hdg_system::SLOTS * NT * NT * nf);
+    k_amg_scale0<NT, __half><<<nblk(nf), 256, 0, st>>>(nf, H->dinv0.p, val0, H->val0h.p);
+  }
   s->ctx->launches += 6;
   for (size_t l = 0; l < H->lev.size(); ++l) {
     AmgLevel& L = H->lev[l];
@@ -1175,22 +1203,22 @@ template <int NT> void numeric_nt(hdg_system* s, const float* val0, cudaStream_t
 // sizes), a thread per face above.  Measured: 49 k faces (p = 4): rows 15 -> 10 us per sweep;
 // 197 k faces (p = 2) and the batch's bins (0.4-0.7 M faces): faces faster.
 constexpr int AMG_ROW_SWEEP_FACES = 100000;
-template <int NT>
-void cheb_sweep(hdg_system* s, const float* val0, const float* b0, const float* in, float* out, int step,
+template <int NT, typename VT>
+void cheb_sweep(hdg_system* s, const VT* val0, const float* b0, const float* in, float* out, int step,
                 const int32_t* cst, cudaStream_t st) {
   AmgHierarchy* H = s->amg;
   const int nf = H->nf;
   if (nf < AMG_ROW_SWEEP_FACES)
-    k_amg_row_cheb<NT><<<nblk((int64_t)nf * NT), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p,
+    k_amg_row_cheb<NT, VT><<<nblk((int64_t)nf * NT), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p,
                                                               H->face_prob.p, b0, H->bt0.p, in, out, H->d0.p, step,
                                                               cst);
   else
-    k_amg_face_cheb<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
+    k_amg_face_cheb<NT, VT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
                                                   H->bt0.p, in, out, H->d0.p, step, cst);
 }
 
-template <int NT>
-void apply_nt(hdg_system* s, const float* val0, const float* b0, float* z0, const int32_t* cst, cudaStream_t st) {
+template <int NT, typename VT>
+void apply_nt(hdg_system* s, const VT* val0, const float* b0, float* z0, const int32_t* cst, cudaStream_t st) {
   AmgHierarchy* H = s->amg;
   const int nf = H->nf;
   const int64_t n0 = (int64_t)nf * NT;
@@ -1201,9 +1229,9 @@ void apply_nt(hdg_system* s, const float* val0, const float* b0, float* z0, cons
   for (int t = 0; t < k; ++t) {
     float* out = ((k - 1 - t) % 2 == 0) ? z0 : H->x0.p;
     const float* in = (t == 0) ? nullptr : (out == z0 ? H->x0.p : z0);
-    cheb_sweep<NT>(s, val0, b0, in, out, t, cst, st);
+    cheb_sweep<NT, VT>(s, val0, b0, in, out, t, cst, st);
   }
-  k_amg_face_residual<NT><<<nblk(n0), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->bt0.p, z0, H->r0.p, H->face_prob.p,
+  k_amg_face_residual<NT, VT><<<nblk(n0), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->bt0.p, z0, H->r0.p, H->face_prob.p,
                                                     cst);
   AmgLevel& L1 = H->lev[0];
   k_amg_restrict0<NT><<<nblk(L1.n), 256, 0, st>>>(L1.n, H->rptr0.p, H->rent0.p, H->dpval0.p, H->r0.p, L1.dl1inv.p,
@@ -1251,7 +1279,7 @@ void apply_nt(hdg_system* s, const float* val0, const float* b0, float* z0, cons
   for (int t = 0; t < k; ++t) {
     const float* in = (t % 2 == 0) ? z0 : H->x0.p;
     float* out = (t % 2 == 0) ? H->x0.p : z0;
-    cheb_sweep<NT>(s, val0, b0, in, out, t, cst, st);
+    cheb_sweep<NT, VT>(s, val0, b0, in, out, t, cst, st);
   }
   if (k % 2 == 1) HDG_CUDA(cudaMemcpyAsync(z0, H->x0.p, sizeof(float) * n0, cudaMemcpyDeviceToDevice, st));
 }
@@ -1272,14 +1300,15 @@ void amg_setup_numeric(hdg_system* s, cudaStream_t st) {
 }
 
 // Algorithmic bytes of one V-cycle: every array a cycle kernel reads or writes, once (gathered
-// neighbour values are counted at their own row).  Level 0: the FP32 block-ELL values, block
+// neighbour values are counted at their own row).  Level 0: the block-ELL values (FP16 or FP32), block
 // columns, block inverses and vectors of the four matrix-touching sweeps (second pre-sweep,
 // residual, two post-sweeps), the first sweep, restriction and prolongation; coarse levels: their
 // CSR matrices and vectors in the same sweeps.
 double amg_cycle_bytes(const hdg_system* s) {
   const AmgHierarchy* H = s->amg;
   const double nf = H->nf, nt = H->nt, n0 = nf * nt, n1 = H->lev.empty() ? 0.0 : H->lev[0].n;
-  const double mat0 = 20.0 * nt * nt * nf + 20.0 * nf;  // FP32 values + block columns
+  const double vb = H->val0h.p ? 2.0 : 4.0;             // FP16 or FP32 level-0 values
+  const double mat0 = 5.0 * vb * nt * nt * nf + 20.0 * nf;  // values + block columns
   const double dinv = 4.0 * nt * nt * nf;
   const int k = amg_cheb_degree();
   double b = 16.0 * n0 + dinv;                             // first sweep: b, D^-1 -> bt, x, d
@@ -1310,14 +1339,21 @@ int amg_cycle_launches(const hdg_system* s) {
   return (k + 2) + (nu + 1) * (nl - 1) + 1 + (nu + 1) * (nl - 1) + (1 + k);
 }
 
-void amg_apply(hdg_system* s, const float* r, float* z, const int32_t* cg_state, cudaStream_t st) {
-  const float* v0 = s->amg->val0f.p ? s->amg->val0f.p : s->d_valf.p;
+template <typename VT> void apply_dispatch(hdg_system* s, const VT* v0, const float* r, float* z,
+                                           const int32_t* cg_state, cudaStream_t st) {
   switch (s->nt) {
-    case 2: apply_nt<2>(s, v0, r, z, cg_state, st); break;
-    case 3: apply_nt<3>(s, v0, r, z, cg_state, st); break;
-    case 4: apply_nt<4>(s, v0, r, z, cg_state, st); break;
-    case 5: apply_nt<5>(s, v0, r, z, cg_state, st); break;
+    case 2: apply_nt<2, VT>(s, v0, r, z, cg_state, st); break;
+    case 3: apply_nt<3, VT>(s, v0, r, z, cg_state, st); break;
+    case 4: apply_nt<4, VT>(s, v0, r, z, cg_state, st); break;
+    case 5: apply_nt<5, VT>(s, v0, r, z, cg_state, st); break;
   }
+}
+
+void amg_apply(hdg_system* s, const float* r, float* z, const int32_t* cg_state, cudaStream_t st) {
+  if (s->amg->val0h.p)
+    apply_dispatch<__half>(s, s->amg->val0h.p, r, z, cg_state, st);
+  else
+    apply_dispatch<float>(s, s->amg->val0f.p, r, z, cg_state, st);
   HDG_CUDA(cudaGetLastError());
 }
 
