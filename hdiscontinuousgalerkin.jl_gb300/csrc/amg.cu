@@ -867,14 +867,12 @@ __global__ void k_amg_face_cheb(int nf, const int32_t* __restrict__ bcol5, const
     }
   } else {
     for (int i = 0; i < NT; ++i) t[i] = bt[(int64_t)f * NT + i];
-    int seen[5];
-    int ns = 0;
+    // padding slots (faces with fewer than four neighbours) repeat the face with zero values,
+    // so every slot is summed without a test and all loads can be issued up front
+#pragma unroll
     for (int k = 0; k < 5; ++k) {
       const int g = bcol5[k * nf + f];
-      bool dup = false;
-      for (int u = 0; u < ns; ++u) dup |= (seen[u] == g);
-      if (dup) continue;
-      seen[ns++] = g;
+#pragma unroll
       for (int j = 0; j < NT; ++j) {
         const float xv = xin[(int64_t)g * NT + j];
         for (int i = 0; i < NT; ++i) t[i] -= ldv(&val[(k * NT + j) * nd + (int64_t)f * NT + i]) * xv;
@@ -921,14 +919,11 @@ __global__ void k_amg_row_cheb(int nf, const int32_t* __restrict__ bcol5, const 
     bt[row] = t;
   } else {
     t = bt[row];
-    int seen[5];
-    int ns = 0;
+    // padding slots repeat the face with zero values: no test needed
+#pragma unroll
     for (int k = 0; k < 5; ++k) {
       const int g = bcol5[k * nf + f];
-      bool dup = false;
-      for (int u = 0; u < ns; ++u) dup |= (seen[u] == g);
-      if (dup) continue;
-      seen[ns++] = g;
+#pragma unroll
       for (int j = 0; j < NT; ++j) t -= ldv(&val[(k * NT + j) * nd + row]) * xin[(int64_t)g * NT + j];
     }
   }
@@ -956,14 +951,11 @@ __global__ void k_amg_face_residual(int nf, const int32_t* __restrict__ bcol5, c
   const int f = (int)(row / NT);
   if (!amg_live(st, face_prob[f])) return;
   float s = b[row];
-  int seen[5];
-  int ns = 0;
+  // padding slots repeat the face with zero values: no test needed
+#pragma unroll
   for (int k = 0; k < 5; ++k) {
     const int g = bcol5[k * nf + f];
-    bool dup = false;
-    for (int t = 0; t < ns; ++t) dup |= (seen[t] == g);
-    if (dup) continue;
-    seen[ns++] = g;
+#pragma unroll
     for (int j = 0; j < NT; ++j) s -= ldv(&val[(k * NT + j) * nd + row]) * x[(int64_t)g * NT + j];
   }
   r[row] = s;
@@ -1103,11 +1095,13 @@ __global__ void k_amg_coarse_solve(const int32_t* __restrict__ crow0, const int3
 
 inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)std::max<int64_t>(1, (n + t - 1) / t); }
 
-// Degree of the level-0 Chebyshev smoother (HDG_AMG_CHEB_DEGREE, 1..4, default 3): each degree
+// Degree of the level-0 Chebyshev smoother (HDG_AMG_CHEB_DEGREE, 1..4, default 4): each degree
 // beyond 1 adds a matrix sweep before and after the coarse correction.  Measured on the
-// 256-problem batch (kappa contrast 1e4, tol 1e-9): degree 1/2/3 took 754/474/359 iterations at
-// most and gave 302/367/398 solves/s; on the 131072-cell p=2 problem with kappa = 1, degree 2 was
-// 5 % faster than 3 (103 vs 99 iterations).
+// 256-problem batch (kappa contrast 1e4, tol 1e-9) with the FP32 level-0 copy: degree 1/2/3
+// took 754/474/359 iterations at most and gave 302/367/398 solves/s; with the FP16 copy, which
+// makes a sweep cheaper, degree 2/3/4 took 474/359/313 iterations and gave 410/447/461 solves/s.
+// On the 131072-cell p=2 problem with kappa = 1, degree 2 was 5 % faster than 3 (103 vs 99
+// iterations).
 // l1-Jacobi sweeps before and after the coarse correction on each coarse level
 // (HDG_AMG_COARSE_SWEEPS, 1..4, default 2).  On the 256-problem batch 1/2/3 sweeps gave
 // 406/418/415 solves/s (396/359/349 iterations for the hardest problem).
@@ -1133,8 +1127,8 @@ bool amg_level0_fp32() {
 int amg_cheb_degree() {
   static const int k = [] {
     const char* e = std::getenv("HDG_AMG_CHEB_DEGREE");
-    const int v = e ? std::atoi(e) : 3;
-    return (v >= 1 && v <= 4) ? v : 3;
+    const int v = e ? std::atoi(e) : 4;
+    return (v >= 1 && v <= 4) ? v : 4;
   }();
   return k;
 }
