@@ -407,7 +407,7 @@ def draw_coefficients(H, rng, n):
 
 
 def run_c5(args, ws, rank, local):
-    """Serving workload: a Poisson stream of solve requests (2000 req/s, seeded); each request is
+    """Serving workload: a Poisson stream of solve requests (2000 req/s by default, seeded); each request is
     drawn like the batching workload; 70 % reuse one of 32 resident meshes with a new source and
     coefficient, 30 % come with a new mesh.  The engine admits by HBM budget, runs flights on
     separate streams and completes requests as their flights converge."""
@@ -421,7 +421,9 @@ def run_c5(args, ws, rank, local):
     ctx = H.Context(local)
     tol = args.tol if args.tol != 1e-12 else 1e-9
     nreq = args.requests
-    rate = 2000.0
+    rate = args.rate
+    if not rate > 0:
+        raise SystemExit("--rate must be positive")
     rng = np.random.default_rng(777 + rank)
     resident = []
     for k in range(32):
@@ -532,7 +534,7 @@ def run_c5(args, ws, rank, local):
         "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * (t_last - first) / nreq, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64",
         "data": "synthetic",
-        "config": {"workload": "c5: Poisson request stream at 2000 req/s (seeded), each drawn like the batching "
+        "config": {"workload": f"c5: Poisson request stream at {rate:g} req/s (seeded), each drawn like the batching "
                                "workload; 70% on one of 32 resident meshes with a new source and kappa, 30% new meshes;"
                                f" continuous batching, {args.precision}, {args.preconditioner}-preconditioned CG "
                                f"tol {tol:g}",
@@ -669,6 +671,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c4", choices=sorted(WORKLOADS) + ["c3", "c4", "c5", "cg"])
     ap.add_argument("--requests", type=int, default=2000)
+    ap.add_argument("--rate", type=float, default=2000.0,
+                    help="c5 only: mean arrival rate in requests/s (2000 is the workload; lower rates show latency "
+                         "without queueing)")
     ap.add_argument("--hbm-budget-gb", type=float, default=64.0)
     ap.add_argument("--max-batch", type=int, default=64)
     ap.add_argument("--max-flights", type=int, default=8)
