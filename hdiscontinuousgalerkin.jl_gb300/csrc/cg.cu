@@ -938,19 +938,27 @@ int run_batch_step(const std::vector<hdg_system*>& sys, const hdg_solver& o, int
         HDG_CUDA(cudaStreamWaitEvent(fork.home, start, 0));
       }
     HDG_CUDA(cudaEventRecord(start, fork.home));
-    // The system with the most element work (the FP64-bound condensation of the highest degree)
-    // heads the critical path: its stream gets the greatest priority, so its element kernel is
-    // not starved of SM slots by the other systems' iteration kernels.
+    // One system gets the greatest stream priority: the one on the longest chain of dependent
+    // launches.  When the systems have been solved before (a batch stepped again with new data),
+    // that is the one whose hardest problem took the most CG iterations; otherwise the one with
+    // the most element work (the FP64-bound condensation of the highest degree), whose element
+    // kernel would otherwise be starved of SM slots by the other systems' iteration kernels.
+    // Measured on the 256-problem batch: 490 solves/s with the element-work rule alone, 504 with
+    // the bin of the most iterations raised, 503 with all bins ranked by their iterations.
     int prio_lo = 0, prio_hi = 0;
     HDG_CUDA(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
-    size_t crit = 0;
+    bool seen_all = true;
+    for (auto* s : sys) seen_all = seen_all && s->last_max_iters > 0;
     auto elem_work = [&](size_t i) { return (double)sys[i]->nc * sys[i]->n * sys[i]->n * (sys[i]->m + 1); };
+    size_t crit = 0;
     for (size_t i = 1; i < ns; ++i)
-      if (elem_work(i) > elem_work(crit)) crit = i;
+      if (seen_all ? sys[i]->last_max_iters > sys[crit]->last_max_iters : elem_work(i) > elem_work(crit)) crit = i;
+    std::vector<int> prio(ns, prio_lo);
+    prio[crit] = prio_hi;
     for (size_t i = 0; i < ns; ++i) {
       cudaStream_t qs;
       cudaEvent_t e;
-      HDG_CUDA(cudaStreamCreateWithPriority(&qs, cudaStreamNonBlocking, i == crit ? prio_hi : prio_lo));
+      HDG_CUDA(cudaStreamCreateWithPriority(&qs, cudaStreamNonBlocking, prio[i]));
       fork.streams.push_back(qs);
       HDG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
       fork.events.push_back(e);
@@ -1009,6 +1017,8 @@ int run_batch_step(const std::vector<hdg_system*>& sys, const hdg_solver& o, int
       if (sv[i]->process(o)) {
         sv[i]->finish(o, &(*stats)[i]);
         hdg_system* s = sys[i];
+        s->last_max_iters = 0;
+        for (auto& r : (*stats)[i]) s->last_max_iters = std::max(s->last_max_iters, r.iterations);
         if (flags & HDG_STEP_RECOVER) {
           if (s->ctx->profiling) s->ev_recover.start(q[i]);
           launch_recover(s, q[i]);

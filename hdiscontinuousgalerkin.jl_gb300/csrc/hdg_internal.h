@@ -305,6 +305,7 @@ struct hdg_system {
   CgState* cg = nullptr;
   AmgHierarchy* amg = nullptr;      // multigrid preconditioner (symbolic part kept across reassembly)
   int amg_gen = 0;                  // count of symbolic setups (captured CG graphs hold their buffers)
+  int last_max_iters = 0;           // most CG iterations of any problem in the last solve (scheduling hint)
   std::vector<char> h_dir_face;     // faces whose dofs apply! prescribed (set by hdg_apply_dirichlet)
   ~hdg_system();
   // partials: 2 per segment; tickets: 4 per problem (CG product, CG update, residual, meandiag)
