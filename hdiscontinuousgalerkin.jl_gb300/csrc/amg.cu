@@ -840,16 +840,15 @@ __device__ __forceinline__ bool amg_live(const int32_t* __restrict__ st, int P) 
 
 
 // Level-0 smoother: step `step` of the Chebyshev iteration (Saad, Iterative Methods, 12.3) for
-// D^-1 A0 on [lambda / CHEB_RATIO, lambda], D the face-block diagonal and lambda the problem's
+// D^-1 A0 on [lambda / ratio, lambda], D the face-block diagonal and lambda the problem's
 // Gershgorin bound.  xin == NULL stands for x = 0 (no product); d holds the previous step's
 // correction and is updated in place (each face reads and writes only its own rows of d).
-constexpr float CHEB_RATIO = 30.f;
 template <int NT, typename VT>
 __global__ void k_amg_face_cheb(int nf, const int32_t* __restrict__ bcol5, const VT* __restrict__ val,
                                 const float* __restrict__ dinv, const float* __restrict__ lam,
                                 const int32_t* __restrict__ face_prob, const float* __restrict__ b,
                                 float* __restrict__ bt, const float* __restrict__ xin, float* __restrict__ xout,
-                                float* __restrict__ d, int step, const int32_t* __restrict__ st) {
+                                float* __restrict__ d, int step, float ratio, const int32_t* __restrict__ st) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf || !amg_live(st, face_prob[f])) return;
   const int64_t nd = (int64_t)nf * NT;
@@ -879,7 +878,7 @@ __global__ void k_amg_face_cheb(int nf, const int32_t* __restrict__ bcol5, const
       }
     }
   }
-  const float hi = fmaxf(lam[face_prob[f]], 1e-30f), lo = hi / CHEB_RATIO;
+  const float hi = fmaxf(lam[face_prob[f]], 1e-30f), lo = hi / ratio;
   const float theta = 0.5f * (hi + lo), delta = 0.5f * (hi - lo), sigma = theta / delta;
   float rp = 1.f / sigma, rc = rp;  // rho_{step-1}, rho_step
   for (int u = 1; u <= step; ++u) {
@@ -900,7 +899,7 @@ __global__ void k_amg_row_cheb(int nf, const int32_t* __restrict__ bcol5, const 
                                 const float* __restrict__ dinv, const float* __restrict__ lam,
                                 const int32_t* __restrict__ face_prob, const float* __restrict__ b,
                                 float* __restrict__ bt, const float* __restrict__ xin, float* __restrict__ xout,
-                                float* __restrict__ d, int step, const int32_t* __restrict__ st) {
+                                float* __restrict__ d, int step, float ratio, const int32_t* __restrict__ st) {
   // one thread per row (f, i): with the block rows scaled by D^-1 the rows of a face are
   // independent.  For small systems (too few faces to fill the GPU) this runs nt times more
   // threads than the face kernel; on large ones it re-reads each face's columns and neighbour
@@ -927,7 +926,7 @@ __global__ void k_amg_row_cheb(int nf, const int32_t* __restrict__ bcol5, const 
       for (int j = 0; j < NT; ++j) t -= ldv(&val[(k * NT + j) * nd + row]) * xin[(int64_t)g * NT + j];
     }
   }
-  const float hi = fmaxf(lam[face_prob[f]], 1e-30f), lo = hi / CHEB_RATIO;
+  const float hi = fmaxf(lam[face_prob[f]], 1e-30f), lo = hi / ratio;
   const float theta = 0.5f * (hi + lo), delta = 0.5f * (hi - lo), sigma = theta / delta;
   float rp = 1.f / sigma, rc = rp;  // rho_{step-1}, rho_step
   for (int u = 1; u <= step; ++u) {
@@ -1124,6 +1123,23 @@ bool amg_level0_fp32() {
   return v;
 }
 
+// The Chebyshev interval is [lambda / ratio, lambda].  A wider interval damps more of the smooth
+// error that the matrix-independent face aggregates leave behind where kappa jumps; with a
+// constant kappa it smooths the high end less well.  Measured (degree 4): on the 256-problem
+// batch (kappa per cell over four decades) ratios 12/20/30/60/120/250/500 gave
+// 462/490/507/528/538/538/533 solves/s; on the 131072-cell p=2 problem with kappa = 1, 30 gave
+// 38.0 solves/s (95 iterations) and 120 gave 33.3 (113).  So 120 for systems with a variable
+// kappa, 30 otherwise; HDG_AMG_CHEB_RATIO (2..1000) sets one value for all.
+float amg_cheb_ratio(const hdg_system* s) {
+  static const float env = [] {
+    const char* e = std::getenv("HDG_AMG_CHEB_RATIO");
+    const float r = e ? (float)std::atof(e) : 0.f;
+    return (r >= 2.f && r <= 1000.f) ? r : 0.f;
+  }();
+  if (env > 0.f) return env;
+  return (s->kappa_cells || s->kappa_field) ? 120.f : 30.f;
+}
+
 int amg_cheb_degree() {
   static const int k = [] {
     const char* e = std::getenv("HDG_AMG_CHEB_DEGREE");
@@ -1205,10 +1221,10 @@ void cheb_sweep(hdg_system* s, const VT* val0, const float* b0, const float* in,
   if (nf < AMG_ROW_SWEEP_FACES)
     k_amg_row_cheb<NT, VT><<<nblk((int64_t)nf * NT), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p,
                                                               H->face_prob.p, b0, H->bt0.p, in, out, H->d0.p, step,
-                                                              cst);
+                                                              amg_cheb_ratio(s), cst);
   else
     k_amg_face_cheb<NT, VT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
-                                                  H->bt0.p, in, out, H->d0.p, step, cst);
+                                                  H->bt0.p, in, out, H->d0.p, step, amg_cheb_ratio(s), cst);
 }
 
 template <int NT, typename VT>
