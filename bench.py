@@ -557,7 +557,7 @@ CG_DESC = ("cg: examples/poisson2D_CG.jl scaled: -div grad u = 2 pi^2 sin(pi x) 
 
 
 def run_cg(args, ws, rank, local):
-    """The continuous-Galerkin Poisson path (the survey's next row): element loop and assemble!
+    """The continuous-Galerkin Poisson path (examples/poisson2D_CG.jl): element loop and assemble!
     into the DofHandler's CSC pattern, apply!, Jacobi-PCG and errornorm, on the device."""
     import numpy as np
     import torch
