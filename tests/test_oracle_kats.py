@@ -173,3 +173,18 @@ def test_corrected_formulation_converges_with_boundary_data(oracle):
             err[fixed] = e
         assert np.log2(err[True][0] / err[True][1]) > p + 0.7, err
         assert min(err[False]) > 0.2, err
+
+
+def test_he_tau_option_is_the_reference_at_tau_one(oracle):
+    """tau in He changes nothing at tau = 1 (the reference's setting) and changes Ate otherwise."""
+    m = oracle.rectangle_mesh(3, 3)
+    for p in (1, 2):
+        K0, b0 = oracle.System(m, p, f=oracle.MANUFACTURED_F).csc()
+        K1, b1 = oracle.System(m, p, f=oracle.MANUFACTURED_F, he_tau=True).csc()
+        assert abs(K0 - K1).max() == 0.0 and np.array_equal(b0, b1)
+        K2, _ = oracle.System(m, p, tau=3.0, f=oracle.MANUFACTURED_F).csc()
+        K3, _ = oracle.System(m, p, tau=3.0, f=oracle.MANUFACTURED_F, he_tau=True).csc()
+        # the difference is -(tau - 1) He, block diagonal per face (He = |e| I on a face's dofs)
+        D = (K3 - K2).toarray()
+        assert np.abs(D - np.diag(np.diag(D))).max() < 1e-12 * np.abs(D).max()
+        assert np.all(np.diag(D) < 0)
