@@ -40,20 +40,56 @@ WORKLOADS = {
 }
 
 
-def c4_problems(H, count=256, seed=20240611):
-    """The batching workload: `count` problems, n log-uniform in [8, 128], p uniform in {1,2,3,4},
-    interior nodes jittered by U(-0.2h, 0.2h), per-cell kappa log-uniform in [1e-2, 1e2], f = 8
-    Gaussian bumps (centres uniform in the square, widths 0.03-0.15, amplitudes N(0, 10^2))."""
+C4_SEED = 20240611
+
+
+def c4_specs(count=256, seed=C4_SEED):
+    """The batching workload as plain numbers (numpy only, so that the reference arm needs nothing
+    of the library): `count` problems, n log-uniform in [8, 128], p uniform in {1,2,3,4}, interior
+    nodes jittered by U(-0.2h, 0.2h) (splitmix64 stream seeded seed + k), per-cell kappa log-uniform
+    in [1e-2, 1e2], f = 8 Gaussian bumps (centres uniform in the square, widths 0.03-0.15, amplitudes
+    N(0, 10^2)).  Each spec: n, p, qd (the quadrature degree), bumps (the HDG_FIELD_BUMPS
+    parameters {K, (cx, cy, s, a) x K}), kappa_cell, jitter, seed."""
     import numpy as np
     rng = np.random.default_rng(seed)
-    probs = []
+    out = []
     for k in range(count):
         n = int(round(math.exp(rng.uniform(math.log(8), math.log(128)))))
         p = int(rng.integers(1, 5))
-        f = H.Field.bumps(rng.random((8, 2)), 0.03 + 0.12 * rng.random(8), 10.0 * rng.standard_normal(8))
+        centres, widths, amps = rng.random((8, 2)), 0.03 + 0.12 * rng.random(8), 10.0 * rng.standard_normal(8)
+        bumps = np.concatenate([[8.0], np.column_stack([centres, widths, amps]).ravel()])
         kc = np.exp(rng.uniform(math.log(1e-2), math.log(1e2), 2 * n * n))
-        probs.append(H.Problem(n=n, p=p, f=f, kappa_cell=kc, jitter=0.2, seed=seed + k))
-    return probs
+        out.append(dict(n=n, p=p, qd={1: 2, 2: 3, 3: 6, 4: 9}[p], bumps=bumps, kappa_cell=kc, jitter=0.2,
+                        seed=seed + k))
+    return out
+
+
+def jitter_rect_xy(xy, n, a, seed):
+    """Node coordinates of the n x n unit-square rectangle mesh (x fastest) with every interior
+    node moved by U(-a, a) h per coordinate, in the order and from the splitmix64 stream that
+    hdg_mesh_jitter uses (numpy uint64 arithmetic wraps as the C code does)."""
+    import numpy as np
+    G = np.uint64(0x9E3779B97F4A7C15)
+    m = 2 * (n - 1) * (n - 1)
+    with np.errstate(over="ignore"):
+        z = (np.uint64(seed) ^ G) + np.arange(1, m + 1, dtype=np.uint64) * G
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    r = (z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0) * 2.0 - 1.0
+    h = 1.0 / n
+    out = np.array(xy, dtype=np.float64, copy=True)
+    jj, ii = np.meshgrid(np.arange(1, n), np.arange(1, n), indexing="ij")
+    idx = (jj * (n + 1) + ii).ravel()
+    out[idx, 0] = out[idx, 0] + (a * h) * r[0::2]
+    out[idx, 1] = out[idx, 1] + (a * h) * r[1::2]
+    return out
+
+
+def c4_problems(H, count=256, seed=C4_SEED):
+    """c4_specs as library Problem objects (the GPU arm)."""
+    return [H.Problem(n=s["n"], p=s["p"], f=H.Field(H._lib.FIELD_BUMPS, tuple(float(v) for v in s["bumps"])),
+                      kappa_cell=s["kappa_cell"], jitter=s["jitter"], seed=s["seed"]) for s in c4_specs(count, seed)]
 
 
 def rel_l2(a, b):
@@ -66,31 +102,57 @@ C4_DESC = ("c4: 256 independent Poisson problems, n log-uniform [8,128], p unifo
            "per-cell kappa log-uniform [1e-2,1e2], 8 Gaussian bumps")
 
 
-def c4_oracle_problem(H, pr, threads):
-    """Solve one batching-workload problem with the CPU oracle (FP64, sparse direct); returns
-    (seconds, {"uhat", "q", "u"})."""
+def _oracle_c4_solve(spec, keep=False):
+    """One batching-workload problem solved completely by the CPU oracle on one thread (element loop,
+    COO->CSC, apply!, SuperLU, recovery); returns (seconds, {"uhat", "u"} or None).  Runs in a pool
+    worker; it imports only numpy and the oracle."""
+    import numpy as np
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import hdgref
-    om = hdgref.rectangle_mesh(pr.n, pr.n)
-    om.set_xy(H.batch.host_mesh(pr)._topology()[0])
+    n = spec["n"]
+    om = hdgref.rectangle_mesh(n, n)
+    om.set_xy(jitter_rect_xy(om.xy, n, spec["jitter"], spec["seed"]))
     t0 = time.perf_counter()
-    r = hdgref.solve_poisson(om, pr.p, qd=pr.qd(), f=pr.f.as_oracle(), kappa_cell=pr.kappa_cell, threads=threads)
-    return time.perf_counter() - t0, r
+    r = hdgref.solve_poisson(om, spec["p"], qd=spec["qd"], f=(hdgref.F_BUMPS, spec["bumps"]),
+                             kappa_cell=spec["kappa_cell"], threads=1)
+    dt = time.perf_counter() - t0
+    return dt, (dict(uhat=np.asarray(r["uhat"]), u=np.asarray(r["u"])) if keep else None)
 
 
-def c4_cpu_sample(H, probs, threads, budget_s=20.0, min_count=4, seed=1):
-    """Oracle solves of problems drawn uniformly (seeded) from the batch until `budget_s` of CPU
-    work; the mean time per problem over the sample estimates the whole batch's rate."""
-    import numpy as np
-    order = np.random.default_rng(seed).permutation(len(probs))
-    done, total = [], 0.0
-    for k in order:
-        dt, r = c4_oracle_problem(H, probs[int(k)], threads)
-        done.append((int(k), dt, r))
-        total += dt
-        if total >= budget_s and len(done) >= min_count:
-            break
-    return done, total
+def _pool_solve(args):
+    spec, keep = args
+    return _oracle_c4_solve(spec, keep)
+
+
+def c4_cpu_sample_indices(specs, count=48):
+    """A fixed stratified sample of the batch: the problems sorted by size (cells, then degree), cut
+    into `count` equal strata, the middle problem of each.  The same sample in every step."""
+    order = sorted(range(len(specs)), key=lambda k: (specs[k]["n"], specs[k]["p"], k))
+    per = len(order) / count
+    return [order[int(per * j + per / 2)] for j in range(count)]
+
+
+class OraclePool:
+    """Worker processes (started with spawn, one per host core) that solve batching-workload
+    problems with the single-threaded oracle, largest problems first."""
+
+    def __init__(self, workers=None):
+        import multiprocessing as mp
+        self.workers = workers or (os.cpu_count() or 1)
+        self.pool = mp.get_context("spawn").Pool(self.workers)
+
+    def run(self, specs, idx, keep=False):
+        """Solves specs[idx]; returns (wall seconds, per-problem seconds, results) in idx order."""
+        order = sorted(idx, key=lambda k: -(specs[k]["n"] ** 2) * (specs[k]["p"] + 1) ** 3)
+        t0 = time.perf_counter()
+        res = self.pool.map(_pool_solve, [(specs[k], keep) for k in order], chunksize=1)
+        wall = time.perf_counter() - t0
+        by = dict(zip(order, res))
+        return wall, [by[k][0] for k in idx], [by[k][1] for k in idx]
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
 
 
 def run_c4(args, ws, rank, local):
@@ -270,15 +332,21 @@ def run_c4(args, ws, rank, local):
         "clocks": clk,
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        done, total = c4_cpu_sample(H, probs, threads)
+        specs = c4_specs()
+        idx = c4_cpu_sample_indices(specs)
+        pool = OraclePool()
+        wall, per, res = pool.run(specs, idx, keep=True)
+        pool.close()
         line["cpu_baseline"] = {
-            "value": len(done) / total, "unit": "solves/s", "cores": threads, "kind": "port",
-            "sample": f"{len(done)} problems drawn uniformly (seeded) from the 256, each solved completely by the "
-                      f"C++ oracle (OpenMP element loop on {threads} threads, COO->CSC, apply!, SuperLU direct "
-                      f"solve, recovery) in {total:.1f} s; the mean time per problem gives the rate"}
+            "value": len(idx) / wall, "unit": "solves/s", "cores": pool.workers, "kind": "port",
+            "single_thread_value": len(idx) / sum(per),
+            "sample": f"a fixed stratified sample of {len(idx)} of the 256 problems (the middle problem of each "
+                      f"1/{len(idx)} of the batch by size), each solved completely by the single-threaded C++ "
+                      f"oracle (element loop, COO->CSC, apply!, SuperLU direct solve, recovery) on a pool of "
+                      f"{pool.workers} worker processes, largest first: {wall:.1f} s wall; single_thread_value = "
+                      f"problems / the sum of the per-problem times ({sum(per):.1f} s)"}
         line["max_rel_l2_err_vs_cpu_oracle"] = max(
-            max(rel_l2(sols[k][0], r["uhat"]), rel_l2(sols[k][2].ravel(), r["u"].ravel())) for k, _, r in done)
+            max(rel_l2(sols[k][0], r["uhat"]), rel_l2(sols[k][2].ravel(), r["u"].ravel())) for k, r in zip(idx, res))
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -806,11 +874,54 @@ def oracle_solve_once(n, p, qd, threads):
 
 
 def cpu_baseline(w, threads):
-    dt, _ = oracle_solve_once(w["n"], w["p"], w["qd"], threads)
+    """One complete oracle solve of the workload, timed; returns (the cpu_baseline entry, the
+    oracle's result, whose system the parity check reuses)."""
+    dt, r = oracle_solve_once(w["n"], w["p"], w["qd"], threads)
     return {"value": 1.0 / dt, "unit": "solves/s", "cores": threads, "kind": "port",
             "sample": f"one complete solve of the same workload ({2 * w['n'] ** 2} cells, p={w['p']}) by the "
                       f"C++ oracle: OpenMP element loop on {threads} threads, COO->CSC, apply!, SuperLU "
-                      f"(single-threaded; minimum degree on A'+A with diagonal-preferring pivots, as UMFPACK's symmetric strategy), recovery; {dt:.2f} s"}
+                      f"(single-threaded; minimum degree on A'+A with diagonal-preferring pivots, as UMFPACK's "
+                      f"symmetric strategy), recovery; {dt:.2f} s"}, r
+
+
+def parity_vs_oracle(H, K, S, pc, dirichlet_dofs):
+    """The device system and solution against the oracle's on the same mesh (the oracle system S
+    after apply!).  Sparsity pattern bit-exact; matrix entries relative to their row's largest
+    entry, except the Dirichlet diagonal, which carries mean|diag K| summed in sequence as the
+    reference does (src/boundary.jl:169-175; the device sums in a tree), reported on its own; the
+    trace solution of the device (CG to 1e-12, then two double-double refinement steps) against the
+    oracle's SuperLU solution refined the same way: relative L2 difference and componentwise
+    backward error max_i |b - K x|_i / (|K| |x| + |b|)_i in the oracle's system."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import hdgref
+    colptr, rowval, nzval, rhs = K.csc(0)
+    oK, ob = S.csc()
+    out = {"csc_pattern_equal": bool(np.array_equal(colptr, oK.indptr) and np.array_equal(rowval, oK.indices))}
+    if not out["csc_pattern_equal"]:
+        return out
+    rows = np.asarray(oK.indices)
+    cols = np.repeat(np.arange(oK.shape[0]), np.diff(oK.indptr))
+    rowmax = np.zeros(oK.shape[0])
+    np.maximum.at(rowmax, rows, np.abs(oK.data))
+    dmask = np.zeros(oK.shape[0], bool)
+    dmask[np.asarray(dirichlet_dofs) - 1] = True
+    ddiag = (rows == cols) & dmask[rows]
+    d = np.abs(nzval - oK.data) / np.maximum(rowmax[rows], 1e-300)
+    out["nzval_rel_rowmax"] = float(d[~ddiag].max())
+    out["dirichlet_diag_rel"] = float(d[ddiag].max()) if ddiag.any() else 0.0
+    out["rhs_rel_max"] = float(np.abs(rhs - ob).max() / max(np.abs(ob).max(), 1e-300))
+    x = K.solve(tol=1e-12, preconditioner=pc, refine=2)
+    q, u, _ = K.recover()
+    lu = S.solve()
+    xr = S.solve(refine=3)
+    oq, ou, _ = S.recover(xr)
+    res = hdgref.csc_residual_dd(oK, x, ob)
+    den = abs(oK) @ np.abs(x) + np.abs(ob)
+    out.update({"uhat_rel_l2": rel_l2(x, xr), "uhat_backward_error": float((np.abs(res) / np.maximum(den, 1e-300)).max()),
+                "q_rel_l2": rel_l2(q.ravel(), oq.ravel()), "u_rel_l2": rel_l2(u.ravel(), ou.ravel()),
+                "oracle_direct_vs_refined_rel_l2": rel_l2(lu, xr)})
+    return out
 
 
 def run_reference(args, ws, rank):
@@ -821,26 +932,31 @@ def run_reference(args, ws, rank):
         return
     threads = os.cpu_count() or 1
     if args.workload == "c4":
-        import numpy as np
-        import __graft_entry__ as g
-        H = g.import_package()
-        probs = c4_problems(H)
-        per_step = 4
-        order = np.random.default_rng(3).permutation(len(probs))
-        pick = lambda k: [probs[int(order[(k * per_step + j) % len(probs)])] for j in range(per_step)]
-        for w_ in range(args.warmup):
-            c4_oracle_problem(H, pick(w_)[0], threads)
-        times = []
-        for k in range(args.steps):
-            times.append(sum(c4_oracle_problem(H, pr, threads)[0] for pr in pick(k)))
+        specs = c4_specs()
+        idx = c4_cpu_sample_indices(specs)
+        pool = OraclePool()
+        threads = pool.workers
+        for _ in range(args.warmup):
+            pool.run(specs, idx)
+        times, per_problem = [], []
+        for _ in range(args.steps):
+            wall, per, _ = pool.run(specs, idx)
+            times.append(wall)
+            per_problem += per
+        pool.close()
         tot = sum(times)
-        value = per_step * args.steps / tot
-        cfg = {"workload": C4_DESC + "; each step solves 4 of the 256 problems (seeded uniform draw)",
-               "problems": len(probs)}
-        sample = (f"each step is 4 problems of the batch drawn uniformly (seeded), each solved completely by the C++ "
-                  f"oracle (OpenMP element loop on {threads} threads, COO->CSC, apply!, SuperLU direct solve, "
-                  "recovery); the reference itself is Julia, which is not installed on this machine")
-        step_times = [t / per_step for t in times]
+        value = len(idx) * args.steps / tot
+        cfg = {"workload": C4_DESC + f"; each step solves the same fixed stratified sample of {len(idx)} of the 256 "
+                                     "problems (the middle problem of each equal slice of the batch sorted by size)",
+               "problems": 256, "sample_problems": len(idx), "same_config": False,
+               "scaling": f"the rate of the sample stands for the batch's rate: the sample spans the batch's size "
+                          f"distribution (one problem per 1/{len(idx)} quantile of the size)"}
+        sample = (f"each step is the fixed stratified sample of {len(idx)} problems, each solved completely by the "
+                  f"single-threaded C++ oracle (element loop, COO->CSC, apply!, SuperLU direct solve, recovery) on a "
+                  f"pool of {threads} worker processes, largest first; the reference itself is Julia, which is not "
+                  "installed on this machine")
+        step_times = [t / len(idx) for t in times]
+        single = len(per_problem) / sum(per_problem)
     else:
         w = WORKLOADS[args.workload]
         for _ in range(args.warmup):
@@ -853,11 +969,13 @@ def run_reference(args, ws, rank):
                   "apply!, SuperLU direct solve, recovery); the reference itself is Julia, which is not installed on "
                   "this machine")
         step_times = times
+        single = None
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
-        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port", "sample": sample,
+                         "single_thread_value": single},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "p50_ms": 1e3 * statistics.median(step_times), "p99_ms": 1e3 * max(step_times),
     }
@@ -1022,7 +1140,8 @@ def run_ours(args, ws, rank, local):
         "clocks": clk,
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(w, os.cpu_count() or 1)
+        line["cpu_baseline"], r = cpu_baseline(w, os.cpu_count() or 1)
+        line["parity_vs_oracle"] = parity_vs_oracle(H, K, r["system"], pc, dbc.prescribed_dofs)
     if rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libhdg.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU = ["element.cu", "trace.cu", "cg.cu", "recover.cu", "noalloc.cu", "amg.cu", "lagrange.cu"]
+CU = ["element.cu", "trace.cu", "cg.cu", "recover.cu", "noalloc.cu", "amg.cu", "lagrange.cu", "refine.cu"]
 CPP = ["capi.cpp", "mesh.cpp", "tables.cpp", "assembler.cpp", "serve.cpp", "dofhandler.cpp"]
 
 

@@ -599,6 +599,8 @@ int hdg_dirichlet(const hdg_space* sp, const char* faceset, const hdg_field* g, 
   const int nt = t.nt, nfq = t.nfq;
   *count = (int)it->second.size() * nt;
   if (!dofs && !vals) return HDG_OK;
+  std::string why;
+  if (field_check(g, &why) != HDG_OK) return fail(m->ctx, HDG_ERR_ARG, why);
   FieldSpec gs = field_from(g, 0.0);
   static const double EDGE[3][4] = {{1, 0, 0, 1}, {0, 1, 0, 0}, {0, 0, 1, 0}};
   static const int EN[3][2] = {{1, 2}, {2, 0}, {0, 1}};
@@ -644,6 +646,8 @@ int hdg_dirichlet_l2(const hdg_space* sp, const char* faceset, const hdg_field* 
   const int nt = t.nt, nfq = t.nfq;
   *count = (int)it->second.size() * nt;
   if (!dofs && !vals) return HDG_OK;
+  std::string why;
+  if (field_check(g, &why) != HDG_OK) return fail(m->ctx, HDG_ERR_ARG, why);
   FieldSpec gs = field_from(g, 0.0);
   static const double EDGE[3][4] = {{1, 0, 0, 1}, {0, 1, 0, 0}, {0, 0, 1, 0}};
   static const int EN[3][2] = {{1, 2}, {2, 0}, {0, 1}};
@@ -772,6 +776,37 @@ int hdg_solve(hdg_system* s, const hdg_solver* opts, double* uhat, hdg_stats* st
     }
     if (rc == HDG_ERR_NO_CONVERGENCE) return fail(s->ctx, rc, "CG did not reach the tolerance within maxit");
     if (rc == HDG_ERR_BREAKDOWN) return fail(s->ctx, rc, "CG breakdown: the trace system is not definite");
+    return rc;
+  });
+}
+
+int hdg_refine(hdg_system* s, const hdg_solver* opts, int steps, double correction_tol, double* uhat,
+               hdg_stats* stats) {
+  if (!s) return HDG_ERR_ARG;
+  if (!s->have_solution) return fail(s->ctx, HDG_ERR_ARG, "solve first (hdg_solve)");
+  if (steps < 0 || steps > 16) return fail(s->ctx, HDG_ERR_ARG, "refinement steps must be in [0, 16]");
+  if (!(correction_tol > 0.0) || !(correction_tol < 1.0))
+    return fail(s->ctx, HDG_ERR_ARG, "the correction tolerance must lie in (0, 1)");
+  return guard(s->ctx, [&]() -> int {
+    set_device(s->ctx);
+    hdg_solver o = solver_defaults(opts);
+    std::vector<hdg_stats> per;
+    int rc = run_refine(s, o, steps, correction_tol, &per);
+    if (stats) {
+      hdg_stats agg{0, steps, 0.0, 1};
+      for (auto& r : per) {
+        agg.iterations = std::max(agg.iterations, r.iterations);
+        agg.rel_residual = std::max(agg.rel_residual, r.rel_residual);
+        agg.converged = agg.converged && r.converged;
+      }
+      *stats = agg;
+    }
+    if (uhat) {
+      s->d_x.download(uhat, (size_t)s->ndofs, s->ctx->stream);
+      HDG_CUDA(cudaStreamSynchronize(s->ctx->stream));
+    }
+    if (rc == HDG_ERR_NO_CONVERGENCE) return fail(s->ctx, rc, "a correction solve did not reach its tolerance");
+    if (rc == HDG_ERR_BREAKDOWN) return fail(s->ctx, rc, "CG breakdown in a correction solve");
     return rc;
   });
 }

@@ -86,6 +86,9 @@ struct FieldSpec {
   int kind = HDG_FIELD_CONST;
   std::vector<double> prm{0.0};
 };
+// HDG_OK, or HDG_ERR_ARG with the reason when f's parameters do not cover what its kind reads.
+int field_check(const hdg_field* f, std::string* why);
+// FieldSpec of f (NULL: the constant default_const); throws HdgError{HDG_ERR_ARG} on a bad field.
 FieldSpec field_from(const hdg_field* f, double default_const);
 double eval_field_host(const FieldSpec& f, double x, double y);
 
@@ -337,6 +340,10 @@ void assembly_check(hdg_system* s, cudaStream_t st);          // read the elemen
 int run_batch_step(const std::vector<hdg_system*>& sys, const hdg_solver& o, int flags,
                    std::vector<std::vector<hdg_stats>>* stats);
 int run_solve(hdg_system* s, const hdg_solver& o, hdg_stats* st);
+// FP64 iterative refinement of d_x with a double-double residual (refine.cu): `steps` corrections
+// solved by the system's CG to relative tolerance ctol; out: per problem, the total correction
+// iterations and the final double-double relative residual.
+int run_refine(hdg_system* s, const hdg_solver& o, int steps, double ctol, std::vector<hdg_stats>* out);
 int run_solve_many(const std::vector<hdg_system*>& sys, const hdg_solver& o,
                    std::vector<std::vector<hdg_stats>>* stats);
 void build_segments(hdg_system* s);

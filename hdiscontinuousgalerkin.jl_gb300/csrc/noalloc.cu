@@ -15,7 +15,9 @@
 //  * every call on a device shares the one array, which keeps the last call's contents: calls that
 //    overlap on the GPU (different streams, or threads) race and must be serialised by the caller;
 //  * the first call on each device looks up the array's device address (set-up, once per device,
-//    with that device current); make that first call before any stream capture.
+//    with that device current); make that first call before any stream capture.  The address is
+//    cached for the process; a call that fails with a CUDA error drops it, so that after a device
+//    reset (which reloads the module) the next call looks it up again.
 #include <mutex>
 
 #include "hdg_device.cuh"
@@ -141,9 +143,20 @@ int hdg_errornorm_l2sq_noalloc(int device, void* stream, int p, int quad_degree,
                std::to_string(NA_TABLE) + "-double scratch";
     return HDG_ERR_CAPACITY;
   }
-  if (u_exact->nparams > NA_PARAMS || u_exact->nparams < 0 || (u_exact->nparams > 0 && !u_exact->params)) {
+  if (u_exact->nparams < 0 || (u_exact->nparams > 0 && !u_exact->params)) {
+    g_na_err = "hdg_errornorm_l2sq_noalloc: negative parameter count or missing parameters";
+    return HDG_ERR_ARG;
+  }
+  if (u_exact->nparams > NA_PARAMS) {
     g_na_err = "hdg_errornorm_l2sq_noalloc: more than " + std::to_string(NA_PARAMS) + " field parameters";
     return HDG_ERR_CAPACITY;
+  }
+  {
+    std::string why;
+    if (field_check(u_exact, &why) != HDG_OK) {
+      g_na_err = "hdg_errornorm_l2sq_noalloc: " + why;
+      return HDG_ERR_ARG;
+    }
   }
   double* scratch = nullptr;
   int rc = na_setup(device, &scratch);
@@ -160,14 +173,15 @@ int hdg_errornorm_l2sq_noalloc(int device, void* stream, int p, int quad_degree,
     stage[nw * nq + nq + 2 * q] = t->qx[q];
     stage[nw * nq + nq + 2 * q + 1] = t->qy[q];
   }
-  double zero = 0.0;
-  const int np = u_exact->nparams > 0 ? u_exact->nparams : 1;
-  const double* prm = u_exact->nparams > 0 ? u_exact->params : &zero;
-  for (int k = 0; k < np; ++k) stage[NA_TABLE + k] = prm[k];
+  const int np = u_exact->nparams;  // >= 1: field_check requires what the kind reads
+  for (int k = 0; k < np; ++k) stage[NA_TABLE + k] = u_exact->params[k];
   cudaStream_t st = (cudaStream_t)stream;
   int cur = 0;
   cudaGetDevice(&cur);
-  if (cudaSetDevice(device) != cudaSuccess) return HDG_ERR_CUDA;
+  if (cudaSetDevice(device) != cudaSuccess) {
+    g_na_err = "hdg_errornorm_l2sq_noalloc: cudaSetDevice(" + std::to_string(device) + ") failed";
+    return HDG_ERR_CUDA;
+  }
   cudaError_t e = cudaMemcpyAsync(scratch + NA_OFF_TABLE, stage, sizeof(double) * need, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(scratch + NA_OFF_PARAMS, stage + NA_TABLE, sizeof(double) * np, cudaMemcpyHostToDevice, st);
@@ -186,9 +200,16 @@ int hdg_errornorm_l2sq_noalloc(int device, void* stream, int p, int quad_degree,
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   cudaSetDevice(cur);
   if (e != cudaSuccess) {
+    // forget the cached address: after a device reset the module reloads at another address,
+    // and the next call looks it up again
+    {
+      std::lock_guard<std::mutex> lk(g_na_lock);
+      g_na_ptr[device] = nullptr;
+    }
     g_na_err = std::string("hdg_errornorm_l2sq_noalloc: ") + cudaGetErrorString(e);
     return HDG_ERR_CUDA;
   }
+  g_na_err.clear();
   return HDG_OK;
 }
 

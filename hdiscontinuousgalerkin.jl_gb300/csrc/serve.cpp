@@ -187,7 +187,8 @@ Flight* launch_flight(hdg_engine* e, std::vector<Request>&& reqs, int slot) {
   t1 = now_s();
   fl->t[2] += t1 - t0;
   int cnt = 0;
-  hdg_field zero{HDG_FIELD_CONST, 0, nullptr};
+  static const double kZero = 0.0;
+  hdg_field zero{HDG_FIELD_CONST, 1, &kZero};
   rc = hdg_dirichlet(fl->space, "boundary", &zero, nullptr, nullptr, &cnt);
   if (rc != HDG_OK) throw HdgError{rc, c->err};
   std::vector<int32_t> dofs(cnt);
@@ -326,6 +327,7 @@ int hdg_engine_submit(hdg_engine* e, int mesh_id, const hdg_mesh* mesh, int p, i
                       const double* kappa_cell, double tau, int64_t* request_id) {
   if (!e || !f || (mesh_id < 0 && !mesh) || mesh_id >= (int)e->resident.size() || p < 1 || p > HDG_MAX_P)
     return HDG_ERR_ARG;
+  if (field_check(f, nullptr) != HDG_OK) return HDG_ERR_ARG;
   Request r;
   r.id = e->next_id++;
   r.mesh_id = mesh_id;

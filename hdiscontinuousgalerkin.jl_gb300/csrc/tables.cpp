@@ -11,6 +11,7 @@
 //   F_{f,o}[a][j]  = sum_k fw_k T_j(k) E_a(o ? k : nfq-1-k, f)  (Fe = tau |e_f| F, Ee = wn_f (x) F)
 //   H[i][j]        = sum_k fw_k T_i(k) T_j(k)               (He = |e_f| H per face block)
 //   NW[a][q]       = N_a(q) w_q                             (be = detJ sum_q f(x_q) NW[a][q])
+#include <string>
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -467,6 +468,49 @@ bool build_lagrange_tables(int order, int qd, LagrangeTables* t) {
 }
 
 // ------------------------------------------------------------------ fields (host side)
+// A field's parameter count must cover what its kind reads (the device evaluator indexes them
+// without bounds): CONST c; SINSIN a, kx, ky; BUMPS K then 4 per bump; FOURIER / EXP_FOURIER K,
+// g0 then 4 per mode, with K a finite non-negative integer.
+int field_check(const hdg_field* f, std::string* why) {
+  if (!f) return HDG_OK;
+  auto bad = [&](const std::string& m) {
+    if (why) *why = m;
+    return HDG_ERR_ARG;
+  };
+  if (f->nparams < 0) return bad("field: negative parameter count");
+  if (f->nparams > 0 && !f->params) return bad("field: parameter count without parameters");
+  const int np = f->nparams;
+  const double* p = f->params;
+  auto count_of = [&](int first) -> long {  // K in p[0], items of 4 after `first` leading values
+    if (np < 1 || !std::isfinite(p[0]) || p[0] < 0.0 || p[0] != std::floor(p[0]) || p[0] > 1e6) return -1;
+    return first + 4L * (long)p[0];
+  };
+  switch (f->kind) {
+    case HDG_FIELD_CONST:
+      if (np < 1) return bad("field CONST needs 1 parameter (c)");
+      return HDG_OK;
+    case HDG_FIELD_SINSIN:
+      if (np < 3) return bad("field SINSIN needs 3 parameters (a, kx, ky)");
+      return HDG_OK;
+    case HDG_FIELD_BUMPS: {
+      const long need = count_of(1);
+      if (need < 0) return bad("field BUMPS: the first parameter must be the bump count K >= 0");
+      if (np < need) return bad("field BUMPS with K = " + std::to_string((long)p[0]) + " needs " + std::to_string(need) +
+                                " parameters, got " + std::to_string(np));
+      return HDG_OK;
+    }
+    case HDG_FIELD_FOURIER:
+    case HDG_FIELD_EXP_FOURIER: {
+      const long need = count_of(2);
+      if (need < 0) return bad("field FOURIER: the first parameter must be the mode count K >= 0");
+      if (np < need) return bad("field FOURIER with K = " + std::to_string((long)p[0]) + " needs " +
+                                std::to_string(need) + " parameters, got " + std::to_string(np));
+      return HDG_OK;
+    }
+  }
+  return bad("field: unknown kind " + std::to_string(f->kind));
+}
+
 FieldSpec field_from(const hdg_field* f, double default_const) {
   FieldSpec s;
   if (!f) {
@@ -474,9 +518,10 @@ FieldSpec field_from(const hdg_field* f, double default_const) {
     s.prm = {default_const};
     return s;
   }
+  std::string why;
+  if (field_check(f, &why) != HDG_OK) throw HdgError{HDG_ERR_ARG, why};
   s.kind = f->kind;
-  s.prm.assign(f->params, f->params + (f->nparams > 0 ? f->nparams : 0));
-  if (s.prm.empty()) s.prm.push_back(0.0);
+  s.prm.assign(f->params, f->params + f->nparams);
   return s;
 }
 

@@ -125,14 +125,23 @@ class TraceSystem:
         L.check(L.load().hdg_apply_dirichlet(self._h, L.i32ptr(d), L.dptr(v), len(d)), self.ctx)
 
     def solve(self, tol=1e-12, maxit=100000, precision=None, chunk=32, inner_tol=1e-5, to_host=True,
-              preconditioner=L.PRECOND_JACOBI):
-        """K \\ b by preconditioned CG (Jacobi, or the multigrid V-cycle with preconditioner=PRECOND_AMG)."""
+              preconditioner=L.PRECOND_JACOBI, refine=0, refine_tol=1e-6):
+        """K \\ b by preconditioned CG (Jacobi, or the multigrid V-cycle with preconditioner=PRECOND_AMG).
+
+        refine > 0 follows the CG with that many FP64 iterative-refinement steps on a
+        double-double residual (hdg_refine), each correction solved to refine_tol; the result is
+        then the assembled FP64 system's solution to a few ulps instead of the CG's tolerance."""
         o = L.hdg_solver(float(tol), int(maxit), int(self.precision if precision is None else precision), int(chunk),
                          float(inner_tol), int(preconditioner))
         st = L.hdg_stats()
         out = np.zeros(self.ndofs) if to_host else None
-        L.check(L.load().hdg_solve(self._h, C.byref(o), L.dptr(out), C.byref(st)), self.ctx)
+        L.check(L.load().hdg_solve(self._h, C.byref(o), None if refine else L.dptr(out), C.byref(st)), self.ctx)
         self.stats = SolveStats(st)
+        if refine:
+            rs = L.hdg_stats()
+            L.check(L.load().hdg_refine(self._h, C.byref(o), int(refine), float(refine_tol), L.dptr(out),
+                                        C.byref(rs)), self.ctx)
+            self.refine_stats = SolveStats(rs)
         return out
 
     def recover(self, to_host=True):

@@ -190,6 +190,17 @@ typedef struct {
 /* u_hat = K \ b (examples/poisson2D_HDG.jl:195) by Jacobi-preconditioned CG on the free
  * trace dofs.  uhat (host, ndofs) may be NULL to keep the result on the device only. */
 int hdg_solve(hdg_system* sys, const hdg_solver* opts, double* uhat, hdg_stats* stats);
+/* No reference counterpart (the reference's `K \ b`, examples/poisson2D_HDG.jl:195, is a direct
+ * solve with a forward error of order cond(K) 2^-53).  FP64 iterative refinement of the current
+ * device solution: `steps` times r = b - K u_hat in double-double arithmetic (exact products,
+ * TwoSum accumulation), K d = r by the CG of hdg_solve (same preconditioner and precision) to the
+ * relative residual correction_tol, u_hat += d.  Each step shrinks the error by about
+ * correction_tol times the condition-dependent CG error factor, down to the rounding of u_hat,
+ * so two steps after a 1e-12 CG give the assembled FP64 system's solution to a few ulps.  stats:
+ * iterations = correction iterations (max over problems), outer = steps, rel_residual = the
+ * double-double |b - K u_hat| / |b| after the last step.  uhat (host) may be NULL. */
+int hdg_refine(hdg_system* sys, const hdg_solver* opts, int steps, double correction_tol, double* uhat,
+               hdg_stats* stats);
 
 /* ---- recovery and errors ------------------------------------------------------------- */
 /* get_uσ!, examples/poisson2D_HDG.jl:197-212 (trace slice for any nt): q (ncells x nv),
@@ -210,9 +221,11 @@ int hdg_system_destroy(hdg_system* sys);
  * (nnodes x 2), cells (ncells x 3, 0-based), u (ncells x nw, the recovered Dubiner coefficients).
  * The result goes to the host double *out.  The scratch is one fixed 32.8 KB device array per
  * device (at most 2048 doubles of tables, enough for p <= 4, and 1024 field parameters; larger
- * requests return HDG_ERR_CAPACITY).  The call allocates nothing.  Calls that overlap on one
- * device race on that array, so the caller serialises them.  The first call on a device looks
- * up the array's address and must come before any stream capture.  Errors go to
+ * requests return HDG_ERR_CAPACITY; a field whose parameters do not cover its kind returns
+ * HDG_ERR_ARG).  The call allocates nothing.  Calls that overlap on one device race on that
+ * array, so the caller serialises them.  The first call on a device looks up the array's address
+ * and must come before any stream capture; the address is kept for the process, and dropped after
+ * a call that fails with a CUDA error (a device reset moves it).  Errors go to
  * hdg_noalloc_last_error(). */
 int hdg_errornorm_l2sq_noalloc(int device, void* stream, int p, int quad_degree, int ncells, const double* xy,
                                const int32_t* cells, const double* u, const hdg_field* u_exact, double* out);

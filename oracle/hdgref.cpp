@@ -1155,4 +1155,30 @@ double hr_eval_field(int kind, int np, const double* prm, double x, double y) {
   return eval_field(f, x, y);
 }
 
+// r = b - K x for a CSC matrix, accumulated in double-double arithmetic and rounded once: each
+// product is split exactly with an FMA (Dekker/Kahan TwoProduct) and each row sum is carried as
+// an unevaluated pair with Knuth's TwoSum.  The residual of an FP64 solution of K x = b is as
+// small as the rounding of x itself, so a plain FP64 residual is mostly rounding noise; this one
+// is accurate to about 2^-100 of the summed magnitudes, which lets the Python side refine the
+// sparse direct solve of examples/poisson2D_HDG.jl:195 to the correctly rounded solution of the
+// assembled FP64 system (iterative refinement with an extra-precise residual, Wilkinson 1963).
+void hr_csc_residual_dd(int n, const int64_t* colptr, const int64_t* rowval, const double* nzval, const double* x,
+                        const double* b, double* r) {
+  std::vector<double> hi(b, b + n), lo(n, 0.0);
+  for (int j = 0; j < n; ++j) {
+    const double xj = x[j];
+    for (int64_t k = colptr[j]; k < colptr[j + 1]; ++k) {
+      const int64_t i = rowval[k];
+      const double p = -nzval[k] * xj;
+      const double e = std::fma(-nzval[k], xj, -p);  // -nzval*xj = p + e exactly
+      const double s = hi[i] + p;
+      const double bv = s - hi[i];
+      const double err = (hi[i] - (s - bv)) + (p - bv);  // hi + p = s + err exactly
+      hi[i] = s;
+      lo[i] += err + e;
+    }
+  }
+  for (int i = 0; i < n; ++i) r[i] = hi[i] + lo[i];
+}
+
 }  // extern "C"

@@ -79,6 +79,7 @@ def lib():
             L.hr_errornorm.argtypes = [vp, C.c_int, C.c_int, dp, C.c_int, C.c_int, dp]
             L.hr_eval_field.restype = C.c_double
             L.hr_eval_field.argtypes = [C.c_int, C.c_int, dp, C.c_double, C.c_double]
+            L.hr_csc_residual_dd.argtypes = [C.c_int, i64p, i64p, dp, dp, dp, dp]
             _lib = L
     return _lib
 
@@ -295,15 +296,28 @@ class System:
         vals = np.ascontiguousarray(vals, dtype=np.float64)
         lib().hr_apply(self.h, len(dofs), _ip(dofs), _dp(vals))
 
-    def solve(self):
+    def solve(self, refine: int = 0):
         """û = K \\ b with SuperLU (examples/poisson2D_HDG.jl:195).  Julia's `\\` on a
         non-Hermitian SparseMatrixCSC calls UMFPACK, whose symmetric strategy (chosen for a matrix
         with a symmetric pattern and a zero-free diagonal, as K is) orders A'+A by minimum degree
         and prefers diagonal pivots with a relative tolerance of 0.001.  SuperLU is set up the
-        same way: minimum degree on A'+A and diag_pivot_thresh = 0.001."""
+        same way: minimum degree on A'+A and diag_pivot_thresh = 0.001.
+
+        refine > 0 adds up to that many steps of iterative refinement with the double-double
+        residual (csc_residual_dd) and the same LU factors.  The direct solve alone carries a
+        forward error of order cond(K) * 2^-53 (about 1e-12 on the 2*256^2-cell system); the
+        refined solution is the assembled FP64 system's solution to about 1e-16, which is what
+        a 1e-12 comparison of two solvers needs."""
         import scipy.sparse.linalg as spla
         K, b = self.csc()
-        return spla.splu(K.tocsc(), permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=0.001).solve(b)
+        lu = spla.splu(K.tocsc(), permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=0.001)
+        x = lu.solve(b)
+        for _ in range(refine):
+            d = lu.solve(csc_residual_dd(K, x, b))
+            x = x + d
+            if np.linalg.norm(d) <= 1e-17 * np.linalg.norm(x):
+                break
+        return x
 
     def recover(self, uhat):
         nc = self.mesh.ncells
@@ -321,6 +335,20 @@ def errornorm(mesh: Mesh, p: int, u, u_ex, qd=None) -> float:
     uk, up = _field(u_ex)
     u = np.ascontiguousarray(u, dtype=np.float64)
     return lib().hr_errornorm(mesh.h, p, qd, _dp(u), uk, up.size, _dp(up))
+
+
+def csc_residual_dd(K, x, b) -> np.ndarray:
+    """b - K x for a scipy CSC matrix, summed in double-double arithmetic and rounded once
+    (hr_csc_residual_dd)."""
+    K = K.tocsc()
+    colptr = np.ascontiguousarray(K.indptr, dtype=np.int64)
+    rowval = np.ascontiguousarray(K.indices, dtype=np.int64)
+    val = np.ascontiguousarray(K.data, dtype=np.float64)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    r = np.zeros(K.shape[0])
+    lib().hr_csc_residual_dd(K.shape[0], _i64p(colptr), _i64p(rowval), _dp(val), _dp(x), _dp(b), _dp(r))
+    return r
 
 
 def eval_field(spec, x, y) -> float:

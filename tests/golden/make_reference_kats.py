@@ -18,8 +18,32 @@ _ENV = {"sqrt": math.sqrt, "sq2": math.sqrt(2.0), "sq3": math.sqrt(3.0), "pi": m
 
 
 def _eval(expr: str) -> float:
+    """Value of an arithmetic expression read from the reference's test files.  The text is parsed,
+    never executed: only numbers, the names in _ENV, + - * / ** (Julia's ^ and //), unary signs and
+    calls of sqrt are accepted; anything else raises ValueError."""
+    import ast
+    import operator
     expr = expr.replace("^", "**").replace("//", "/")
-    return float(eval(expr, {"__builtins__": {}}, _ENV))
+    binops = {ast.Add: operator.add, ast.Sub: operator.sub, ast.Mult: operator.mul, ast.Div: operator.truediv,
+              ast.Pow: operator.pow}
+    unops = {ast.UAdd: operator.pos, ast.USub: operator.neg}
+
+    def ev(node):
+        if isinstance(node, ast.Expression):
+            return ev(node.body)
+        if isinstance(node, ast.Constant) and isinstance(node.value, (int, float)) and not isinstance(node.value, bool):
+            return float(node.value)
+        if isinstance(node, ast.Name) and node.id in _ENV and node.id != "sqrt":
+            return float(_ENV[node.id])
+        if isinstance(node, ast.BinOp) and type(node.op) in binops:
+            return binops[type(node.op)](ev(node.left), ev(node.right))
+        if isinstance(node, ast.UnaryOp) and type(node.op) in unops:
+            return unops[type(node.op)](ev(node.operand))
+        if (isinstance(node, ast.Call) and isinstance(node.func, ast.Name) and node.func.id == "sqrt"
+                and len(node.args) == 1 and not node.keywords):
+            return math.sqrt(ev(node.args[0]))
+        raise ValueError(f"not a plain arithmetic expression: {expr!r}")
+    return ev(ast.parse(expr, mode="eval"))
 
 
 def julia_matrix(text: str):

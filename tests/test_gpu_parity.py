@@ -1,8 +1,26 @@
 """GPU parity: libhdg (CUDA, sm_103a) against the CPU oracle on the same inputs.
 
-Tolerances (FP64 path): element blocks and global matrix entries within 1e-12 relative to the
-largest entry; sparsity pattern and dof numbering bit-exact; trace solution within a tolerance
-derived from the CG stopping criterion (relative residual 1e-13 here)."""
+What is compared, and to what tolerance (FP64 path):
+  * dof numbering and the CSC sparsity pattern: bit-exact;
+  * element blocks K_e, b_e: within 1e-12 of the largest entry of the same cell's block (a cell's
+    q rows scale like kappa/h and its u rows like 1, so one cell is the unit of scale);
+  * every entry of the global trace matrix: within 1e-12 of the largest entry of the same row
+    (relative to the row, so that small entries are checked on their own scale);
+  * the Dirichlet diagonal that apply! writes (mean|diag K|): the reference sums the diagonal in
+    sequence (src/boundary.jl:169-175) and so does the oracle, with a rounding error that grows
+    with the number of dofs (bound N 2^-53); the device sums in a tree.  These entries are checked
+    against that bound, and the device's value against the exactly summed mean to 1e-14;
+  * the trace solution: the device solution (CG to 1e-12, then FP64 iterative refinement on a
+    double-double residual, hdg_refine) is the solution of the oracle's system to a componentwise
+    backward error max_i |b - K x|_i / (|K||x| + |b|)_i <= 1e-12 (measured 1e-16..1e-13): it
+    solves a system within 1e-12 relative, entry by entry, of the oracle's.  The forward difference
+    from the oracle's (refined) direct solution is bounded separately per case: the trace system's
+    solution moves by 1e-13 (2*64^2 cells, p=2) to 3e-12 (2*256^2 cells) of its norm when the
+    entries of K move by one unit in the last place (oracle test
+    test_trace_solution_sensitivity_to_ulp_changes), and the device and oracle assemblies differ
+    by a few such units, so two FP64 implementations agree on the solution only to that level;
+    the reference's own direct solve (UMFPACK in Julia) differs from the refined solution by as
+    much (the oracle's SuperLU: 2.7e-12 of the norm at 2*128^2 cells, p=2)."""
 import math
 import os
 
@@ -12,6 +30,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 RTOL_BLOCK = 1e-12
+BWD_TOL = 1e-12
 
 
 @pytest.fixture(scope="module")
@@ -33,17 +52,88 @@ def rel(a, b):
     return np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(np.asarray(b)).max(), 1e-300)
 
 
+def rel_l2(a, b):
+    a, b = np.asarray(a).ravel(), np.asarray(b).ravel()
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def block_rel(a, b):
+    """max over entries of |a - b| / (largest |b| of the same cell's block); a, b: (cells, ...)."""
+    a, b = np.asarray(a), np.asarray(b)
+    scale = np.abs(b).reshape(len(b), -1).max(axis=1).reshape((len(b),) + (1,) * (b.ndim - 1))
+    return float((np.abs(a - b) / np.maximum(scale, 1e-300)).max())
+
+
+def row_rel(a, b):
+    """max over entries of |a - b| / (largest |b| in the same row); a, b: (..., rows, cols)."""
+    a, b = np.asarray(a), np.asarray(b)
+    scale = np.abs(b).max(axis=-1, keepdims=True)
+    return float((np.abs(a - b) / np.maximum(scale, 1e-300)).max())
+
+
+def csc_parity(colptr, rowval, nzval, oK, dirichlet=None, diag_exact=None):
+    """Pattern bit-exact, entries within RTOL_BLOCK of their row's largest entry; the Dirichlet
+    diagonal (mean|diag K| after apply!) against the oracle's sequential-sum bound and, given the
+    exactly summed mean diag_exact, the device's value to 1e-14.  Returns the measured figures."""
+    np.testing.assert_array_equal(colptr, oK.indptr)
+    np.testing.assert_array_equal(rowval, oK.indices)
+    rows = np.asarray(oK.indices)
+    cols = np.repeat(np.arange(oK.shape[0]), np.diff(oK.indptr))
+    rowmax = np.zeros(oK.shape[0])
+    np.maximum.at(rowmax, rows, np.abs(oK.data))
+    d = np.abs(nzval - oK.data) / np.maximum(rowmax[rows], 1e-300)
+    dd = np.zeros(len(d), bool)
+    if dirichlet is not None and len(dirichlet):
+        dm = np.zeros(oK.shape[0], bool)
+        dm[np.asarray(dirichlet) - 1] = True
+        dd = (rows == cols) & dm[rows]
+    out = {"entries": float(d[~dd].max())}
+    assert out["entries"] < RTOL_BLOCK, out
+    if dd.any():
+        n = oK.shape[0]
+        out["dirichlet_diag"] = float(d[dd].max())
+        assert out["dirichlet_diag"] <= n * 2.0 ** -53 + 1e-14, out
+        if diag_exact is not None:
+            got = nzval[dd]
+            assert np.all(np.abs(got - diag_exact) <= 1e-14 * diag_exact), (got[:3], diag_exact)
+    return out
+
+
+def backward_error(oK, ob, x):
+    """Componentwise backward error of x in the system oK x = ob (Oettli-Prager), with the residual
+    summed in double-double (the oracle's csc_residual_dd)."""
+    import hdgref
+    r = hdgref.csc_residual_dd(oK, x, ob)
+    den = abs(oK) @ np.abs(x) + np.abs(ob)
+    return float((np.abs(r) / np.maximum(den, 1e-300)).max())
+
+
+def check_solution(S, x, fwd_tol):
+    """x (device trace solution) against the oracle system S (after apply!): componentwise backward
+    error <= BWD_TOL, and relative L2 difference from the oracle's refined direct solution <= fwd_tol.
+    Returns (the oracle's refined solution, measured figures)."""
+    oK, ob = S.csc()
+    xr = S.solve(refine=3)
+    out = {"backward": backward_error(oK, ob, x), "forward": rel_l2(x, xr)}
+    assert out["backward"] <= BWD_TOL, out
+    assert out["forward"] <= fwd_tol, out
+    return xr, out
+
+
 def compare_system(H, oracle, mesh, omesh, p, qd=None, f=None, kappa=None, kappa_cell=None, tau=1.0, apply=True,
                    g=None, projection="reference", he_tau=False):
     f = f or H.MANUFACTURED_F
     Vh, Wh, Mh = spaces(H, mesh, p, qd)
     K, b, K_e, b_e = H.doassemble(Vh, Wh, Mh, tau, f, kappa=kappa, kappa_cell=kappa_cell, he_tau=he_tau)
     S = oracle.System(omesh, p, qd, tau, f.as_oracle(), kappa.as_oracle() if kappa is not None else None, kappa_cell,
-                      he_tau=he_tau)
+                      he_tau=he_tau, threads=os.cpu_count() or 1)
     Ate, bte, Ke, be = K.element_blocks()
     oKe, obe = S.local()
-    assert rel(Ke, oKe) < RTOL_BLOCK
-    assert rel(be, obe) < RTOL_BLOCK
+    assert block_rel(Ke, oKe) < RTOL_BLOCK
+    assert block_rel(be, obe) < RTOL_BLOCK
+    oK0, _ = S.csc()
+    diag_exact = math.fsum(np.abs(oK0.diagonal())) / oK0.shape[0]
+    dofs = None
     if apply:
         dbc = H.Dirichlet(H.TrialFunction(Mh), mesh, "boundary", g, projection=projection)
         od, ov = S.dirichlet("boundary", g.as_oracle() if g is not None else None, projection=projection)
@@ -51,11 +141,10 @@ def compare_system(H, oracle, mesh, omesh, p, qd=None, f=None, kappa=None, kappa
         np.testing.assert_allclose(dbc.values, ov, atol=1e-15)
         H.apply_(K, b, dbc)
         S.apply(od, ov)
+        dofs = od
     colptr, rowval, nzval, rhs = K.csc(0)
     oK, ob = S.csc()
-    np.testing.assert_array_equal(colptr, oK.indptr)
-    np.testing.assert_array_equal(rowval, oK.indices)
-    assert rel(nzval, oK.data) < RTOL_BLOCK
+    csc_parity(colptr, rowval, nzval, oK, dofs, diag_exact if apply else None)
     assert rel(rhs, ob) < RTOL_BLOCK
     return K, S, (Vh, Wh, Mh)
 
@@ -65,15 +154,14 @@ def test_golden_figure21(H, oracle, kats, figure_root):
     mesh = H.parse_mesh_triangle(figure_root)
     omesh = oracle.parse_mesh_triangle(figure_root)
     K, S, (Vh, Wh, Mh) = compare_system(H, oracle, mesh, omesh, 1)
-    uhat = H.solve(K, None, tol=1e-14)
-    ref = S.solve()
-    assert rel(uhat, ref) < 1e-12
+    uhat = H.solve(K, None, tol=1e-12, refine=2)
+    ref, _ = check_solution(S, uhat, 1e-13)
     sigma_h, u_h, uhat_h = H.TrialFunction(Vh), H.TrialFunction(Wh), H.TrialFunction(Mh)
     K_e = H.system._LocalView(K, "K")
     H.get_usigma_(sigma_h, u_h, uhat_h, uhat, K_e, None, mesh)
     oq, ou, ouc = S.recover(ref)
-    assert rel(u_h.m_values, ou) < 1e-11
-    assert rel(sigma_h.m_values, oq) < 1e-11
+    assert row_rel(u_h.m_values, ou) < 1e-12
+    assert row_rel(sigma_h.m_values, oq) < 1e-12
     e = H.errornorm(u_h, H.MANUFACTURED_U)
     assert e == pytest.approx(oracle.errornorm(omesh, 1, ou, oracle.MANUFACTURED_U), rel=1e-10)
     assert e <= kats["figure2_1_errornorm_sq_max"]
@@ -84,8 +172,12 @@ def test_rect10_example_bound(H, oracle, kats):
     mesh = H.rectangle_mesh(H.TriangleCell, (10, 10), (0.0, 0.0), (1.0, 1.0))
     uhat, q, u, st = H.solve_poisson(mesh, 1, H.MANUFACTURED_F, tol=1e-13)
     r = oracle.solve_poisson(oracle.rectangle_mesh(10, 10), 1)
-    assert rel(uhat, r["uhat"]) < 1e-11
-    assert rel(u, r["u"]) < 1e-11
+    # the one-call flow stops the CG at 1e-13 (no refinement): its solution is still the oracle
+    # system's to a componentwise backward error below 1e-12
+    oK, ob = r["system"].csc()
+    assert backward_error(oK, ob, uhat) <= BWD_TOL
+    assert rel_l2(uhat, r["uhat"]) < 1e-12
+    assert rel_l2(u, r["u"]) < 1e-12
     e = oracle.errornorm(oracle.rectangle_mesh(10, 10), 1, u, oracle.MANUFACTURED_U)
     assert e <= kats["rect10_errornorm_sq_max"]
 
@@ -96,10 +188,10 @@ def test_rectangle_parity(H, oracle, n, p, qd):
     mesh = H.rectangle_mesh(H.TriangleCell, (n, n), (0.0, 0.0), (1.0, 1.0))
     omesh = oracle.rectangle_mesh(n, n)
     K, S, _ = compare_system(H, oracle, mesh, omesh, p, qd)
-    uhat = H.solve(K, None, tol=1e-14)
-    # the recursive CG residual reaches 1e-14; the true FP64 residual plateaus near 1e-13..1e-12
-    assert K.stats.converged and K.stats.rel_residual < 1e-11
-    assert rel(uhat, S.solve()) < 1e-11
+    uhat = H.solve(K, None, tol=1e-12, refine=2)
+    assert K.stats.converged and K.refine_stats.converged
+    # at these sizes (<= 2*32^2 cells) the two FP64 solutions agree to 1e-12 of the norm as well
+    check_solution(S, uhat, 1e-12)
 
 
 def test_non_square_box(H, oracle):
@@ -160,9 +252,9 @@ def test_dirichlet_projection_and_he_tau_match_oracle(H, oracle, n, p, qd, tau, 
         # He without tau and tau > 1: the trace matrix is indefinite on the free dofs (the oracle's
         # eigenvalues show positive ones), a system for a direct solver, not for CG
         return
-    uhat = H.solve(K, None, tol=1e-14)
+    uhat = H.solve(K, None, tol=1e-12, refine=2)
     assert K.stats.converged
-    assert rel(uhat, S.solve()) < 1e-11
+    check_solution(S, uhat, 1e-12)
 
 
 def test_corrected_options_converge_with_boundary_data(H):
@@ -414,12 +506,11 @@ def test_unstructured_figure1_parity(H, oracle, p, qd):
     mesh = H.parse_mesh_triangle(root)
     omesh = oracle.parse_mesh_triangle(root)
     K, S, (Vh, Wh, Mh) = compare_system(H, oracle, mesh, omesh, p, qd=qd)
-    uhat = H.solve(K, None, tol=1e-14)
-    ref = S.solve()
-    assert rel(uhat, ref) < 1e-11
+    uhat = H.solve(K, None, tol=1e-12, refine=2)
+    ref, _ = check_solution(S, uhat, 1e-12)
     q, u, _ = K.recover()
     oq, ou, _ = S.recover(ref)
-    assert rel(u, ou) < 1e-10 and rel(q, oq) < 1e-10
+    assert rel_l2(u, ou) < 1e-12 and rel_l2(q, oq) < 1e-12
     e = K.errornorm(H.MANUFACTURED_U)
     assert e == pytest.approx(oracle.errornorm(omesh, p, ou, oracle.MANUFACTURED_U, qd=qd), rel=1e-9)
     assert e < {1: 1e-3, 2: 1e-4, 3: 1e-5}[p]
@@ -522,3 +613,63 @@ def test_cg_poisson_path_refuses_bad_inputs(H):
     mesh.set_coordinates(xy)
     with pytest.raises(H.HDGError):
         H.doassemble_cg(Wh, K, dh, H.MANUFACTURED_F)
+
+
+@pytest.mark.parametrize("n,fwd", [(64, 1e-11), (128, 4e-11)])
+def test_scaled_manufactured_parity(H, oracle, n, fwd):
+    """The scaled plain configuration (manufactured Poisson, p = 2, tau = 1, FP64) at 2*64^2 and
+    2*128^2 cells: CSC pattern bit-exact, matrix, rhs and element blocks entry by entry, the trace
+    solution (Jacobi-PCG to 1e-12 + refinement) in backward error and against the per-size forward
+    bound, and the recovered q and u."""
+    mesh = H.rectangle_mesh(H.TriangleCell, (n, n), (0.0, 0.0), (1.0, 1.0))
+    omesh = oracle.rectangle_mesh(n, n)
+    K, S, _ = compare_system(H, oracle, mesh, omesh, 2)
+    uhat = H.solve(K, None, tol=1e-12, refine=2)
+    assert K.stats.converged and K.refine_stats.converged
+    ref, m = check_solution(S, uhat, fwd)
+    q, u, _ = K.recover()
+    oq, ou, _ = S.recover(ref)
+    assert rel_l2(q, oq) <= fwd and rel_l2(u, ou) <= fwd
+
+
+def test_precision_config_shape_parity(H, oracle):
+    """The precision configuration's ingredients on 2*128^2 cells: p = 3, interior nodes jittered by
+    U(-0.2h, 0.2h), kappa = exp(g) with g 64 random Fourier modes (wavelength >= 0.1, RMS 1), a
+    random smooth Fourier source; the FP64 device assembly against the oracle's entry by entry and
+    the trace solution in backward error."""
+    import bench
+    n, p, qd = 128, 3, 6
+    mesh = H.rectangle_mesh(H.TriangleCell, (n, n), (0.0, 0.0), (1.0, 1.0))
+    mesh.jitter(0.2, 4242)
+    omesh = oracle.rectangle_mesh(n, n)
+    omesh.set_xy(H.get_vertices_matrix(mesh))
+    kappa, f = bench.c3_fields(H)
+    K, S, _ = compare_system(H, oracle, mesh, omesh, p, qd, f=f, kappa=kappa)
+    uhat = H.solve(K, None, tol=1e-12, preconditioner=H.PRECOND_AMG, refine=2)
+    ref, m = check_solution(S, uhat, 1e-9)
+    q, u, _ = K.recover()
+    oq, ou, _ = S.recover(ref)
+    assert rel_l2(u, ou) <= 1e-9 and rel_l2(q, oq) <= 1e-9
+
+
+@pytest.mark.parametrize("p", [1, 2])
+def test_unstructured_at_scale_parity(H, oracle, tmp_path, p):
+    """Triangle-format ingestion at scale: a 100,352-cell jittered Delaunay mesh of the unit square
+    written by tests/golden/make_unstructured_mesh.py, read by parse_mesh_triangle on both sides;
+    numbering and face sets bit-exact, trace matrix entry by entry, trace solution in backward error."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    import make_unstructured_mesh as gen
+    root = str(tmp_path / "square")
+    assert gen.write_triangle_mesh(root, 225, 2024) >= 100_000
+    mesh = H.parse_mesh_triangle(root)
+    omesh = oracle.parse_mesh_triangle(root)
+    xy, cn, cf, fc = mesh._topology()
+    assert np.array_equal(cf, omesh.cell_faces) and np.array_equal(fc, omesh.faces) and np.array_equal(xy, omesh.xy)
+    assert sorted(H.getfaceset(mesh, "boundary")) == omesh.faceset("boundary").tolist()
+    K, S, _ = compare_system(H, oracle, mesh, omesh, p)
+    uhat = H.solve(K, None, tol=1e-12, preconditioner=H.PRECOND_AMG, refine=2)
+    ref, m = check_solution(S, uhat, 1e-10)
+    q, u, _ = K.recover()
+    oq, ou, _ = S.recover(ref)
+    assert rel_l2(u, ou) <= 1e-10

@@ -266,3 +266,58 @@ def test_dofhandler_and_dirichlet_match_cg_oracle(H, oracle, order):
     assert np.array_equal(dh.cell_dofs.reshape(cd.shape), cd)
     dbc = H.Dirichlet(u, dh, "boundary", lambda x: 0.0)
     assert np.array_equal(dbc.prescribed_dofs, cgref.boundary_dofs(om, cd, order))
+
+
+def test_bench_workload_generator_matches_library(H, oracle):
+    """The batching workload that bench.py's reference arm builds with numpy and the oracle alone
+    (no libhdg) is the one the GPU arm builds through the library: the same jittered coordinates
+    (splitmix64 stream of hdg_mesh_jitter) and the same source parameters, bit for bit."""
+    import bench
+    specs = bench.c4_specs()
+    probs = bench.c4_problems(H)
+    assert len(specs) == len(probs) == 256
+    for k in (0, 1, 17, 100, 255):
+        s, pr = specs[k], probs[k]
+        assert (s["n"], s["p"], s["qd"]) == (pr.n, pr.p, pr.qd())
+        assert np.array_equal(np.asarray(pr.f.params), s["bumps"])
+        assert np.array_equal(pr.kappa_cell, s["kappa_cell"])
+        xy_lib = H.batch.host_mesh(pr)._topology()[0]
+        om = oracle.rectangle_mesh(s["n"], s["n"])
+        xy_np = bench.jitter_rect_xy(om.xy, s["n"], s["jitter"], s["seed"])
+        assert np.array_equal(xy_lib, xy_np), k
+
+
+def test_bench_cpu_sample_is_stratified():
+    import bench
+    specs = bench.c4_specs()
+    idx = bench.c4_cpu_sample_indices(specs)
+    assert len(idx) == len(set(idx)) == 48
+    sizes = sorted(specs[k]["n"] for k in idx)
+    alln = sorted(s["n"] for s in specs)
+    assert sizes[0] <= alln[len(alln) // 40] and sizes[-1] >= alln[-len(alln) // 40 - 1]
+
+
+@pytest.mark.parametrize("kind,prm,code,word", [
+    (2, [3.0, 0.5, 0.5, 0.1, 1.0], -1, b"BUMPS"),        # K = 3 bumps, parameters for one
+    (1, [1.0], -1, b"SINSIN"),                          # sin sin needs a, kx, ky
+    (3, [2.0, 0.0, 1.0, 1.0, 0.0, 1.0], -1, b"FOURIER"),  # K = 2 modes, parameters for one
+    (4, [-1.0, 0.0], -1, b"FOURIER"),                   # negative mode count
+    (9, [1.0], -1, b"unknown kind"),
+    (0, [], -1, b"CONST"),                              # a constant needs its value
+    (0, [1.0] * 5000, -12, b"field parameters"),         # over the scratch capacity
+])
+def test_field_parameters_checked_before_device_work(H, kind, prm, code, word):
+    """A field whose parameters do not cover what its kind reads is refused on the host, before any
+    CUDA call (this runs without a GPU): the device evaluator would otherwise read past the
+    parameters.  The no-allocation error norm also refuses a count over its fixed capacity."""
+    import ctypes as C
+    lib = H._lib.load()
+    arr = np.ascontiguousarray(prm, dtype=np.float64) if prm else np.zeros(1)
+    fc = H._lib.hdg_field(kind, len(prm), arr.ctypes.data_as(C.POINTER(C.c_double)))
+    dummy = (C.c_double * 8)()
+    out = C.c_double(-7.0)
+    rc = lib.hdg_errornorm_l2sq_noalloc(0, None, 1, 0, 1, C.addressof(dummy), C.addressof(dummy),
+                                        C.addressof(dummy), C.byref(fc), C.byref(out))
+    assert rc == code
+    assert word in lib.hdg_noalloc_last_error()
+    assert out.value == -7.0

@@ -6,6 +6,7 @@ test/test_basis.jl, examples/poisson2D_HDG.jl); the oracle must reproduce them b
 result is compared with it.
 """
 import math
+import os
 
 import numpy as np
 import pytest
@@ -188,3 +189,58 @@ def test_he_tau_option_is_the_reference_at_tau_one(oracle):
         D = (K3 - K2).toarray()
         assert np.abs(D - np.diag(np.diag(D))).max() < 1e-12 * np.abs(D).max()
         assert np.all(np.diag(D) < 0)
+
+
+def test_double_double_residual_is_exact(oracle):
+    """csc_residual_dd (the residual the refinement of both the oracle's direct solve and the
+    device's hdg_refine relies on) equals b - K x computed in exact rational arithmetic, rounded
+    once, on a matrix whose products and sums round in plain FP64."""
+    import scipy.sparse as sp
+    from fractions import Fraction
+    rng = np.random.default_rng(5)
+    n = 40
+    K = sp.random(n, n, density=0.2, random_state=7, format="csc") + sp.identity(n, format="csc") * 3.0
+    K.data *= 1.0 + rng.standard_normal(K.nnz) * 1e-3
+    x = rng.standard_normal(n) * np.exp(rng.uniform(-10, 10, n))
+    b = K @ x  # FP64: the exact residual is the rounding error of this product
+    r = oracle.csc_residual_dd(K, x, b)
+    Kc = K.tocsc()
+    exact = [Fraction(v) for v in b]
+    for j in range(n):
+        for q in range(Kc.indptr[j], Kc.indptr[j + 1]):
+            exact[Kc.indices[q]] -= Fraction(Kc.data[q]) * Fraction(x[j])
+    want = np.array([float(v) for v in exact])
+    assert np.any(want != 0.0)
+    scale = np.abs(Kc) @ np.abs(x)
+    assert np.all(np.abs(r - want) <= 1e-28 * scale + 1e-300)
+
+
+def test_trace_solution_sensitivity_to_ulp_changes(oracle):
+    """The trace system's solution is sensitive at the 1e-13 level to one-ulp changes of K's entries
+    on 2*64^2 cells (p = 2), and the sensitivity grows with the mesh (3e-12 on 2*256^2 cells was
+    measured with the same construction), so two FP64 assemblies of K that are not bit-identical
+    cannot agree on the solution to 1e-12 at the scaled configuration; the comparison of solutions
+    is therefore made in backward error.  Also pins that the refined direct solve has a backward
+    error at the 1e-16 level."""
+    import scipy.sparse.linalg as spla
+    rng = np.random.default_rng(0)
+    m = oracle.rectangle_mesh(64, 64)
+    S = oracle.System(m, 2, None, 1.0, oracle.MANUFACTURED_F, threads=os.cpu_count() or 1)
+    S.apply(*S.dirichlet())
+    K, b = S.csc()
+
+    def solve(K_):
+        lu = spla.splu(K_.tocsc(), permc_spec="MMD_AT_PLUS_A", diag_pivot_thresh=0.001)
+        x = lu.solve(b)
+        for _ in range(3):
+            x = x + lu.solve(oracle.csc_residual_dd(K_, x, b))
+        return x
+    x0 = solve(K)
+    r = oracle.csc_residual_dd(K, x0, b)
+    den = abs(K) @ np.abs(x0) + np.abs(b)
+    assert np.all(r[den == 0] == 0) and (np.abs(r[den > 0]) / den[den > 0]).max() < 1e-15
+    K1 = K.copy()
+    K1.data = K1.data * (1.0 + 2.0 ** -53 * rng.choice([-1.0, 1.0], K1.nnz))
+    x1 = solve(K1)
+    d = np.linalg.norm(x1 - x0) / np.linalg.norm(x0)
+    assert 1e-14 < d < 1e-12, d
