@@ -612,7 +612,7 @@ int hdg_dirichlet(const hdg_space* sp, const char* faceset, const hdg_field* g, 
     int fl = 0;
     while (m->cfaces[3 * c + fl] != f) ++fl;
     const bool o = m->cells[3 * c + EN[fl][1]] > m->cells[3 * c + EN[fl][0]];
-    // the reference's projection (src/boundary.jl:232-242): the accumulator N runs across the
+    // the reference's projection (src/boundary.jl:27-37): the accumulator N runs across the
     // basis functions of a face, the weights are the parent's volume weights, no |e|
     double acc = 0.0;
     for (int i = 0; i < nt; ++i) {

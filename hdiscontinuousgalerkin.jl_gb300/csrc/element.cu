@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(EWARPS * 32) k_element_condense(ElemArgs a) {
   __syncthreads();
 
   for (int e = blockIdx.x * EWARPS + warp; e < a.nc; e += gridDim.x * EWARPS) {
-    // ---- geometry (reinit!, src/ScalarFunctionSpaces.jl:251-282) -------------------------
+    // ---- geometry (reinit!, src/ScalarFunctionSpaces.jl:101-132) -------------------------
     int nid = (lane < 3) ? a.cells[3 * e + lane] : 0;
     double px = 0.0, py = 0.0;
     if (lane < 3) {

@@ -12,7 +12,7 @@
 //     top = k+1, D, right = k+2 with k = base+1+[i=1]+[j=1].
 // The face table rows [v1 v2 c1 c2] keep the vertex order of the creating cell, as the
 // reference does.  Triangle-format meshes use the generic first-visit hash construction
-// (src/triangle_mesh.jl:94-154).
+// (src/triangle_mesh.jl:48-108).
 #include <algorithm>
 #include <cmath>
 #include <cstring>

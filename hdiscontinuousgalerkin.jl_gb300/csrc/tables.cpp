@@ -1,7 +1,7 @@
 // Reference-element tables of the HDG spaces, built once per (p, quad_degree) on the host in FP64.
 //
-// The function spaces of the reference (src/ScalarFunctionSpaces.jl:181-249,
-// src/VectorFunctionSpaces.jl:10-18, src/TraceFunctionSpaces.jl:74-91) cache basis values at
+// The function spaces of the reference (src/ScalarFunctionSpaces.jl:31-99,
+// src/VectorFunctionSpaces.jl:10-18, src/TraceFunctionSpaces.jl:11-28) cache basis values at
 // the quadrature points and re-multiply them per cell.  On an affine triangle every element
 // integral of examples/poisson2D_HDG.jl:88-153 is a small combination of a few fixed
 // reference matrices, so this file also packs those matrices for the device:

@@ -179,7 +179,7 @@ __global__ void k_gather_rhs(const int nf, const int32_t* __restrict__ fcell, co
   b[t] = v;
 }
 
-// meandiag(K) = mean |K_ii| of each problem (src/boundary.jl:374-380), a deterministic
+// meandiag(K) = mean |K_ii| of each problem (src/boundary.jl:169-175), a deterministic
 // per-problem reduction over the segments.
 template <int NT>
 __global__ void k_meandiag(SegArgs g, const int32_t* __restrict__ prob_row0, const int nf,
@@ -196,7 +196,7 @@ __global__ void k_meandiag(SegArgs g, const int32_t* __restrict__ prob_row0, con
     mdiag[P] = s0 / (double)(prob_row0[P + 1] - prob_row0[P]);
 }
 
-// b -= sum_d v_d K[:, d] over prescribed dofs with v_d != 0 (src/boundary.jl:334-343); gv holds
+// b -= sum_d v_d K[:, d] over prescribed dofs with v_d != 0 (src/boundary.jl:128-137); gv holds
 // v at prescribed dofs and 0 elsewhere, so this is one sparse product with gv.
 template <int NT>
 __global__ void k_lift(const int nf, const int32_t* __restrict__ bcol5, const double* __restrict__ val,
@@ -215,7 +215,7 @@ __global__ void k_lift(const int nf, const int32_t* __restrict__ bcol5, const do
   b[r] -= s;
 }
 
-// Rows and columns of prescribed dofs zeroed, K[d,d] = m, b[d] = v m (src/boundary.jl:344-362).
+// Rows and columns of prescribed dofs zeroed, K[d,d] = m, b[d] = v m (src/boundary.jl:138-157).
 // The result is stored in "solver form": free rows negated, so that the matrix the CG sees is
 // symmetric positive definite (the condensed HDG trace operator is negative definite on the free
 // dofs).  hdg_system_get_csc undoes the sign when exporting.

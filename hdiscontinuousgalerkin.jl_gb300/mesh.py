@@ -11,17 +11,17 @@ import numpy as np
 from . import _lib as L
 from .context import default_context
 
-Cell = namedtuple("Cell", ["nodes", "faces"])  # 1-based ids, src/mesh.jl:201-204
+Cell = namedtuple("Cell", ["nodes", "faces"])  # 1-based ids, src/mesh.jl:17-20
 Node = namedtuple("Node", ["x"])
 
 
 class TriangleCell:
-    """Cell{2,3,3}: marker type for rectangle_mesh(TriangleCell, ...), src/mesh.jl:208."""
+    """Cell{2,3,3}: marker type for rectangle_mesh(TriangleCell, ...), src/mesh.jl:24."""
     reference_edge_nodes = ((2, 3), (3, 1), (1, 2))
 
 
 class PolygonalMesh:
-    """PolygonalMesh{2,3,3,2,Float64} (src/mesh.jl:227-233) backed by an hdg_mesh handle."""
+    """PolygonalMesh{2,3,3,2,Float64} (src/mesh.jl:43-49) backed by an hdg_mesh handle."""
 
     def __init__(self, handle, ctx):
         self._h = handle
@@ -166,7 +166,7 @@ def _records(path):
 
 
 def parse_mesh_triangle(root_file: str, ctx="default") -> PolygonalMesh:
-    """parse_mesh_triangle(root_file) (src/triangle_mesh.jl:161-172): .node, .edge, .ele files."""
+    """parse_mesh_triangle(root_file) (src/triangle_mesh.jl:115-126): .node, .edge, .ele files."""
     nodes = [(float(r[1]), float(r[2])) for r in _records(root_file + ".node")]
     edges = [(int(r[1]), int(r[2]), int(r[3])) for r in _records(root_file + ".edge")]
     cells = [(int(r[1]), int(r[2]), int(r[3])) for r in _records(root_file + ".ele")]

@@ -43,7 +43,7 @@ class Legendre:
 
 
 class GenericFiniteElement:
-    """GenericFiniteElement(func_basis) with P1 Lagrange geometry (src/FiniteElement.jl:128-147)."""
+    """GenericFiniteElement(func_basis) with P1 Lagrange geometry (src/FiniteElement.jl:8-27)."""
 
     def __init__(self, basis):
         self.basis = basis
@@ -150,7 +150,7 @@ class _CellState:
 
 
 class ScalarFunctionSpace:
-    """ScalarFunctionSpace(mesh, fe; quad_degree = order+1) (src/ScalarFunctionSpaces.jl:174-179)."""
+    """ScalarFunctionSpace(mesh, fe; quad_degree = order+1) (src/ScalarFunctionSpaces.jl:24-29)."""
 
     def __init__(self, mesh, fe, update_face_data: bool = True, quad_degree: int | None = None):
         self.mesh, self.fe = mesh, fe
@@ -185,7 +185,7 @@ class VectorFunctionSpace(ScalarFunctionSpace):
 
 
 class ScalarTraceFunctionSpace:
-    """ScalarTraceFunctionSpace(Wh, fe_trace) (src/TraceFunctionSpaces.jl:74-91)."""
+    """ScalarTraceFunctionSpace(Wh, fe_trace) (src/TraceFunctionSpaces.jl:11-28)."""
 
     def __init__(self, parent: ScalarFunctionSpace, fe):
         if fe.order != parent.order:

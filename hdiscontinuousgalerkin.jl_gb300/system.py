@@ -1,7 +1,7 @@
 """The HDG Poisson flow of examples/poisson2D_HDG.jl on the GPU:
 
     K, b, K_e, b_e = doassemble(Vh, Wh, Mh, tau, f)       # :58-186 (device)
-    apply_(K, b, dbc)                                      # apply!, src/boundary.jl:326-363
+    apply_(K, b, dbc)                                      # apply!, src/boundary.jl:121-158
     uhat = solve(K, b)                                     # K \\ b, :195 (device CG)
     get_usigma_(sigma_h, u_h, uhat_h, uhat, K_e, b_e, mesh)  # get_uσ!, :197-212
     errornorm(u_h, u_ex)                                   # src/DiscreteFunctions.jl:97-120
@@ -201,12 +201,12 @@ def doassemble(Vh: VectorFunctionSpace, Wh: ScalarFunctionSpace, Mh: ScalarTrace
 
 
 class Dirichlet:
-    """Dirichlet(û_h, mesh, faceset, g) on the trace space (src/boundary.jl:212-247), or
+    """Dirichlet(û_h, mesh, faceset, g) on the trace space (src/boundary.jl:11-42), or
     Dirichlet(u, dh, faceset, g) on a nodal field of a DofHandler (src/boundary.jl:44-95)."""
 
     def __init__(self, u, mesh, faceset: str, g=None, projection: str = "reference"):
         """projection="l2" takes the L2 projection of g onto the trace basis (hdg_dirichlet_l2)
-        instead of the reference's accumulation (src/boundary.jl:232-242)."""
+        instead of the reference's accumulation (src/boundary.jl:27-37)."""
         from .dofhandler import DofHandler, DirichletDH
         if isinstance(mesh, DofHandler):
             d = DirichletDH(u, mesh, faceset, g if g is not None else (lambda x: 0.0))
@@ -229,7 +229,7 @@ class Dirichlet:
 
 
 def apply_(K, b, dbc: Dirichlet):
-    """apply!(K, b, dbc) (src/boundary.jl:121-158, :326-363) on the device system: the HDG
+    """apply!(K, b, dbc) (src/boundary.jl:121-158, :121-158) on the device system: the HDG
     TraceSystem of doassemble or the LagrangeSystem of doassemble_cg (b is refreshed in place)."""
     from .lagrange import LagrangeSystem
     if isinstance(K, LagrangeSystem):
@@ -297,7 +297,7 @@ def errornorm(u_h: TrialFunction, u_ex, norm_type: str = "L2") -> float:
 
 
 class CellIterator:
-    """CellIterator(mesh) (src/iterator.jl:130-177): yields itself with current_cellid, nodes, coords."""
+    """CellIterator(mesh) (src/iterator.jl:10-65): yields itself with current_cellid, nodes, coords."""
 
     def __init__(self, mesh):
         self.mesh = mesh

@@ -24,15 +24,15 @@ extern "C" {
 enum {
   HDG_OK = 0,
   HDG_ERR_ARG = -1,            /* invalid argument / size */
-  HDG_ERR_NEG_DETJ = -2,       /* ArgumentError("det(J) is not positive"), src/ScalarFunctionSpaces.jl:260 */
+  HDG_ERR_NEG_DETJ = -2,       /* ArgumentError("det(J) is not positive"), src/ScalarFunctionSpaces.jl:110 */
   HDG_ERR_BAD_ORDER = -3,      /* ArgumentError("Quadrature rule of order … not available"), src/quadrature.jl:24 */
-  HDG_ERR_NOT_BOUNDARY = -4,   /* "Face … is not in boundary", src/boundary.jl:227 / generate_mesh.jl:80 */
+  HDG_ERR_NOT_BOUNDARY = -4,   /* "Face … is not in boundary", src/boundary.jl:22 / generate_mesh.jl:80 */
   HDG_ERR_NO_CONVERGENCE = -5, /* CG reached maxit (no reference counterpart: the reference solves directly) */
   HDG_ERR_OOM = -6,            /* device allocation failed */
   HDG_ERR_CUDA = -7,           /* CUDA runtime error */
   HDG_ERR_SINGULAR = -8,       /* a local system had a zero pivot (LAPACK SingularException) */
   HDG_ERR_BREAKDOWN = -9,      /* CG breakdown: p'Ap <= 0 (trace system not definite) */
-  HDG_ERR_UNKNOWN_SET = -10,   /* KeyError on a face set name, src/mesh.jl:259 */
+  HDG_ERR_UNKNOWN_SET = -10,   /* KeyError on a face set name, src/mesh.jl:75 */
   HDG_ERR_TIMEOUT = -11,       /* a bounded device wait gave up */
   HDG_ERR_CAPACITY = -12       /* a request exceeds a fixed capacity (admission budget, scratch size) */
 };
@@ -87,7 +87,7 @@ int hdg_ctx_set_profiling(hdg_ctx* ctx, int on);
  * queried, but no space can be built on it. */
 int hdg_mesh_rectangle(hdg_ctx* ctx, int nx, int ny, const double LL[2], const double UR[2], hdg_mesh** out);
 /* Triangle-format mesh from already-parsed arrays: parse_cells! face construction,
- * src/triangle_mesh.jl:94-154.  cell_nodes: ncells x 3 (1-based); edges: nedges x 3
+ * src/triangle_mesh.jl:48-108.  cell_nodes: ncells x 3 (1-based); edges: nedges x 3
  * (v1, v2, boundary marker) as in the .edge file. */
 int hdg_mesh_from_cells(hdg_ctx* ctx, int nnodes, const double* xy, int ncells, const int32_t* cell_nodes,
                         int nedges, const int32_t* edges, hdg_mesh** out);
@@ -97,11 +97,11 @@ int hdg_mesh_set_coordinates(hdg_mesh* mesh, const double* xy);
 int hdg_mesh_jitter(hdg_mesh* mesh, double a, uint64_t seed);
 int hdg_mesh_sizes(const hdg_mesh* mesh, int* nnodes, int* ncells, int* nfaces);
 /* Node coordinates (nnodes x 2), cell nodes and faces (ncells x 3, 1-based), and the face
- * table rows [v1 v2 cell1 cell2] (nfaces x 4, cell2 = 0 on the boundary), src/mesh.jl:227-233.
+ * table rows [v1 v2 cell1 cell2] (nfaces x 4, cell2 = 0 on the boundary), src/mesh.jl:43-49.
  * Any pointer may be NULL. */
 int hdg_mesh_get_topology(const hdg_mesh* mesh, double* xy, int32_t* cell_nodes, int32_t* cell_faces,
                           int32_t* faces);
-/* getfaceset(mesh, name), sorted ascending, 1-based: src/mesh.jl:259.  out may be NULL. */
+/* getfaceset(mesh, name), sorted ascending, 1-based: src/mesh.jl:75.  out may be NULL. */
 int hdg_mesh_faceset(const hdg_mesh* mesh, const char* name, int32_t* out, int* count);
 int hdg_mesh_destroy(hdg_mesh* mesh);
 
@@ -109,7 +109,7 @@ int hdg_mesh_destroy(hdg_mesh* mesh);
 /* The triple (ScalarFunctionSpace, VectorFunctionSpace, ScalarTraceFunctionSpace) of
  * examples/poisson2D_HDG.jl:41-44 over one mesh: Dubiner degree p for u and q (component-major
  * vector dofs), Legendre degree p on the edges.  quad_degree <= 0 selects the reference default
- * p+1 (src/ScalarFunctionSpaces.jl:174-179). */
+ * p+1 (src/ScalarFunctionSpaces.jl:24-29). */
 int hdg_space_create(hdg_mesh* mesh, int p, int quad_degree, hdg_space** out);
 /* getnbasefunctions of W, V and M; getnquadpoints; getnfacequadpoints. */
 int hdg_space_info(const hdg_space* space, int* nw, int* nv, int* nt, int* nq, int* nfq);
@@ -118,7 +118,7 @@ int hdg_space_info(const hdg_space* space, int* nw, int* nv, int* nt, int* nq, i
 int hdg_space_tables(const hdg_space* space, double* pts, double* w, double* N, double* dN, double* fpts,
                      double* fw, double* E, double* T);
 /* reinit!(fs, cell) geometry on the host: detJ, Jinv (2x2), detJf (3), unit normals (3x2).
- * src/ScalarFunctionSpaces.jl:251-282.  cell is 1-based. */
+ * src/ScalarFunctionSpaces.jl:101-132.  cell is 1-based. */
 int hdg_space_cell_geometry(const hdg_space* space, int cell, double* detJ, double* Jinv, double* detJf,
                             double* normals);
 int hdg_space_destroy(hdg_space* space);
@@ -148,7 +148,7 @@ int hdg_system_get_csc(const hdg_system* sys, int base, int64_t* colptr, int64_t
 int hdg_system_get_element_blocks(const hdg_system* sys, double* Ate, double* bte, double* Ke, double* be);
 
 /* ---- boundary conditions ------------------------------------------------------------- */
-/* Dirichlet(u_hat, mesh, faceset, g), src/boundary.jl:212-247: prescribed trace dofs (1-based)
+/* Dirichlet(u_hat, mesh, faceset, g), src/boundary.jl:11-42: prescribed trace dofs (1-based)
  * and values.  The values follow the reference's projection exactly (its accumulator is not
  * reset between basis functions); they are all 0 for g = 0, the case every example uses.
  * dofs/vals may be NULL to query count. */
@@ -156,14 +156,14 @@ int hdg_dirichlet(const hdg_space* space, const char* faceset, const hdg_field* 
                   int* count);
 /* The corrected trace projection: u_i = int_0^1 g mu_i ds on every face of the set, the L2
  * projection onto the orthonormal Legendre basis (same arguments and dof order as hdg_dirichlet,
- * which keeps the reference's projection, src/boundary.jl:232-242, for parity). */
+ * which keeps the reference's projection, src/boundary.jl:27-37, for parity). */
 int hdg_dirichlet_l2(const hdg_space* space, const char* faceset, const hdg_field* g, int32_t* dofs, double* vals,
                      int* count);
 /* on != 0: systems assembled from this space from now on use He = tau int mu mu dS in the
  * condensation (each system keeps the choice it was created with, also when reassembled).  The
  * reference's He carries no tau (examples/poisson2D_HDG.jl:149), consistent only for tau = 1. */
 int hdg_space_set_he_tau(hdg_space* space, int on);
-/* apply!(K, b, dbc), src/boundary.jl:326-363 (APPLY_TRANSPOSE): b -= v K[:,d]; zero rows and
+/* apply!(K, b, dbc), src/boundary.jl:121-158 (APPLY_TRANSPOSE): b -= v K[:,d]; zero rows and
  * columns of the prescribed dofs; K[d,d] = mean|diag K|; b[d] = v * mean|diag K|. */
 int hdg_apply_dirichlet(hdg_system* sys, const int32_t* dofs, const double* vals, int n);
 

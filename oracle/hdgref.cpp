@@ -16,7 +16,7 @@
 //     Legendre three-term recurrence in long double (ascending nodes), call site
 //     src/quadrature.jl:30.
 //   * Tensors.jl (REQUIRE: >= 0.8.0) forward-mode `gradient`: a dual-number type, call sites
-//     src/ScalarFunctionSpaces.jl:215,232,235.
+//     src/ScalarFunctionSpaces.jl:65,82,85.
 //   * LinearAlgebra `factorize` on a general square matrix = LU with partial pivoting
 //     (examples/poisson2D_HDG.jl:160); restated as a textbook right-looking getrf.
 //   * SparseArrays `sparse(I,J,V)` = COO -> CSC with duplicates summed (src/assembler.jl:48).
@@ -302,8 +302,8 @@ struct Tables {
   std::vector<double> T;    // [nt][nfq]
 };
 
-// _scalar_fs tables (src/ScalarFunctionSpaces.jl:181-249) + trace tables
-// (src/TraceFunctionSpaces.jl:74-91); face points via src/quadrature.jl:60-75.
+// _scalar_fs tables (src/ScalarFunctionSpaces.jl:31-99) + trace tables
+// (src/TraceFunctionSpaces.jl:11-28); face points via src/quadrature.jl:60-75.
 bool build_tables(int p, int qd, Tables* t) {
   t->p = p;
   t->qd = qd;
@@ -422,7 +422,7 @@ void build_cell(Mesh& m, std::map<std::pair<int, int>, int>& dict, const int el[
       m.faces.push_back(0);
       dict[key] = fid;
       ef[i] = fid;
-      if (markers && boundary_new) {  // src/triangle_mesh.jl:126-142
+      if (markers && boundary_new) {  // src/triangle_mesh.jl:81-96
         auto mk = markers->find(key);
         if (mk != markers->end() && mk->second > 0) boundary_new->push_back(fid);
       }
@@ -491,7 +491,7 @@ void* hr_rect_mesh(int nx, int ny, double llx, double lly, double urx, double ur
   return m;
 }
 
-// parse_cells! face construction for a Triangle-format mesh, src/triangle_mesh.jl:94-154.
+// parse_cells! face construction for a Triangle-format mesh, src/triangle_mesh.jl:48-108.
 // The text parsing itself is done by the Python side of the oracle.
 void* hr_mesh_from_triangle(int nn, const double* xy, int nc, const int* ele, int ne, const int* edges) {
   Mesh* m = new Mesh();
@@ -595,7 +595,7 @@ int hr_rule(int kind, int order, double* x, double* y, double* w) {
 
 namespace {
 
-// reinit!(::ScalarFunctionSpace, x), src/ScalarFunctionSpaces.jl:251-282 (+ weighted_normal
+// reinit!(::ScalarFunctionSpace, x), src/ScalarFunctionSpaces.jl:101-132 (+ weighted_normal
 // src/shapes.jl:80-87).  P1 geometry: dMdξ = (-1,-1),(1,0),(0,1).
 struct Geo {
   double detJ, J[2][2], Jinv[2][2], detJf[3], nrm[3][2];
@@ -652,7 +652,7 @@ void element_blocks(const Mesh& m, const Tables& t, int c, double tau, const Fie
   b->nw = nw; b->nv = nv; b->nt = nt; b->m = mm; b->n = nv + nw;
   b->A.assign(nv * nv, 0); b->B.assign(nv * nw, 0); b->C.assign(nw * nw, 0);
   b->E.assign(nv * mm, 0); b->F.assign(nw * mm, 0); b->H.assign(mm * mm, 0); b->be.assign(nw, 0);
-  // shape_gradient / dNdx = dNdξ ⋅ Jinv, src/ScalarFunctionSpaces.jl:264-266
+  // shape_gradient / dNdx = dNdξ ⋅ Jinv, src/ScalarFunctionSpaces.jl:114-116
   std::vector<double> dNdx(nw * t.nq * 2);
   for (int i = 0; i < nw; ++i)
     for (int q = 0; q < t.nq; ++q)
@@ -664,7 +664,7 @@ void element_blocks(const Mesh& m, const Tables& t, int c, double tau, const Fie
   const double* X[3] = {&m.xy[2 * (nd[0] - 1)], &m.xy[2 * (nd[1] - 1)], &m.xy[2 * (nd[2] - 1)]};
   // Cell integrals, examples/poisson2D_HDG.jl:88-104
   for (int q = 0; q < t.nq; ++q) {
-    double dO = g.detJ * t.vol.w[q];  // getdetJdV, src/ScalarFunctionSpaces.jl:288
+    double dO = g.detJ * t.vol.w[q];  // getdetJdV, src/ScalarFunctionSpaces.jl:138
     double xq = 0, yq = 0;            // spatial_coordinate, src/DiscreteFunctions.jl:16-24
     for (int i = 0; i < 3; ++i) {
       xq += t.M[i * t.nq + q] * X[i][0];
@@ -699,7 +699,7 @@ void element_blocks(const Mesh& m, const Tables& t, int c, double tau, const Fie
   for (int f = 0; f < 3; ++f) {
     bool o = orientation(m, c, f);
     for (int q = 0; q < nfq; ++q) {
-      double dS = g.detJf[f] * t.face.w[q];  // getfacedetJdS, src/ScalarFunctionSpaces.jl:302
+      double dS = g.detJf[f] * t.face.w[q];  // getfacedetJdS, src/ScalarFunctionSpaces.jl:152
       int qf = o ? q : nfq - 1 - q;          // shape_value(..., orientation), :303
       for (int i = 0; i < nw; ++i) {
         double w = t.E[(i * nfq + q) * 3 + f];
@@ -707,7 +707,7 @@ void element_blocks(const Mesh& m, const Tables& t, int c, double tau, const Fie
         double wf = t.E[(i * nfq + qf) * 3 + f];
         for (int j = 0; j < nt; ++j) b->F[i * mm + nt * f + j] += (tau * (t.T[j * nfq + q] * wf)) * dS;
       }
-      // trace space shares the parent's detJf (src/TraceFunctionSpaces.jl:97)
+      // trace space shares the parent's detJf (src/TraceFunctionSpaces.jl:34)
       for (int i = 0; i < nv; ++i) {
         int ci = i / nw, ai = i % nw;
         double vn = t.E[(ai * nfq + qf) * 3 + f] * g.nrm[f][ci];  // v ⋅ n, src/VectorFunctionSpaces.jl:50-57
@@ -970,7 +970,7 @@ void hr_system_local(const void* sv, double* Ke, double* be) {
   if (be) std::memcpy(be, S->be.data(), S->be.size() * 8);
 }
 
-// Dirichlet(::ScalarTraceFunctionSpace, mesh, faceset, g), src/boundary.jl:216-247, kept
+// Dirichlet(::ScalarTraceFunctionSpace, mesh, faceset, g), src/boundary.jl:11-42, kept
 // with its projection as written (accumulator not reset per basis function, parent volume
 // weights, no detJf).  Fills dofs (1-based) and values; returns the count.
 int hr_dirichlet(const void* mv, int p, int qd, const char* faceset, int gkind, int gnp, const double* gprm, int* dofs,
@@ -996,7 +996,7 @@ int hr_dirichlet(const void* mv, int p, int qd, const char* faceset, int gkind, 
     double N = 0.0;
     for (int i = 0; i < nt; ++i) {
       for (int q = 0; q < nfq; ++q) {
-        int oq = o ? q : nfq - 1 - q;  // spatial_coordinate(fs, face, q, x, orientation), src/TraceFunctionSpaces.jl:110-120
+        int oq = o ? q : nfq - 1 - q;  // spatial_coordinate(fs, face, q, x, orientation), src/TraceFunctionSpaces.jl:43-57
         double s = t.face.x[oq];
         // L = P1 geometry at the face point of local edge fl
         double ex = (1.0 - s) * REF_EDGE[fl][0][0] + s * REF_EDGE[fl][1][0];
@@ -1063,7 +1063,7 @@ int hr_dirichlet_l2(const void* mv, int p, int qd, const char* faceset, int gkin
   return k;
 }
 
-// apply!(K, f, dbc) with APPLY_TRANSPOSE, src/boundary.jl:326-380.
+// apply!(K, f, dbc) with APPLY_TRANSPOSE, src/boundary.jl:121-175.
 void hr_apply(void* sv, int nd, const int* dofs1, const double* vals) {
   System* S = (System*)sv;
   const int N = S->ndofs;

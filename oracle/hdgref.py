@@ -4,7 +4,7 @@ TEST INFRASTRUCTURE ONLY.  Loaded by tests/, ``__graft_entry__.smoke()`` and ben
 CPU-baseline leg as the test oracle; the product never imports it.
 
 The C++ half (``hdgref.cpp``) restates the reference's element loop, condensation and
-assembly; this half restates the Triangle-format reader (src/triangle_mesh.jl:47-172) and
+assembly; this half restates the Triangle-format reader (src/triangle_mesh.jl:1-126) and
 performs the global solve ``K \\ b`` (examples/poisson2D_HDG.jl:195) with scipy's SuperLU,
 standing in for the UMFPACK LU that Julia's SparseArrays uses for a non-Hermitian matrix.
 """
@@ -105,7 +105,7 @@ def _field(spec):
 
 
 class Mesh:
-    """Oracle mesh (1-based ids, as in the reference's PolygonalMesh, src/mesh.jl:227-233)."""
+    """Oracle mesh (1-based ids, as in the reference's PolygonalMesh, src/mesh.jl:43-49)."""
 
     def __init__(self, handle):
         if not handle:
@@ -180,7 +180,7 @@ def _records(path):
 
 
 def parse_mesh_triangle(root: str) -> Mesh:
-    """parse_mesh_triangle(root_file), src/triangle_mesh.jl:161-172."""
+    """parse_mesh_triangle(root_file), src/triangle_mesh.jl:115-126."""
     nodes = [_read_line(ln, (int, float, float, int))[1:3] for ln in _records(root + ".node")]
     edges = [_read_line(ln, (int, int, int, int))[1:4] for ln in _records(root + ".edge")]
     cells = [_read_line(ln, (int, int, int, int))[1:4] for ln in _records(root + ".ele")]

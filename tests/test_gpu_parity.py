@@ -308,7 +308,7 @@ def test_error_paths(H):
     with pytest.raises(H.HDGError) as e:
         H.solve(K, b, maxit=2, chunk=1)
     assert e.value.code == -5
-    # a flipped cell: det(J) <= 0 (src/ScalarFunctionSpaces.jl:260)
+    # a flipped cell: det(J) <= 0 (src/ScalarFunctionSpaces.jl:110)
     xy = H.get_vertices_matrix(mesh)
     xy[6] = xy[6] + np.array([0.6, 0.6])
     mesh.set_coordinates(xy)

@@ -321,3 +321,17 @@ def test_field_parameters_checked_before_device_work(H, kind, prm, code, word):
     assert rc == code
     assert word in lib.hdg_noalloc_last_error()
     assert out.value == -7.0
+
+
+def test_reference_citations_point_inside_the_cited_files():
+    """Every src/, examples/ or test/ citation with line numbers in the repository's sources and
+    documents lies inside the cited reference file (skipped where the reference tree is absent)."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import check_citations as cc
+    tree = cc.reference_tree([])
+    if not tree:
+        pytest.skip("reference tree not present")
+    n, bad = cc.check(tree)
+    assert n > 100
+    assert not bad, "\n".join(bad)

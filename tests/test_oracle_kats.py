@@ -112,7 +112,7 @@ def test_bases(oracle):
             d0 += (a - b) ** 2 * wi
             d1 += ((ga - gb) ** 2).sum() * wi
         assert d0 < 2.2e-16 and d1 < 2.2e-16
-    # test/test_basis.jl:90-120: orthonormal Legendre on [0,1]
+    # test/test_basis.jl:63-95: orthonormal Legendre on [0,1]
     ref = [lambda s: 1.0, lambda s: math.sqrt(3) * (2 * s - 1), lambda s: math.sqrt(5) * (6 * s * s - 6 * s + 1),
            lambda s: math.sqrt(7) * (2 * s - 1) * (10 * s * s - 10 * s + 1)]
     for k in range(4):
@@ -156,7 +156,7 @@ def test_l2_trace_projection_is_exact_for_polynomials(oracle):
 
 def test_corrected_formulation_converges_with_boundary_data(oracle):
     """tau = 4, u = sin(pi x / 2) sin(pi y / 2) (nonzero on x = 1, y = 1): the reference's trace
-    projection (src/boundary.jl:232-242) and He without tau (examples/poisson2D_HDG.jl:149) give no
+    projection (src/boundary.jl:27-37) and He without tau (examples/poisson2D_HDG.jl:149) give no
     convergence; the L2 projection with tau in He gives rate p + 1."""
     u = (oracle.F_SINSIN, [1.0, 0.5, 0.5])
     f = (oracle.F_SINSIN, [0.5 * np.pi ** 2, 0.5, 0.5])
