@@ -212,6 +212,26 @@ struct AmgHierarchy {
 
 void destroy_amg(AmgHierarchy* h) { delete h; }
 
+namespace {
+// The (0,0) entry (constant trace mode) of each of the 5 block slots of every face row.
+__global__ void k_amg_mode0(int nf, int nt, const double* __restrict__ val, double* __restrict__ out) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= 5 * (int64_t)nf) return;
+  const int k = (int)(t / nf), f = (int)(t - (int64_t)k * nf);
+  const int64_t ndofs = (int64_t)nf * nt;
+  out[t] = val[(int64_t)(k * nt) * ndofs + (int64_t)f * nt];
+}
+
+// Strength threshold of the level-0 aggregation (HDG_AMG_THETA; 0 = aggregate on every coupling).
+double amg_theta() {
+  static const double th = [] {
+    const char* e = std::getenv("HDG_AMG_THETA");
+    return e ? std::atof(e) : 0.0;
+  }();
+  return th;
+}
+}  // namespace
+
 // ------------------------------------------------------------------------------------------
 // Symbolic setup
 void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) {
@@ -237,8 +257,50 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
   }
   std::vector<char> active(nf);
   for (int f = 0; f < nf; ++f) active[f] = !dirichlet_face[f];
+  std::vector<int32_t> bcol5((size_t)5 * nf);
+  s->d_bcol5.download(bcol5.data(), bcol5.size(), st);
+  HDG_CUDA(cudaStreamSynchronize(st));
+  // Level-0 aggregation graph: all face couplings, or (theta > 0) only the strong ones,
+  // |a_fg| >= theta sqrt(a_ff a_gg) on the constant trace mode (the near-null space), from the
+  // matrix assembled when the setup runs.  With kappa jumping between cells, a face's couplings
+  // through a low-kappa cell are weak next to its diagonal, and aggregates that span such a jump
+  // interpolate the smooth error badly (Vanek, Mandel & Brezina 1996, strength of connection).
+  const double theta = amg_theta();
+  std::vector<int32_t> sptr(fptr), sadj(fadj);
+  if (theta > 0.0) {
+    DevBuf<double> d_m0;
+    d_m0.alloc((size_t)5 * nf);
+    k_amg_mode0<<<(unsigned)((5 * (int64_t)nf + 255) / 256), 256, 0, st>>>(nf, nt, s->d_val.p, d_m0.p);
+    HDG_CUDA(cudaGetLastError());
+    s->ctx->launches++;
+    std::vector<double> m0((size_t)5 * nf);
+    d_m0.download(m0.data(), m0.size(), st);
+    HDG_CUDA(cudaStreamSynchronize(st));
+    std::vector<double> dg(nf, 0.0);
+    for (int f = 0; f < nf; ++f)
+      for (int k = 0; k < 5; ++k)
+        if (bcol5[(size_t)k * nf + f] == f) dg[f] = std::max(dg[f], std::fabs(m0[(size_t)k * nf + f]));
+    std::vector<std::vector<int32_t>> strong(nf);
+    for (int f = 0; f < nf; ++f)
+      for (int k = 0; k < 5; ++k) {
+        const int g = bcol5[(size_t)k * nf + f];
+        if (g == f) continue;
+        if (std::fabs(m0[(size_t)k * nf + f]) >= theta * std::sqrt(dg[f] * dg[g])) {
+          strong[f].push_back(g);
+          strong[g].push_back(f);  // symmetric closure
+        }
+      }
+    sadj.clear();
+    for (int f = 0; f < nf; ++f) {
+      auto& v = strong[f];
+      std::sort(v.begin(), v.end());
+      v.erase(std::unique(v.begin(), v.end()), v.end());
+      sadj.insert(sadj.end(), v.begin(), v.end());
+      sptr[f + 1] = (int32_t)sadj.size();
+    }
+  }
   std::vector<int32_t> agg0;
-  const int na0 = aggregate(nf, fptr, fadj, active, &agg0);
+  const int na0 = aggregate(nf, sptr, sadj, active, &agg0);
   std::vector<int> size0(na0, 0);
   for (int f = 0; f < nf; ++f)
     if (agg0[f] >= 0) ++size0[agg0[f]];
@@ -258,9 +320,6 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
     for (int c = 0; c < nc && c < PW; ++c) pcol0[(size_t)f * PW + c] = cols[c];
   }
   // A0 P0 pattern per face: union over the 5 slot faces of their P0 columns
-  std::vector<int32_t> bcol5((size_t)5 * nf);
-  s->d_bcol5.download(bcol5.data(), bcol5.size(), st);
-  HDG_CUDA(cudaStreamSynchronize(st));
   // (at most 5 slots x PW columns = 25 entries per face, kept in a fixed-width table)
   constexpr int APW = 5 * PW;
   std::vector<int32_t> apc((size_t)nf * APW);

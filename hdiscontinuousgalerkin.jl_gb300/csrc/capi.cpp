@@ -570,7 +570,15 @@ int hdg_system_get_element_blocks(const hdg_system* s, double* Ate, double* bte,
     const int n = s->n, m = s->m, nc = s->nc;
     std::vector<double> AB((size_t)nc * m * (m + 1)), KB((size_t)nc * n * (m + 1));
     if (Ate || bte) s->d_AB.download(AB.data(), AB.size(), st);
-    if (Ke || be) s->d_KB.download(KB.data(), KB.size(), st);
+    if ((Ke || be) && s->kb_u_only) {  // the element path kept the u rows only: form the q rows
+      DevBuf<double> full;
+      full.alloc(KB.size());
+      launch_expand_ke(const_cast<hdg_system*>(s), full.p, st);
+      full.download(KB.data(), KB.size(), st);
+      HDG_CUDA(cudaStreamSynchronize(st));
+    } else if (Ke || be) {
+      s->d_KB.download(KB.data(), KB.size(), st);
+    }
     HDG_CUDA(cudaStreamSynchronize(st));
     for (int c = 0; c < nc; ++c) {
       for (int i = 0; i < m; ++i) {

@@ -211,8 +211,8 @@ bool build_lagrange_tables(int order, int qd, LagrangeTables* t);
 struct RefLayout {
   int M, D0, D1, C, F, H, NW, N, Q;
   // Schur-complement tables (valid when RefTables::schur): M^-1 D_l, Q_lm = D_l' M^-1 D_m,
-  // MF_{f,o} = M^-1 F_{f,o}, DMF_{l,f,o} = D_l' M^-1 F_{f,o}
-  int SMD0, SMD1, SQ00, SQ01, SQ11, SMF, SDMF, total;
+  // MF_{f,o} = M^-1 F_{f,o}, DMF_{l,f,o} = D_l' M^-1 F_{f,o}, PFF_{g,o';f,o} = F_{g,o'}' M^-1 F_{f,o}
+  int SMD0, SMD1, SQ00, SQ01, SQ11, SMF, SDMF, PFF, total;
 };
 RefLayout ref_layout(int nw, int nt, int nq);
 
@@ -258,8 +258,10 @@ struct hdg_system {
     return CoefDev{space->mesh->d_cell_prob.p, d_fkind.p, d_foff.p, d_fprm.p, d_kkind.p, d_koff.p, d_kprm.p,
                    d_tau.p};
   }
-  // per-cell condensed blocks: AB = [Ate | bte] (m x (m+1)), KB = [K_e | b_e] (n x (m+1))
+  // per-cell condensed blocks: AB = [Ate | bte] (m x (m+1)), KB = [K_e | b_e] (n x (m+1)), or,
+  // after the Cholesky-Schur element path (kb_u_only), only its u rows [X_u | b_u] (nw x (m+1))
   DevBuf<double> d_AB, d_KB;
+  bool kb_u_only = false;
   DevBuf<float> d_ABf, d_KBf;
   DevBuf<double> d_kappa;  // per-cell kappa (optional)
   DevBuf<double> d_fprm, d_kprm;
@@ -362,6 +364,8 @@ struct CgSolver {
 CgSolver* make_cg_solver(hdg_system* s);
 void mesh_concat(hdg_mesh* out, const std::vector<const hdg_mesh*>& parts);
 void launch_recover(hdg_system* s, cudaStream_t st);
+// The full [K_e | b_e] (ncells x n x (m+1), device) from the stored u rows (kb_u_only systems).
+void launch_expand_ke(hdg_system* s, double* out, cudaStream_t st);
 double run_errornorm(hdg_system* s, const FieldSpec& uex, cudaStream_t st);
 void run_nodal_avg(hdg_system* s, double* host_out, cudaStream_t st);
 void destroy_cg(CgState* c);

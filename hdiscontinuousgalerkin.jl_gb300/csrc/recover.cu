@@ -26,6 +26,69 @@ __global__ void k_recover(const int nc, const int32_t* __restrict__ cfaces, cons
   qu[t] = s;
 }
 
+// Recovery for the Cholesky-Schur element path, which stores only the u rows [X_u | b_u] of
+// [K_e | b_e]: u = X_u u_hat_e + b_u, then q from u, q_c = kf (adl0_c M^-1 D0 u + adl1_c M^-1 D1 u
+// - sum_f wn_f,c M^-1 F_{f,o} u_hat_f) (the q rows of K_e applied to the same u_hat_e, in closed form:
+// Ae = (det J / kappa) diag(M, M) on this path).  One thread per cell; tables read through L1.
+template <int P>
+__global__ void k_recover_u(const int nc, const int32_t* __restrict__ cells, const int32_t* __restrict__ cfaces,
+                            const uint8_t* __restrict__ orient, const double* __restrict__ xy,
+                            const double* __restrict__ kcell, const double* __restrict__ SMD0,
+                            const double* __restrict__ SMD1, const double* __restrict__ SMF,
+                            const double* __restrict__ KBu, const double* __restrict__ x, double* __restrict__ qu) {
+  using D = Dims<P>;
+  constexpr int NW = D::NW, NT = D::NT, NV = D::NV, N = D::N, M = D::M;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nc) return;
+  double uh[M];
+#pragma unroll
+  for (int f = 0; f < 3; ++f) {
+    const int g = cfaces[3 * e + f];
+#pragma unroll
+    for (int j = 0; j < NT; ++j) uh[f * NT + j] = x[g * NT + j];
+  }
+  const double* Xu = KBu + (size_t)e * NW * (M + 1);
+  double u[NW];
+#pragma unroll
+  for (int ia = 0; ia < NW; ++ia) {
+    double t = Xu[ia * (M + 1) + M];
+#pragma unroll
+    for (int j = 0; j < M; ++j) t += Xu[ia * (M + 1) + j] * uh[j];
+    u[ia] = t;
+    qu[(size_t)e * N + NV + ia] = t;
+  }
+  const int n0 = cells[3 * e], n1 = cells[3 * e + 1], n2 = cells[3 * e + 2];
+  const double J00 = xy[2 * n1] - xy[2 * n0], J01 = xy[2 * n2] - xy[2 * n0];
+  const double J10 = xy[2 * n1 + 1] - xy[2 * n0 + 1], J11 = xy[2 * n2 + 1] - xy[2 * n0 + 1];
+  const double detJ = J00 * J11 - J01 * J10;
+  const double ad00 = J11, ad01 = -J01, ad10 = -J10, ad11 = J00;
+  const double wn[3][2] = {{-(J10 - J11), J00 - J01}, {-J11, J01}, {J10, -J00}};
+  const double kinv = kcell ? 1.0 / kcell[e] : 1.0;
+  const double kf = 1.0 / (kinv * detJ);
+  const unsigned ob = orient[e];
+#pragma unroll 1
+  for (int ia = 0; ia < NW; ++ia) {
+    double g0 = 0.0, g1 = 0.0;
+#pragma unroll
+    for (int ib = 0; ib < NW; ++ib) {
+      g0 += __ldg(SMD0 + ia * NW + ib) * u[ib];
+      g1 += __ldg(SMD1 + ia * NW + ib) * u[ib];
+    }
+    double q0 = ad00 * g0 + ad10 * g1, q1 = ad01 * g0 + ad11 * g1;
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      const int fo = f * 2 + ((ob >> f) & 1);
+      double mf = 0.0;
+#pragma unroll
+      for (int j = 0; j < NT; ++j) mf += __ldg(SMF + (fo * NW + ia) * NT + j) * uh[f * NT + j];
+      q0 -= wn[f][0] * mf;
+      q1 -= wn[f][1] * mf;
+    }
+    qu[(size_t)e * N + ia] = kf * q0;
+    qu[(size_t)e * N + NW + ia] = kf * q1;
+  }
+}
+
 template <int P>
 __global__ void k_errornorm(const int nc, const int32_t* __restrict__ cells, const double* __restrict__ xy,
                             const double* __restrict__ ref, int nq, int offN, int offQ, const double* __restrict__ qw,
@@ -78,6 +141,18 @@ template <int P> void recover_p(hdg_system* s, cudaStream_t st) {
   hdg_mesh* m = s->space->mesh;
   const int64_t tot = (int64_t)m->nc * D::N;
   s->d_qu.alloc((size_t)tot);
+  if constexpr (P != 2) {
+    if (s->kb_u_only) {
+      const RefLayout L = ref_layout(s->space->t.nw, s->space->t.nt, s->space->t.nq);
+      const double* ref = s->space->d_ref.p;
+      k_recover_u<P><<<(unsigned)((m->nc + 127) / 128), 128, 0, st>>>(
+          m->nc, m->d_cells.p, m->d_cfaces.p, m->d_orient.p, m->d_xy.p, s->kappa_cells ? s->d_kappa.p : nullptr,
+          ref + L.SMD0, ref + L.SMD1, ref + L.SMF, s->d_KB.p, s->d_x.p, s->d_qu.p);
+      HDG_CUDA(cudaGetLastError());
+      s->ctx->launches++;
+      return;
+    }
+  }
   k_recover<P><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(m->nc, m->d_cfaces.p, s->d_KB.p, s->d_x.p, s->d_qu.p);
   HDG_CUDA(cudaGetLastError());
   s->ctx->launches++;

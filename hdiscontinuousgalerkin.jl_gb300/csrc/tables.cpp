@@ -210,6 +210,7 @@ RefLayout ref_layout(int nw, int nt, int nq) {
   L.SQ11 = o; o += nw * nw;
   L.SMF = o; o += 6 * nw * nt;
   L.SDMF = o; o += 12 * nw * nt;
+  L.PFF = o; o += 36 * nt * nt;
   L.total = o;
   return L;
 }
@@ -387,6 +388,14 @@ bool build_ref_tables(int p, int qd, RefTables* t) {
               long double s = 0;
               for (int k = 0; k < nw; ++k) s += (long double)D[l][k * nw + i] * MF[(size_t)k * nt + j];
               P[L.SDMF + ((l * 6 + fo) * nw + i) * nt + j] = (double)s;
+            }
+        // PFF_{go,fo} = F_{go}' M^-1 F_{fo} (nt x nt), the face-face term of the condensed operator
+        for (int go = 0; go < 6; ++go)
+          for (int i = 0; i < nt; ++i)
+            for (int j = 0; j < nt; ++j) {
+              long double s = 0;
+              for (int k = 0; k < nw; ++k) s += (long double)P[L.F + (go * nw + k) * nt + i] * MF[(size_t)k * nt + j];
+              P[L.PFF + ((go * 6 + fo) * nt + i) * nt + j] = (double)s;
             }
       }
     }
