@@ -5,7 +5,8 @@
 // Method (Vanek, Mandel & Brezina 1996; Vanek, Brezina & Mandel 2001).
 //  * Level 0 is the trace matrix itself: faces with nt dofs each, in the block-ELL layout.  The
 //    near-null space is the constant trace (Legendre mode 0 = 1 on every face).  Faces are
-//    aggregated greedily on the face graph (faces of a common cell are neighbours); Dirichlet
+//    aggregated greedily on the graph of their strong couplings (faces of a common cell whose
+//    mode-0 coupling is at least theta times the geometric mean of their diagonals); Dirichlet
 //    faces (decoupled after apply!) belong to no aggregate.  The tentative prolongator puts
 //    1/sqrt(|J|) on the mode-0 row of every face of aggregate J.
 //  * Level l >= 1 is a scalar CSR matrix.  Its nodes are aggregated on the quotient of the level
@@ -21,11 +22,13 @@
 //    coarsest solve.  Pre- and post-smoothing apply the same polynomial, so the cycle is a
 //    symmetric positive definite preconditioner.
 //
-// Aggregates depend only on the mesh and the Dirichlet faces, never on matrix values.  The
-// symbolic setup (aggregates, every sparsity pattern, the P' lists) therefore runs once per
-// system on the host and is reused when the system is reassembled with new coefficients; the
-// numeric setup (block inverses, bounds, P, A P, P' A P, coarsest inverses) runs on the device
-// after every assembly.  Batched systems are block diagonal: aggregates never cross problems,
+// Level-0 aggregates follow the strong couplings of the matrix assembled when the symbolic setup
+// runs (strength of connection on the constant trace mode, theta = 0.2); coarser aggregates depend
+// only on the graph.  The symbolic setup (aggregates, every sparsity pattern, the P' lists) runs
+// once per system on the host, at its first multigrid solve, and is kept when the system is
+// reassembled: with new coefficients the preconditioner stays symmetric positive definite and
+// valid, fitted to the first ones.  The numeric setup (block inverses, bounds, P, A P, P' A P,
+// coarsest inverses) runs on the device after every assembly.  Batched systems are block diagonal: aggregates never cross problems,
 // so each problem gets its own hierarchy inside the shared arrays.
 //
 // Everything in the hierarchy and the cycle is FP32: the preconditioner only has to be a fixed
@@ -223,10 +226,16 @@ __global__ void k_amg_mode0(int nf, int nt, const double* __restrict__ val, doub
 }
 
 // Strength threshold of the level-0 aggregation (HDG_AMG_THETA; 0 = aggregate on every coupling).
+// Measured on the 256-problem batch (kappa per cell over four decades, degree-4 Chebyshev):
+// theta = 0 / 0.02 / 0.05 / 0.1 / 0.15 / 0.2 / 0.25 / 0.35 gave 541 / 716 / 834 / 912 / 921 / 930 /
+// 893 / 873 solves/s (mean CG iterations 162 / 106 / 86 / 74 / 70 / 69 / 70 / 71); with kappa = 1
+// (2*256^2 cells, p = 2) 0.2 changes nothing (95 iterations), and on 2*128^2 cells at p = 4 it
+// takes 52 iterations instead of 68.
 double amg_theta() {
   static const double th = [] {
     const char* e = std::getenv("HDG_AMG_THETA");
-    return e ? std::atof(e) : 0.0;
+    const double v = e ? std::atof(e) : 0.2;
+    return (v >= 0.0 && v < 1.0) ? v : 0.2;
   }();
   return th;
 }
@@ -1183,8 +1192,9 @@ bool amg_level0_fp32() {
 }
 
 // The Chebyshev interval is [lambda / ratio, lambda].  A wider interval damps more of the smooth
-// error that the matrix-independent face aggregates leave behind where kappa jumps; with a
-// constant kappa it smooths the high end less well.  Measured (degree 4): on the 256-problem
+// error that coarse aggregates leave behind where kappa jumps; with a constant kappa it smooths
+// the high end less well.  (With the strength-of-connection aggregates the ratio hardly matters:
+// 30 and 120 are within 1 % on the batch.)  Measured before them (degree 4): on the 256-problem
 // batch (kappa per cell over four decades) ratios 12/20/30/60/120/250/500 gave
 // 462/490/507/528/538/538/533 solves/s; on the 131072-cell p=2 problem with kappa = 1, 30 gave
 // 38.0 solves/s (95 iterations) and 120 gave 33.3 (113).  So 120 for systems with a variable
@@ -1199,11 +1209,15 @@ float amg_cheb_ratio(const hdg_system* s) {
   return (s->kappa_cells || s->kappa_field) ? 120.f : 30.f;
 }
 
+// Degree of the level-0 Chebyshev smoother (HDG_AMG_CHEB_DEGREE, 1..4).  With the
+// strength-of-connection aggregates the cheaper polynomial wins: on the 256-problem batch degree
+// 2 / 3 / 4 gave 1015 / 961 / 931 solves/s (mean CG iterations 78 / 73 / 68); with kappa = 1 on
+// 2*256^2 cells (p = 2) degree 2 was already the fastest.
 int amg_cheb_degree() {
   static const int k = [] {
     const char* e = std::getenv("HDG_AMG_CHEB_DEGREE");
-    const int v = e ? std::atoi(e) : 4;
-    return (v >= 1 && v <= 4) ? v : 4;
+    const int v = e ? std::atoi(e) : 2;
+    return (v >= 1 && v <= 4) ? v : 2;
   }();
   return k;
 }
