@@ -155,6 +155,101 @@ class OraclePool:
         self.pool.join()
 
 
+FP64_TFLOPS_MEASURED = 1.21  # FMA-loop probe on the GB300s (all lanes, FP64 pipe), TFLOP/s
+
+
+def element_cost(p, schur):
+    """Per-cell algorithmic bytes and FP64 FLOPs of the element kernel of degree p.  Bytes: read 3
+    node ids, 6 coordinates, the orientation byte and kappa (69 B); write [Ate | bte] and the stored
+    rows of [K_e | b_e] (all n rows on the full path, the nw u rows on the Cholesky-Schur path).
+    FLOPs: the operations the kernel performs (2 per FMA); the dense-LU count of the survey (2/3 n^3
+    + 2 n^2 (m+1) + 2 m^2 n + ...) is the nominal work and is reported beside it."""
+    nw, nt = (p + 1) * (p + 2) // 2, p + 1
+    n, m = 3 * nw, 3 * nt
+    rc = nw + m + 1
+    rows = nw if schur else n
+    nbytes = 69 + 8 * (m * (m + 1) + rows * (m + 1))
+    if schur:
+        chol = sum((rc - k - 1) + sum(rc - i for i in range(k + 1, nw)) for k in range(nw))
+        fma = (7 * nw * (nw + 1) // 2 + 3 * nw * m + chol + (m * (m + 1) // 2 + m) * nw + 2 * (m * (m + 1) // 2)
+               + nw * (nw - 1) // 2 * (m + 1) + nw * (m + 1))
+    else:
+        nc = n + m + 1
+        fma = (sum((n - k - 1) * (nc - k - 1) for k in range(n)) + n * (n - 1) // 2 * (m + 1)
+               + 3 * nw * (m + 1) * 3 + m * (m + 1) * nw)
+    nominal = 2 * n ** 3 // 3 + 2 * n * n * (m + 1) + 2 * m * m * n
+    return nbytes, 2 * fma, nominal
+
+
+def c4_rooflines(H, B, tims, pc, hbm, peak_kind):
+    """The dominant kernel of the timed batch step (the kernel instance with the largest estimated
+    time per step: mean event-timed launch x launches) and the element kernels."""
+    k = 2  # Chebyshev degree of the level-0 smoother: 2k sweeps per V-cycle
+    chunk = 8
+    cand = []
+    for bn, t in zip(B.bins, tims):
+        it = max(B.stats[i].iterations for i in bn.idx)
+        it_launched = -(-it // chunk) * chunk
+        nt = bn.p + 1
+        if pc == H.PRECOND_AMG:
+            smp = bn.kernel_sample(1)
+            if smp["launches"]:
+                cand.append(dict(kernel=f"k_amg_face_cheb<{nt}, __half> (level-0 Chebyshev sweep, p={bn.p} bin)",
+                                 key=f"c4:k_amg_face_cheb<{nt}>", mean_ms=smp["ms"] / smp["launches"],
+                                 bytes_per_launch=smp["bytes"] / smp["launches"], launches=it_launched * 2 * k,
+                                 full_launch_bytes=bn.ndofs * (5 * 2 * nt + 20 / nt + 20),
+                                 sampled_launches=smp["launches"]))
+        if t["cg_samples"]:
+            cand.append(dict(kernel=f"k_cg_a<{nt}, double> (FP64 q = A z + beta q, p={bn.p} bin)", key=f"c4:k_cg_a<{nt}>",
+                             mean_ms=t["cg_a_ms"], bytes_per_launch=t["cg_a_bytes"], launches=it_launched,
+                             full_launch_bytes=bn.ndofs * (40 * nt + 20 / nt + 40), sampled_launches=t["cg_samples"]))
+    for c in cand:
+        c["est_ms_per_step"] = c["mean_ms"] * c["launches"]
+    dom = max(cand, key=lambda c: c["est_ms_per_step"]) if cand else None
+    rl = None
+    if dom:
+        ach = dom["bytes_per_launch"] / (dom["mean_ms"] / 1e3) / 1e9
+        rl = {"kernel": dom["kernel"], "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+              "traffic": profile_traffic(dom["key"]), "algorithmic_bytes_per_launch": dom["bytes_per_launch"],
+              "avg_launch_ms": dom["mean_ms"], "sampled_launches": dom["sampled_launches"],
+              "algorithmic_bytes_per_full_launch": dom["full_launch_bytes"],
+              "est_ms_per_step": dom["est_ms_per_step"],
+              "how": "CUDA events around each launch of the sampled (un-graphed) CG chunks of the timed step, on "
+                     "the bin's stream while the other bins run; bytes = rows of the problems that iterated x "
+                     "bytes per row; traffic: ncu dram read+write per launch of the same kernel in the same bench "
+                     "command at the full row count (compare with algorithmic_bytes_per_full_launch)",
+              "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
+              "fallback 6.8 TB/s",
+              "others": [{kk: c[kk] for kk in ("kernel", "mean_ms", "bytes_per_launch", "launches", "est_ms_per_step")}
+                         for c in sorted(cand, key=lambda c: -c["est_ms_per_step"])[:6]]}
+    el = []
+    tot_b = tot_f = tot_nom = tot_ms = 0.0
+    for bn, t in zip(B.bins, tims):
+        schur = bn.p != 2
+        nb, fl, nom = element_cost(bn.p, schur)
+        cells = bn.mesh.ncells
+        ms = t["element_ms"]
+        el.append({"p": bn.p, "path": "cholesky-schur" if schur else "full LU", "cells": cells, "ms": ms,
+                   "gbs": cells * nb / (ms / 1e3) / 1e9 if ms else None,
+                   "fp64_tflops": cells * fl / (ms / 1e3) / 1e12 if ms else None})
+        tot_b += cells * nb
+        tot_f += cells * fl
+        tot_nom += cells * nom
+        tot_ms += ms
+    ach = tot_b / (tot_ms / 1e3) / 1e9 if tot_ms else None
+    rl_el = {"kernel": "k_element_chol (p=1,3,4) + k_element_condense (p=2), all bins", "bound": "fp64 pipe",
+             "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm if ach else None,
+             "fp64_tflops": tot_f / (tot_ms / 1e3) / 1e12 if tot_ms else None,
+             "fp64_peak_tflops": FP64_TFLOPS_MEASURED,
+             "fp64_frac": tot_f / (tot_ms / 1e3) / 1e12 / FP64_TFLOPS_MEASURED if tot_ms else None,
+             "nominal_dense_lu_tflops": tot_nom / (tot_ms / 1e3) / 1e12 if tot_ms else None,
+             "ms_sum_of_bins": tot_ms, "bins": el,
+             "how": "element kernel of each bin timed with CUDA events in the timed step (bins run concurrently, so "
+                    "each kernel shares the GPU); HBM fraction of measured copy bandwidth and FP64 fraction of the "
+                    "measured FMA rate"}
+    return rl, rl_el
+
+
 def run_c4(args, ws, rank, local):
     """Batched workload: the degree-binned batch (one launch sequence for all problems of a
     degree, interleaved CG) against the plain FP64 path that solves the problems one at a time."""
@@ -232,12 +327,8 @@ def run_c4(args, ws, rank, local):
     value = ws * len(probs) / (batch_ms / 1e3)
     iters = [s.iterations for s in B.stats]
 
-    # ---- roofline of the dominant phase (last timed step) ----
-    # The degree bins iterate concurrently on their own streams, so the CG kernels of one bin
-    # overlap those of the others and a single launch's duration is not its own.  The CG phase is
-    # therefore measured as a whole: the algorithmic bytes of every iteration launch of every bin
-    # (rows of the problems that iterated x the per-row bytes of the two kernels) over the
-    # phase's wall time (the longest bin, all bins starting together).
+    # ---- rooflines, from the last timed step (profiling on: every 8th CG chunk of each bin runs
+    # un-graphed with each kernel timed on its own, on the bin's stream, while the other bins run) ----
     peaks, peak_kind = measured_peaks()
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     tims = [bn.timings() for bn in B.bins]
@@ -248,25 +339,7 @@ def run_c4(args, ws, rank, local):
     cg_ms = max(t["cg_ms"] for t in tims)
     cg_bytes = sum(t["cg_bytes"] for t in tims)
     el_ms = sum(t["element_ms"] for t in tims)
-    nw_ = lambda p: (p + 1) * (p + 2) // 2
-    el_bytes = sum(2 * pr.n * pr.n * (12 + 48 + 1 + 8 * ((3 * pr.p + 3) * (3 * pr.p + 4) +
-                                                       3 * nw_(pr.p) * (3 * pr.p + 4))) for pr in probs)
-    if cg_ms >= el_ms:
-        if pc == H.PRECOND_AMG:
-            kname = "k_cg_a"
-            dom = ("CG iteration kernels (k_cg_a + k_cg_b_mg + multigrid V-cycle + k_cg_c) of all degree bins, "
-                   "on concurrent streams")
-        else:
-            kname = "k_cg_a_fresh" if prec == H.PREC_MIXED else "k_cg_a"
-            dom = f"CG iteration kernels ({kname} + k_cg_b) of all degree bins, on concurrent streams"
-        alg, dur = cg_bytes, cg_ms
-    else:
-        kname = "k_element_condense"
-        dom = "k_element_condense (all degree bins)"
-        alg, dur = el_bytes, el_ms
-    achieved = alg / (dur / 1e3) / 1e9 if dur > 0 else None
-    traffic = profile_traffic("c4_" + args.precision + ":" + kname)
-
+    rl, rl_element = c4_rooflines(H, B, tims, pc, hbm, peak_kind)
     # ---- plain path, one timed pass over the batch ----
     p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     p0.record(stream)
@@ -321,12 +394,10 @@ def run_c4(args, ws, rank, local):
         "phase_ms": {"element_ms_sum_of_bins": el_ms, "cg_ms_longest_bin": cg_ms},
         "bins": bins_detail,
         "gpu_launches": launches,
-        "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
-                     "algorithmic_bytes": alg, "duration_ms": dur,
-                     "note": "whole-phase figure: algorithmic bytes of all launches of the phase / its wall time",
-                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
-                     "fallback 6.8 TB/s"},
+        "roofline": rl, "roofline_element": rl_element,
+        "cg_phase": {"algorithmic_bytes": cg_bytes, "wall_ms_longest_bin": cg_ms,
+                     "achieved_gbs": cg_bytes / (cg_ms / 1e3) / 1e9 if cg_ms > 0 else None,
+                     "note": "all CG iteration launches of all bins (concurrent streams) / the longest bin's CG wall time"},
         "e2e": {"value": ws * len(probs) * e2e_n / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "clocks": clk,
@@ -858,7 +929,7 @@ def profile_traffic(kernel: str):
         if not fn.endswith((".md", ".txt")):
             continue
         for ln in open(os.path.join(d, fn)):
-            m = re.match(r"\s*traffic_bytes_per_launch\[(\w+)\]\s*[:=]\s*([0-9.eE+]+)", ln)
+            m = re.match(r"\s*traffic_bytes_per_launch\[([^\]]+)\]\s*[:=]\s*([0-9.eE+]+)", ln)
             if m and m.group(1) == kernel:
                 return float(m.group(2))
     return None

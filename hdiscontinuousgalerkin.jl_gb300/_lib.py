@@ -92,6 +92,7 @@ SIGNATURES = {
     "hdg_dirichlet_l2": ([vp, C.c_char_p, C.POINTER(hdg_field), i32p, dp, intp], ip),
     "hdg_space_set_he_tau": ([vp, ip], ip),
     "hdg_solve": ([vp, C.POINTER(hdg_solver), dp, C.POINTER(hdg_stats)], ip),
+    "hdg_system_kernel_sample": ([vp, ip, dp, dp, intp], ip),
     "hdg_refine": ([vp, C.POINTER(hdg_solver), ip, C.c_double, dp, C.POINTER(hdg_stats)], ip),
     "hdg_recover": ([vp, dp, dp, dp], ip),
     "hdg_errornorm_l2sq": ([vp, C.POINTER(hdg_field), dp], ip),

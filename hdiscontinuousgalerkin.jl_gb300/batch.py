@@ -139,6 +139,14 @@ class Bin:
         L.check(L.load().hdg_system_timings(self.h, C.byref(t)), self.ctx.handle)
         return {k: getattr(t, k) for k, _ in L.hdg_timings._fields_}
 
+    def kernel_sample(self, which=1) -> dict:
+        """One kernel family of the last solve's sampled chunks, timed launch by launch
+        (hdg_system_kernel_sample): summed event ms, summed algorithmic bytes, launches."""
+        ms, by, n = C.c_double(), C.c_double(), C.c_int()
+        L.check(L.load().hdg_system_kernel_sample(self.h, int(which), C.byref(ms), C.byref(by), C.byref(n)),
+                self.ctx.handle)
+        return {"ms": ms.value, "bytes": by.value, "launches": n.value}
+
     def _pinned(self, count):
         ptr = C.c_void_p()
         L.check(L.load().hdg_host_alloc(C.c_size_t(8 * count), C.byref(ptr)), self.ctx.handle)

@@ -34,6 +34,7 @@
 // Everything in the hierarchy and the cycle is FP32: the preconditioner only has to be a fixed
 // SPD approximation.  All sums run in a fixed order, so the cycle is deterministic.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -244,6 +245,9 @@ double amg_theta() {
 // ------------------------------------------------------------------------------------------
 // Symbolic setup
 void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) {
+  const bool verbose = std::getenv("HDG_AMG_VERBOSE") != nullptr;
+  auto clk = [] { return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count(); };
+  double tph[8] = {clk(), 0, 0, 0, 0, 0, 0, 0};
   if (s->amg) destroy_amg(s->amg);
   s->amg = new AmgHierarchy();
   ++s->amg_gen;
@@ -289,27 +293,33 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
     for (int f = 0; f < nf; ++f)
       for (int k = 0; k < 5; ++k)
         if (bcol5[(size_t)k * nf + f] == f) dg[f] = std::max(dg[f], std::fabs(m0[(size_t)k * nf + f]));
-    std::vector<std::vector<int32_t>> strong(nf);
+    // strong neighbours in a fixed-width table (at most 4 slots each way), then compacted to CSR
+    constexpr int SW = 8;
+    std::vector<int32_t> tab((size_t)nf * SW);
+    std::vector<uint8_t> cnt(nf, 0);
     for (int f = 0; f < nf; ++f)
       for (int k = 0; k < 5; ++k) {
         const int g = bcol5[(size_t)k * nf + f];
         if (g == f) continue;
         if (std::fabs(m0[(size_t)k * nf + f]) >= theta * std::sqrt(dg[f] * dg[g])) {
-          strong[f].push_back(g);
-          strong[g].push_back(f);  // symmetric closure
+          if (cnt[f] < SW) tab[(size_t)f * SW + cnt[f]++] = g;
+          if (cnt[g] < SW) tab[(size_t)g * SW + cnt[g]++] = f;  // symmetric closure
         }
       }
     sadj.clear();
+    sadj.reserve((size_t)nf * 4);
     for (int f = 0; f < nf; ++f) {
-      auto& v = strong[f];
-      std::sort(v.begin(), v.end());
-      v.erase(std::unique(v.begin(), v.end()), v.end());
-      sadj.insert(sadj.end(), v.begin(), v.end());
+      int32_t* v = &tab[(size_t)f * SW];
+      std::sort(v, v + cnt[f]);
+      const int n = (int)(std::unique(v, v + cnt[f]) - v);
+      sadj.insert(sadj.end(), v, v + n);
       sptr[f + 1] = (int32_t)sadj.size();
     }
   }
+  tph[1] = clk();
   std::vector<int32_t> agg0;
   const int na0 = aggregate(nf, sptr, sadj, active, &agg0);
+  tph[2] = clk();
   std::vector<int> size0(na0, 0);
   for (int f = 0; f < nf; ++f)
     if (agg0[f] >= 0) ++size0[agg0[f]];
@@ -363,6 +373,7 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
       }
     }
   }
+  tph[3] = clk();
   // P0' lists and the level-1 pattern (rows = aggregates)
   std::vector<int32_t> rptr0, rent0;  // entries f * PW + c of P0 per column, in entry order
   bucket(na0, pcol0, &rptr0, &rent0);
@@ -372,20 +383,29 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
   L1.h_prob.assign(na0, 0);
   L1.h_B.assign(na0, 0.0);
   std::vector<int32_t> cols;
+  // column unions below use a stamp per column (the row that last added it): each candidate is
+  // looked at once, and only the distinct columns of a row are sorted
+  std::vector<int32_t> mark((size_t)na0, -1);
   for (int J = 0; J < na0; ++J) {
     cols.clear();
     for (int t = rptr0[J]; t < rptr0[J + 1]; ++t) {
       const int f = rent0[t] / PW;
-      cols.insert(cols.end(), &apc[(size_t)f * APW], &apc[(size_t)f * APW] + apn[f]);
+      for (int q = 0; q < apn[f]; ++q) {
+        const int32_t c = apc[(size_t)f * APW + q];
+        if (mark[c] != J) {
+          mark[c] = J;
+          cols.push_back(c);
+        }
+      }
     }
     std::sort(cols.begin(), cols.end());
-    cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
     L1.h_col.insert(L1.h_col.end(), cols.begin(), cols.end());
     L1.h_ptr[J + 1] = (int32_t)L1.h_col.size();
     L1.h_B[J] = std::sqrt((double)size0[J]);
   }
   for (int f = 0; f < nf; ++f)
     if (agg0[f] >= 0) L1.h_prob[agg0[f]] = fprob[f];
+  tph[4] = clk();
   // quotient graph of the face graph for level 1's aggregation
   std::vector<int32_t> gptr, gadj;
   quotient(nf, fptr, fadj, agg0, na0, &gptr, &gadj);
@@ -410,6 +430,7 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
   H->dpval0.alloc((size_t)nf * nt * PW);
   H->lev.clear();
   H->lev.push_back(std::move(L1));
+  tph[5] = clk();
   // coarser levels
   auto max_per_problem = [&](const AmgLevel& L) {
     std::vector<int> cnt(s->nprob, 0);
@@ -430,24 +451,30 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
     for (int i = 0; i < n; ++i) tent[i] = nrm[agg[i]] > 0 ? (float)(F.h_B[i] / nrm[agg[i]]) : 0.f;
     // P pattern row i: aggregates of the columns of A row i
     std::vector<int32_t> pptr(n + 1, 0), pcol, v;
+    std::vector<int32_t> cmark((size_t)na, -1);
+    auto add = [&](int32_t c, int32_t row) {
+      if (cmark[c] != row) {
+        cmark[c] = row;
+        v.push_back(c);
+      }
+    };
     for (int i = 0; i < n; ++i) {
       v.clear();
-      for (int e = F.h_ptr[i]; e < F.h_ptr[i + 1]; ++e) v.push_back(agg[F.h_col[e]]);
+      for (int e = F.h_ptr[i]; e < F.h_ptr[i + 1]; ++e) add(agg[F.h_col[e]], i);
       std::sort(v.begin(), v.end());
-      v.erase(std::unique(v.begin(), v.end()), v.end());
       pcol.insert(pcol.end(), v.begin(), v.end());
       pptr[i + 1] = (int32_t)pcol.size();
     }
     // A P pattern row i: union of the P rows of A row i's columns
     std::vector<int32_t> apptr(n + 1, 0), apcol;
+    std::fill(cmark.begin(), cmark.end(), -1);
     for (int i = 0; i < n; ++i) {
       v.clear();
       for (int e = F.h_ptr[i]; e < F.h_ptr[i + 1]; ++e) {
         const int k = F.h_col[e];
-        v.insert(v.end(), pcol.begin() + pptr[k], pcol.begin() + pptr[k + 1]);
+        for (int q = pptr[k]; q < pptr[k + 1]; ++q) add(pcol[q], i);
       }
       std::sort(v.begin(), v.end());
-      v.erase(std::unique(v.begin(), v.end()), v.end());
       apcol.insert(apcol.end(), v.begin(), v.end());
       apptr[i + 1] = (int32_t)apcol.size();
     }
@@ -464,14 +491,20 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
     C.h_ptr.assign(na + 1, 0);
     C.h_prob.assign(na, 0);
     C.h_B = nrm;
+    std::fill(cmark.begin(), cmark.end(), -1);
     for (int J = 0; J < na; ++J) {
       cols.clear();
       for (int t = rptr[J]; t < rptr[J + 1]; ++t) {
         const int i = rrow[t];
-        cols.insert(cols.end(), apcol.begin() + apptr[i], apcol.begin() + apptr[i + 1]);
+        for (int q = apptr[i]; q < apptr[i + 1]; ++q) {
+          const int32_t c = apcol[q];
+          if (cmark[c] != J) {
+            cmark[c] = J;
+            cols.push_back(c);
+          }
+        }
       }
       std::sort(cols.begin(), cols.end());
-      cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
       C.h_col.insert(C.h_col.end(), cols.begin(), cols.end());
       C.h_ptr[J + 1] = (int32_t)C.h_col.size();
     }
@@ -494,6 +527,7 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
     gadj.swap(qadj);
     H->lev.push_back(std::move(C));
   }
+  tph[6] = clk();
   // device copies of every level's matrix pattern and vectors
   for (auto& L : H->lev) {
     L.ptr.upload(L.h_ptr.data(), L.h_ptr.size(), st);
@@ -524,7 +558,11 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
   H->coff.upload(coff.data(), coff.size(), st);
   H->cinv.alloc(std::max(coff[s->nprob], 1));
   H->built = true;
-  if (std::getenv("HDG_AMG_VERBOSE")) {  // level sizes: rows (largest problem's rows)
+  if (verbose) {  // level sizes: rows (largest problem's rows); host time of the set-up phases (ms)
+    tph[7] = clk();
+    std::fprintf(stderr, "amg setup ms: strength %.1f agg0 %.1f p0 %.1f level1 %.1f upload0 %.1f coarse %.1f upload %.1f\n",
+                 1e3 * (tph[1] - tph[0]), 1e3 * (tph[2] - tph[1]), 1e3 * (tph[3] - tph[2]), 1e3 * (tph[4] - tph[3]),
+                 1e3 * (tph[5] - tph[4]), 1e3 * (tph[6] - tph[5]), 1e3 * (tph[7] - tph[6]));
     std::fprintf(stderr, "amg: %d problems, level 0: %d faces x %d", s->nprob, nf, nt);
     for (const AmgLevel& L : H->lev) {
       std::vector<int> cnt(s->nprob, 0);
@@ -1291,6 +1329,11 @@ void cheb_sweep(hdg_system* s, const VT* val0, const float* b0, const float* in,
                 const int32_t* cst, cudaStream_t st) {
   AmgHierarchy* H = s->amg;
   const int nf = H->nf;
+  EventPair* ep = nullptr;
+  if (s->prof_cheb0) {  // a sampled chunk: each sweep timed on its own
+    ep = new EventPair();
+    ep->start(st);
+  }
   if (nf < AMG_ROW_SWEEP_FACES)
     k_amg_row_cheb<NT, VT><<<nblk((int64_t)nf * NT), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p,
                                                               H->face_prob.p, b0, H->bt0.p, in, out, H->d0.p, step,
@@ -1298,6 +1341,10 @@ void cheb_sweep(hdg_system* s, const VT* val0, const float* b0, const float* in,
   else
     k_amg_face_cheb<NT, VT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p, H->face_prob.p, b0,
                                                   H->bt0.p, in, out, H->d0.p, step, amg_cheb_ratio(s), cst);
+  if (ep) {
+    ep->stop(st);
+    s->ev_cheb0.push_back(ep);
+  }
 }
 
 template <int NT, typename VT>
@@ -1413,6 +1460,17 @@ double amg_cycle_bytes(const hdg_system* s) {
     b += 2.0 * (8.0 * npc + 12.0 * n);                      // restriction and prolongation
   }
   return b;
+}
+
+// Algorithmic bytes per trace row of the 2k level-0 Chebyshev sweeps of one V-cycle: the first
+// forms D^-1 b (b and the row's D^-1 row read, bt, x, d written); each of the other 2k - 1 reads
+// the row of D^-1 A0 (5 nt values of 2 or 4 bytes), the block columns (20 bytes per face), bt, x
+// (neighbour values counted once, at their own row), d read and written, x out.
+double amg_cheb0_bytes_per_row(const hdg_system* s) {
+  const AmgHierarchy* H = s->amg;
+  const double nt = H->nt, vb = H->val0h.p ? 2.0 : 4.0;
+  const int k = amg_cheb_degree();
+  return (16.0 + 4.0 * nt) + (2 * k - 1) * (5.0 * vb * nt + 20.0 / nt + 20.0);
 }
 
 int amg_cycle_launches(const hdg_system* s) {

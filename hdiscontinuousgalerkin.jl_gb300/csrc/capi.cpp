@@ -56,6 +56,9 @@ void order_streams(cudaStream_t before, cudaStream_t after) {
 hdg_system::~hdg_system() {
   if (cg) destroy_cg(cg);
   if (amg) destroy_amg(amg);
+  for (auto* e : ev_cg_a) delete e;
+  for (auto* e : ev_cg_b) delete e;
+  for (auto* e : ev_cheb0) delete e;
 }
 
 extern "C" {
@@ -346,6 +349,18 @@ static void set_coefficients_many(hdg_system* s, const double* taus, const hdg_f
   s->d_fkind.upload(fk.data(), np, st);
   s->d_foff.upload(fo.data(), np, st);
   s->d_fprm.upload(fp.data(), fp.size(), st);
+  // the element kernels evaluate a Gaussian bump as a exp(|x - c|^2 k) with k = -1/(2 s^2) formed
+  // here once, instead of dividing by 2 s^2 at every quadrature point
+  std::vector<double> fpp(fp);
+  for (int P = 0; P < np; ++P)
+    if (fk[P] == HDG_FIELD_BUMPS) {
+      const int K = (int)fpp[fo[P]];
+      for (int b = 0; b < K; ++b) {
+        double& sw = fpp[fo[P] + 1 + 4 * b + 2];
+        sw = -1.0 / (2.0 * sw * sw);
+      }
+    }
+  s->d_fprep.upload(fpp.data(), fpp.size(), st);
   s->d_kkind.upload(kk.data(), np, st);
   s->d_koff.upload(ko.data(), np, st);
   s->d_kprm.upload(kp.data(), kp.size(), st);
@@ -894,6 +909,20 @@ int hdg_system_timings(hdg_system* s, hdg_timings* out) {
     }
     out->cg_iterations = s->cg_iterations;
     out->cg_bytes = s->prof_all_bytes;
+    return HDG_OK;
+  });
+}
+
+int hdg_system_kernel_sample(hdg_system* s, int which, double* total_ms, double* total_bytes, int* launches) {
+  if (!s || !total_ms || !total_bytes || !launches) return HDG_ERR_ARG;
+  if (which != HDG_SAMPLE_CHEB0) return fail(s->ctx, HDG_ERR_ARG, "unknown kernel sample");
+  return guard(s->ctx, [&]() -> int {
+    set_device(s->ctx);
+    double t = 0.0;
+    for (auto* e : s->ev_cheb0) t += e->ms();
+    *total_ms = t;
+    *total_bytes = s->prof_cheb0_bytes;
+    *launches = (int)s->ev_cheb0.size();
     return HDG_OK;
   });
 }

@@ -591,6 +591,9 @@ template <int NT> struct SolverNT : CgSolver {
     s->ev_cg_a.clear();
     s->ev_cg_b.clear();
     s->prof_a_bytes = s->prof_b_bytes = s->prof_all_bytes = 0.0;
+    for (auto* e : s->ev_cheb0) delete e;
+    s->ev_cheb0.clear();
+    s->prof_cheb0_bytes = 0.0;
     sample_pending = false;
     it_prev.assign(nprob, 0);
     if (s->ctx->profiling) s->ev_cg.start(st);
@@ -669,7 +672,9 @@ template <int NT> struct SolverNT : CgSolver {
         if constexpr (sizeof(T) == sizeof(double)) {
           if (mg) {  // the update, the V-cycle and the r.z kernel are timed together
             k_cg_b_mg<NT><<<s->nseg, CG_BLOCK, 0, st>>>(a, c->r32.p);
+            s->prof_cheb0 = true;  // and each level-0 smoother sweep on its own
             amg_apply(s, c->r32.p, c->z32.p, c->st.p, st);
+            s->prof_cheb0 = false;
             k_cg_c<NT><<<s->nseg, CG_BLOCK, 0, st>>>(a, c->z32.p, 0, 0);
           } else {
             k_cg_b<NT, T><<<s->nseg, CG_BLOCK, 0, st>>>(a, 0);
@@ -707,7 +712,7 @@ template <int NT> struct SolverNT : CgSolver {
     s->ctx->launches++;
   }
 
-  void residual(bool replace) {
+  void residual(bool replace, bool sync = true) {
     HDG_CUDA(cudaMemcpyAsync(c->st.p, c->h_st, sizeof(int32_t) * ST * nprob, cudaMemcpyHostToDevice, st));
     if (mixed) x_to_double();
     if (mixed) k_cg_residual<NT, float><<<s->nseg, CG_BLOCK, 0, st>>>(a32, s->d_val.p, replace ? 1 : 0, nullptr);
@@ -722,7 +727,7 @@ template <int NT> struct SolverNT : CgSolver {
       s->ctx->launches++;
     }
     HDG_CUDA(cudaMemcpyAsync(c->h_sc, c->sc.p, sizeof(double) * SC * nprob, cudaMemcpyDeviceToHost, st));
-    HDG_CUDA(cudaStreamSynchronize(st));
+    if (sync) HDG_CUDA(cudaStreamSynchronize(st));
   }
 
   // Rebuilds the segment tables from the running problems (all = restore the full tables).
@@ -787,6 +792,7 @@ template <int NT> struct SolverNT : CgSolver {
     }
     s->prof_a_bytes += rows_it * bytes_per_row_a();
     s->prof_b_bytes += rows_it * bytes_per_row_b();
+    if (mg) s->prof_cheb0_bytes += rows_it * amg_cheb0_bytes_per_row(s);
   }
 
   bool process(const hdg_solver& o) override {
@@ -856,16 +862,26 @@ template <int NT> struct SolverNT : CgSolver {
 
   void finish(const hdg_solver& o, std::vector<hdg_stats>* out) override {
     (void)o;
+    finish_enqueue();
+    HDG_CUDA(cudaStreamSynchronize(st));
+    finish_collect(out);
+  }
+
+  void finish_enqueue() override {
     if (s->nseg != nseg_full) set_segments(true);  // restore the full tables (other kernels use them)
     if (mixed) x_to_double();
     if (!mixed) {  // report the true FP64 residual of every problem
       for (int P = 0; P < nprob; ++P) c->h_st[ST * P + 3] = 1;
-      residual(false);
-      for (int P = 0; P < nprob; ++P) c->h_st[ST * P + 3] = 0;
-      HDG_CUDA(cudaMemcpyAsync(c->st.p, c->h_st, sizeof(int32_t) * ST * nprob, cudaMemcpyHostToDevice, st));
+      residual(false, false);
     }
-    HDG_CUDA(cudaStreamSynchronize(st));
     if (s->ctx->profiling) s->ev_cg.stop(st);
+  }
+
+  // After the work finish_enqueue queued has landed.  The refine flags it raised on the host are
+  // cleared here; the device copy is rewritten by the next prepare().
+  void finish_collect(std::vector<hdg_stats>* out) override {
+    if (!mixed)
+      for (int P = 0; P < nprob; ++P) c->h_st[ST * P + 3] = 0;
     out->assign(nprob, hdg_stats{});
     int itmax = 0;
     for (int P = 0; P < nprob; ++P) {

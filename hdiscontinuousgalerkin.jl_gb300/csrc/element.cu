@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(EWARPS * 32) k_element_condense(ElemArgs a) {
     const int prob = a.co.cell_prob[e];
     const double tau = a.co.tau[prob];
     const int fkind = a.co.fkind[prob];
-    const double* fprm = a.co.fprm + a.co.foff[prob];
+    const double* fprm = a.co.fprep + a.co.foff[prob];
     double kinv = 1.0;
     if (a.kappa_mode == 1) kinv = 1.0 / a.kcell[e];
     const double smass = kinv * detJ;
@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(EWARPS * 32) k_element_condense(ElemArgs a) {
       double xi = ref[L.Q + 2 * q], eta = ref[L.Q + 2 * q + 1];
       double xq = (1.0 - xi - eta) * x1 + xi * x2 + eta * x3;
       double yq = (1.0 - xi - eta) * y1 + xi * y2 + eta * y3;
-      sq[q] = eval_field_kind(fkind, fprm, xq, yq);
+      sq[q] = eval_source_prepared(fkind, fprm, xq, yq);
       if (a.kappa_mode == 2) sq[nq + q] = 1.0 / eval_field_kind(a.co.kkind[prob], a.co.kprm + a.co.koff[prob], xq, yq);
     }
     __syncwarp();
@@ -241,22 +241,31 @@ __global__ void __launch_bounds__(EWARPS * 32) k_element_condense(ElemArgs a) {
   }
 }
 
-// Cholesky-Schur path: invertible reference mass and kappa constant on each cell (p = 1, and
-// p = 3, 4 with exact-enough rules).  Then Ae = (det J / kappa) diag(M, M) is inverted in closed
-// form, and with kf = kappa / det J the condensation needs only the nw x nw Schur complement
+// Schur path with an LDL' factorisation: invertible reference mass and kappa constant on each
+// cell (p = 1, and p = 3, 4 with exact-enough rules).  Then Ae = (det J / kappa) diag(M, M) is
+// inverted in closed form, and with kf = kappa / det J the condensation needs only the nw x nw
+// Schur complement
 //   S  = C + kf sum_c B_c' M^-1 B_c = C + kf (a00 Q00 + a01 (Q01 + Q01') + a11 Q11)    (SPD)
 //   R' = [R'_f] with R'_f = tau |e_f| F_{f,o} + kf (b0_f DMF0_{f,o} + b1_f DMF1_{f,o}), and be,
-// where B_c = adl0_c D0 + adl1_c D1, b_l f = adj(J) row l . wn_f.  Writing S = U'U (Cholesky) and
-// Z = U'^-1 [R' | be], the condensed blocks are
-//   Ate_{fi,gj} = (Z'Z)_{fi,gj} - kf (wn_f . wn_g) (F_{f,o}' M^-1 F_{g,o'})_{ij} - [f = g] |e_f| He_ij
-//   bte_{fi}    = -(Z'Z)_{fi,be}
+// where B_c = adl0_c D0 + adl1_c D1, b_l f = adj(J) row l . wn_f.  Writing S = U' D U (U unit
+// upper triangular) and R~ = U'^-1 [R' | be], the condensed blocks are
+//   Ate_{fi,gj} = (R~' D^-1 R~)_{fi,gj} - kf (wn_f . wn_g) (F_{f,o}' M^-1 F_{g,o'})_{ij} - [f = g] |e_f| He_ij
+//   bte_{fi}    = -(R~' D^-1 R~)_{fi,be}
 // (the same Ate = [Ee;Fe]' Me^-1 [-Ee;Fe] - He and bte = -[Ee;Fe]' Me^-1 [0;be] that the full
 // elimination of examples/poisson2D_HDG.jl:155-174 forms, reordered), symmetric by construction, so
-// only the upper triangle is computed.  The u rows of [K_e | b_e], X_u = U^-1 Z, are stored; the q
-// rows follow linearly from them, q = kf (adl0 M^-1 D0 u + adl1 M^-1 D1 u - sum_f wn_f M^-1 F_f u_hat_f),
-// and are formed at recovery (k_recover_u) or when the blocks are exported (k_expand_ke).
-// Per cell at p = 4 this is about 8k FP64 FMAs instead of the 20k of the pivoted elimination of S
-// with the q rows, and 3.8 KB written instead of 7.7 KB.
+// only the upper triangle is computed.  The u rows of [K_e | b_e], X_u = U^-1 D^-1 R~, are stored;
+// the q rows follow linearly from them, q = kf (adl0 M^-1 D0 u + adl1 M^-1 D1 u - sum_f wn_f M^-1
+// F_f u_hat_f), and are formed at recovery (k_recover_u) or when the blocks are exported
+// (k_expand_ke).  Per cell at p = 4 this is about 8k FP64 FMAs instead of the 20k of the pivoted
+// elimination of S with the q rows, and 3.8 KB written instead of 7.7 KB.  The kernel is bound by
+// the FP64 pipe, which counts warp instructions: the pivots need no square root, their
+// reciprocals come from recip_newton, and the bump source's -1/(2 s^2) is formed on the host.
+// v[f] for a face index f known only at run time, without indexing a local array (which would
+// place the array in local memory)
+__device__ __forceinline__ double sel3(int f, double v0, double v1, double v2) {
+  return f == 0 ? v0 : (f == 1 ? v1 : v2);
+}
+
 template <int P, int EWARPS>
 __global__ void __launch_bounds__(EWARPS * 32) k_element_chol(ElemArgs a) {
   using D = Dims<P>;
@@ -280,11 +289,12 @@ __global__ void __launch_bounds__(EWARPS * 32) k_element_chol(ElemArgs a) {
   const double* DMF = smem + n1 + n2;            // [2][6][NW][NT]
   const double* PFF = DMF + 12 * NW * NT;        // [6][6][NT][NT]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int wstride = ((NW * LDW + nq + 2 * NW) + 1) & ~1;
+  const int wstride = ((NW * LDW + NW * (M + 1) + nq + 2 * NW) + 1) & ~1;
   double* W = smem + ((n1 + n2 + n3 + 1) & ~1) + warp * wstride;
-  double* sq = W + NW * LDW;  // f at the quadrature points
+  double* Y = W + NW * LDW;   // D^-1 R~ (NW x (M+1))
+  double* sq = Y + NW * (M + 1);  // f at the quadrature points
   double* be = sq + nq;
-  double* rinv = be + NW;     // 1 / U_kk
+  double* rinv = be + NW;     // 1 / d_k
   __syncthreads();
 
   for (int e = blockIdx.x * EWARPS + warp; e < a.nc; e += gridDim.x * EWARPS) {
@@ -311,7 +321,7 @@ __global__ void __launch_bounds__(EWARPS * 32) k_element_chol(ElemArgs a) {
     const double tau = a.co.tau[prob];
     const double hs = a.he_tau ? tau : 1.0;
     const int fkind = a.co.fkind[prob];
-    const double* fprm = a.co.fprm + a.co.foff[prob];
+    const double* fprm = a.co.fprep + a.co.foff[prob];
     const double kinv = (a.kappa_mode == 1) ? 1.0 / a.kcell[e] : 1.0;
     const double kf = 1.0 / (kinv * detJ);
     // ---- source at the volume points, be ----------------------------------------------------
@@ -319,7 +329,7 @@ __global__ void __launch_bounds__(EWARPS * 32) k_element_chol(ElemArgs a) {
       const double xi = Qp[2 * q], eta = Qp[2 * q + 1];
       const double xq = (1.0 - xi - eta) * x1 + xi * x2 + eta * x3;
       const double yq = (1.0 - xi - eta) * y1 + xi * y2 + eta * y3;
-      sq[q] = eval_field_kind(fkind, fprm, xq, yq);
+      sq[q] = eval_source_prepared(fkind, fprm, xq, yq);
     }
     __syncwarp();
     for (int i = lane; i < NW; i += 32) {
@@ -349,32 +359,32 @@ __global__ void __launch_bounds__(EWARPS * 32) k_element_chol(ElemArgs a) {
       } else if (col < NW + M) {
         const int f = (col - NW) / NT, j = (col - NW) - f * NT;
         const int fo = f * 2 + ((ob >> f) & 1);
-        v = tau * el[f] * Ff[(fo * NW + ia) * NT + j] +
-            kf * (b0f[f] * DMF[((0 * 6 + fo) * NW + ia) * NT + j] + b1f[f] * DMF[((1 * 6 + fo) * NW + ia) * NT + j]);
+        v = tau * sel3(f, el[0], el[1], el[2]) * Ff[(fo * NW + ia) * NT + j] +
+            kf * (sel3(f, b0f[0], b0f[1], b0f[2]) * DMF[((0 * 6 + fo) * NW + ia) * NT + j] +
+                  sel3(f, b1f[0], b1f[1], b1f[2]) * DMF[((1 * 6 + fo) * NW + ia) * NT + j]);
       } else {
         v = be[ia];
       }
       W[ia * LDW + col] = v;
     }
     __syncwarp();
-    // ---- S = U'U, carrying the right-hand sides: rows of U and Z = U'^-1 [R' | be] in place ----
+    // ---- S = U' D U (LDL', no square roots), carrying the right-hand sides ---------------------
+    // Elimination without pivoting (S is SPD): after step k, row k holds d_k and d_k U_k., and the
+    // right-hand sides R~ = (D U)'^-1 ... = L^-1 [R' | be]; Y = D^-1 R~ (row k scaled when it is
+    // final).  Lane l owns column j = k+1+l (RC - k - 1 <= 31 columns: one pass).
+    static_assert(RC <= 32, "one lane per column of [S | R' | be]");
     for (int k = 0; k < NW; ++k) {
       const double d = W[k * LDW + k];
       if (!(d > 0.0) && lane == 0) atomicOr(a.err, 2);  // not positive definite (LAPACK PosDefException)
-      const double u = sqrt(d);
-      const double ri = 1.0 / u;
-      __syncwarp();
-      for (int j = k + 1 + lane; j < RC; j += 32) W[k * LDW + j] *= ri;
-      if (lane == 0) {
-        W[k * LDW + k] = u;
-        rinv[k] = ri;
-      }
-      __syncwarp();
-      const int cols = RC - k - 1, rows = NW - k - 1;
-      for (int t = lane; t < rows * cols; t += 32) {
-        const int i = k + 1 + t / cols, j = k + 1 + (t - (t / cols) * cols);
-        if (j < i) continue;
-        W[i * LDW + j] -= W[k * LDW + i] * W[k * LDW + j];
+      const double r = recip_newton(d);
+      const int j = k + 1 + lane;
+      if (lane == 0) rinv[k] = r;
+      if (j < RC) {
+        const double t = W[k * LDW + j] * r;
+        if (j >= NW) Y[k * (M + 1) + (j - NW)] = t;
+#pragma unroll 4
+        for (int i = k + 1; i < NW; ++i)
+          if (j >= i) W[i * LDW + j] -= W[k * LDW + i] * t;
       }
       __syncwarp();
     }
@@ -388,36 +398,37 @@ __global__ void __launch_bounds__(EWARPS * 32) k_element_chol(ElemArgs a) {
         ++r;
       }
       const int c = (rem == M - r) ? M : r + rem;
-      double dot = 0.0;
+      double dot = 0.0;  // (R~' D^-1 R~)_rc = (R' S^-1 R')_rc
 #pragma unroll
-      for (int ia = 0; ia < NW; ++ia) dot += W[ia * LDW + NW + r] * W[ia * LDW + NW + c];
+      for (int ia = 0; ia < NW; ++ia) dot += Y[ia * (M + 1) + r] * W[ia * LDW + NW + c];
       if (c == M) {
         AB[r * (M + 1) + M] = -dot;
       } else {
         const int f = r / NT, i = r - f * NT, g = c / NT, j = c - g * NT;
         const int fo = f * 2 + ((ob >> f) & 1), go = g * 2 + ((ob >> g) & 1);
-        double v = dot - kf * (wn[f][0] * wn[g][0] + wn[f][1] * wn[g][1]) * PFF[((fo * 6 + go) * NT + i) * NT + j];
-        if (f == g) v -= hs * el[f] * Hh[i * NT + j];
+        const double wfx = sel3(f, wn[0][0], wn[1][0], wn[2][0]), wfy = sel3(f, wn[0][1], wn[1][1], wn[2][1]);
+        const double wgx = sel3(g, wn[0][0], wn[1][0], wn[2][0]), wgy = sel3(g, wn[0][1], wn[1][1], wn[2][1]);
+        double v = dot - kf * (wfx * wgx + wfy * wgy) * PFF[((fo * 6 + go) * NT + i) * NT + j];
+        if (f == g) v -= hs * sel3(f, el[0], el[1], el[2]) * Hh[i * NT + j];
         AB[r * (M + 1) + c] = v;
         if (c != r) AB[c * (M + 1) + r] = v;
       }
     }
     __syncwarp();
-    // ---- X_u = U^-1 Z (back substitution in place) and out --------------------------------------
-    for (int k = NW - 1; k >= 0; --k) {
-      const double ri = rinv[k];
-      for (int j = lane; j <= M; j += 32) W[k * LDW + NW + j] *= ri;
-      __syncwarp();
-      for (int t = lane; t < k * (M + 1); t += 32) {
-        const int i = t / (M + 1), j = t - (t / (M + 1)) * (M + 1);
-        W[i * LDW + NW + j] -= W[i * LDW + k] * W[k * LDW + NW + j];
+    // ---- X_u = U^-1 Y: lane j <= m owns column j; the back substitution runs in its registers,
+    // and each row of X_u goes out as one coalesced store of m+1 values --------------------------
+    if (lane <= M) {
+      double x[NW];
+#pragma unroll
+      for (int k = NW - 1; k >= 0; --k) {
+        double t = 0.0;
+#pragma unroll
+        for (int i = k + 1; i < NW; ++i) t += W[k * LDW + i] * x[i];
+        x[k] = Y[k * (M + 1) + lane] - rinv[k] * t;
       }
-      __syncwarp();
-    }
-    double* KB = a.KB + (size_t)e * NW * (M + 1);
-    for (int t = lane; t < NW * (M + 1); t += 32) {
-      const int ia = t / (M + 1), j = t - ia * (M + 1);
-      KB[t] = W[ia * LDW + NW + j];
+      double* KB = a.KB + (size_t)e * NW * (M + 1);
+#pragma unroll
+      for (int ia = 0; ia < NW; ++ia) KB[ia * (M + 1) + lane] = x[ia];
     }
     __syncwarp();
   }
@@ -470,7 +481,7 @@ template <int P, int EWARPS> size_t smem_bytes_chol(const ElemArgs& a) {
   constexpr int LDW = (D::NW + D::M + 1) | 1;
   const RefLayout& G = a.L;
   const int tab = (G.Q + 2 * a.nq - G.C) + 3 * D::NW * D::NW + (G.PFF + 36 * D::NT * D::NT - G.SDMF);
-  const int wstride = ((D::NW * LDW + a.nq + 2 * D::NW) + 1) & ~1;
+  const int wstride = ((D::NW * LDW + D::NW * (D::M + 1) + a.nq + 2 * D::NW) + 1) & ~1;
   return (size_t)(((tab + 1) & ~1) + EWARPS * wstride) * sizeof(double);
 }
 

@@ -43,6 +43,33 @@ __device__ __forceinline__ double eval_field_kind(int kind, const double* __rest
   }
   return 0.0;
 }
+// The source as the element kernels read it (CoefDev::fprep): Gaussian bumps carry -1/(2 s^2) in
+// place of s, every other kind its plain parameters.
+__device__ __forceinline__ double eval_source_prepared(int kind, const double* __restrict__ p, double x, double y) {
+  if (kind != HDG_FIELD_BUMPS) return eval_field_kind(kind, p, x, y);
+  const int K = (int)p[0];
+  double s = 0.0;
+  for (int k = 0; k < K; ++k) {
+    const double* b = p + 1 + 4 * k;
+    const double dx = x - b[0], dy = y - b[1];
+    s += b[3] * exp((dx * dx + dy * dy) * b[2]);
+  }
+  return s;
+}
+
+// 1/d by Newton-Raphson iteration from the FP32 approximate reciprocal: each step r <- r + r (1 - d r)
+// squares the relative error (about 2^-22 -> 2^-44 -> below 2^-53), so two steps give the FP64
+// reciprocal to within an ulp at a fraction of the cost of a correctly rounded FP64 division.
+// Outside the FP32 range the FP64 division is used.
+__device__ __forceinline__ double recip_newton(double d) {
+  const float df = (float)d;
+  if (!(fabsf(df) > 1e-30f && fabsf(df) < 1e30f)) return 1.0 / d;
+  double r = (double)__fdividef(1.0f, df);
+  r = fma(r, fma(-d, r, 1.0), r);
+  r = fma(r, fma(-d, r, 1.0), r);
+  return r;
+}
+
 __device__ __forceinline__ double eval_field_dev(const FieldDev& f, double x, double y) {
   return eval_field_kind(f.kind, f.prm, x, y);
 }

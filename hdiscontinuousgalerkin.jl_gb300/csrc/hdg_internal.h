@@ -110,6 +110,8 @@ struct CoefDev {
   const int32_t* koff;
   const double* kprm;
   const double* tau;         // [nprob]
+  // fprm with each Gaussian bump's width s replaced by -1/(2 s^2) (element kernels' source)
+  const double* fprep;
 };
 
 // ------------------------------------------------------------------ objects
@@ -256,7 +258,7 @@ struct hdg_system {
   std::vector<int32_t> h_seg_prob, h_seg_row0, h_seg_row1, h_prob_blk0, h_prob_nblk;  // host copies
   CoefDev coef_dev() const {
     return CoefDev{space->mesh->d_cell_prob.p, d_fkind.p, d_foff.p, d_fprm.p, d_kkind.p, d_koff.p, d_kprm.p,
-                   d_tau.p};
+                   d_tau.p, d_fprep.p};
   }
   // per-cell condensed blocks: AB = [Ate | bte] (m x (m+1)), KB = [K_e | b_e] (n x (m+1)), or,
   // after the Cholesky-Schur element path (kb_u_only), only its u rows [X_u | b_u] (nw x (m+1))
@@ -265,6 +267,7 @@ struct hdg_system {
   DevBuf<float> d_ABf, d_KBf;
   DevBuf<double> d_kappa;  // per-cell kappa (optional)
   DevBuf<double> d_fprm, d_kprm;
+  DevBuf<double> d_fprep;  // d_fprm prepared for the element kernels (CoefDev::fprep)
   FieldSpec f, kappa;
   bool kappa_field = false, kappa_cells = false;
   // Trace matrix.  Host: block rows sorted by face id (h_browptr/h_bcol, the export pattern).
@@ -298,6 +301,10 @@ struct hdg_system {
   // profiling
   EventPair ev_element, ev_gather, ev_apply, ev_cg, ev_recover;
   std::vector<EventPair*> ev_cg_a, ev_cg_b;
+  // level-0 multigrid smoother sweeps of the sampled chunks, each timed on its own
+  bool prof_cheb0 = false;
+  std::vector<EventPair*> ev_cheb0;
+  double prof_cheb0_bytes = 0.0;  // their algorithmic bytes (rows of the problems that iterated)
   // algorithmic bytes moved by the sampled CG launches (rows of the problems that iterated)
   double prof_a_bytes = 0.0, prof_b_bytes = 0.0;
   double prof_all_bytes = 0.0;  // algorithmic bytes of every iteration launch of the last solve
@@ -358,6 +365,10 @@ struct CgSolver {
   virtual void enqueue_status_copy() = 0;             // enqueue the per-problem status read-back
   virtual bool process(const hdg_solver& o) = 0;      // after the read-back: true when all problems are done
   virtual void finish(const hdg_solver& o, std::vector<hdg_stats>* out) = 0;
+  // finish() in two halves, for callers that do not wait: finish_enqueue queues the final true
+  // residual on the stream; finish_collect forms the statistics once that work has landed.
+  virtual void finish_enqueue() = 0;
+  virtual void finish_collect(std::vector<hdg_stats>* out) = 0;
   virtual void set_stream(cudaStream_t stream) = 0;   // stream of the iteration (after prepare)
   hdg_system* s = nullptr;
 };
@@ -377,6 +388,7 @@ void amg_setup_numeric(hdg_system* s, cudaStream_t st);
 void amg_apply(hdg_system* s, const float* r, float* z, const int32_t* cg_state, cudaStream_t st);
 int amg_cycle_launches(const hdg_system* s);                             // kernels per V-cycle
 double amg_cycle_bytes(const hdg_system* s);                             // algorithmic bytes per V-cycle
+double amg_cheb0_bytes_per_row(const hdg_system* s);  // level-0 sweeps of one V-cycle, per trace row
 
 void mesh_build_rectangle(hdg_mesh* m, int nx, int ny, const double LL[2], const double UR[2]);
 int mesh_build_from_cells(hdg_mesh* m, int nnodes, const double* xy, int ncells, const int32_t* cells1, int nedges,

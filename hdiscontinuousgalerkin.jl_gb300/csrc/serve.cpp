@@ -84,6 +84,47 @@ struct Flight {
   }
 };
 
+// A resident mesh's device-resident single-problem system: device mesh, space, trace system
+// (with its Dirichlet set recorded), CG state and multigrid hierarchy stay allocated between
+// requests.  A request on it uploads its source and coefficients, reassembles, applies the
+// recorded Dirichlet set, runs the multigrid numeric set-up and the CG, and recovers: no mesh,
+// space or system is built and no symbolic set-up runs.  The multigrid aggregates are the ones
+// fitted to the first request's matrix; later coefficients keep a valid preconditioner.
+struct ResidentSys {
+  hdg_ctx ctx;  // own stream
+  int mesh_id = -1, p = 0, qd = 0;
+  hdg_mesh* mesh = nullptr;
+  hdg_space* space = nullptr;
+  hdg_system* sys = nullptr;
+  CgSolver* cg = nullptr;
+  cudaEvent_t ready = nullptr;
+  bool busy = false;        // serving a request or being built
+  bool completing = false;  // CG done; the final residual, recovery and downloads are queued
+  int rep = 0;
+  size_t bytes = 0;
+  std::vector<Request> reqs;  // the request being served (one)
+  double* h_x = nullptr;      // page-locked destinations of the solution downloads
+  double* h_qu = nullptr;
+  explicit ResidentSys(int device) {
+    ctx.device = device;
+    ctx.own_stream = false;
+    ctx.profiling = false;
+    HDG_CUDA(cudaStreamCreateWithFlags(&ctx.stream, cudaStreamNonBlocking));
+    HDG_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+  }
+  ~ResidentSys() {
+    cudaStreamSynchronize(ctx.stream);
+    if (ready) cudaEventDestroy(ready);
+    delete cg;
+    if (sys) hdg_system_destroy(sys);
+    if (space) hdg_space_destroy(space);
+    if (mesh) hdg_mesh_destroy(mesh);
+    if (h_x) cudaFreeHost(h_x);
+    if (h_qu) cudaFreeHost(h_qu);
+    cudaStreamDestroy(ctx.stream);
+  }
+};
+
 struct hdg_engine {
   hdg_ctx* ctx = nullptr;
   double budget = 0;
@@ -92,6 +133,18 @@ struct hdg_engine {
   hdg_solver solver{};
   std::vector<std::shared_ptr<hdg_mesh>> resident;
   std::vector<int> resident_p;
+  // device-resident systems per resident mesh (HDG_ENGINE_RESIDENT_COPIES of them at most; 0 turns
+  // the resident path off and sends resident requests to union flights like the others)
+  std::vector<std::vector<std::unique_ptr<ResidentSys>>> rpool;
+  std::vector<ResidentSys*> ractive;  // serving a request
+  // Off by default: on the 2000 req/s stream 2 / 4 copies per mesh served 311 / 373 requests/s
+  // against 458 for union flights alone.  A resident request costs about 1 ms of host work, but a
+  // single small problem is launch-bound (some 29 kernels per multigrid CG iteration), and the
+  // aggregates fitted to the first request's kappa take about twice the iterations (157 against
+  // 77 on average) for the next requests' random kappa.
+  int resident_copies = 0;
+  int64_t n_resident_solves = 0;
+  double t_resident_start = 0;
   std::deque<Request> pending;
   std::vector<std::unique_ptr<Flight>> flights;
   std::deque<Result> done;
@@ -107,18 +160,20 @@ struct hdg_engine {
     std::vector<Request> reqs;
     int slot;
     size_t bytes;
+    ResidentSys* rs;  // a resident system to build (slot unused), or null for a flight
   };
   std::vector<std::thread> builders;
   std::mutex mu;
   std::condition_variable cv;
   std::deque<Job> jobs;
-  struct Done {  // a finished build: the flight, or the failure of its admission
+  struct Done {  // a finished build: the flight (or resident system), or the failure of its admission
     Flight* fl;
     int slot;
     size_t bytes;
     int rc;
     std::string msg;
     int nreq;
+    ResidentSys* rs;
   };
   std::vector<Done> built;
   int building = 0;       // jobs queued or being built
@@ -206,6 +261,60 @@ Flight* launch_flight(hdg_engine* e, std::vector<Request>&& reqs, int slot) {
   return fl.release();
 }
 
+// Builds a resident system from its first request and queues that request's solve (set-up and
+// first CG preparation, as a flight of one problem; the engine step gives it its chunks).
+void build_resident(hdg_engine* e, ResidentSys* rs, std::vector<Request>&& reqs) {
+  hdg_ctx* c = &rs->ctx;
+  const Request& r = reqs[0];
+  const hdg_mesh* part = request_mesh(e, r);
+  int rc = hdg_mesh_concat(c, 1, &part, &rs->mesh);
+  if (rc != HDG_OK) throw HdgError{rc, c->err};
+  rc = hdg_space_create(rs->mesh, r.p, r.qd, &rs->space);
+  if (rc != HDG_OK) throw HdgError{rc, c->err};
+  hdg_field f{r.f.kind, (int)r.f.prm.size(), r.f.prm.data()};
+  double tau = r.tau;
+  rc = hdg_assemble_condense_batch(rs->space, &tau, &f, nullptr, r.kappa.empty() ? nullptr : r.kappa.data(),
+                                   e->solver.precision, &rs->sys);
+  if (rc != HDG_OK) throw HdgError{rc, c->err};
+  int cnt = 0;
+  static const double kZero = 0.0;
+  hdg_field zero{HDG_FIELD_CONST, 1, &kZero};
+  rc = hdg_dirichlet(rs->space, "boundary", &zero, nullptr, nullptr, &cnt);
+  if (rc != HDG_OK) throw HdgError{rc, c->err};
+  std::vector<int32_t> dofs(cnt);
+  std::vector<double> vals(cnt);
+  rc = hdg_dirichlet(rs->space, "boundary", &zero, dofs.data(), vals.data(), &cnt);
+  if (rc == HDG_OK) rc = hdg_apply_dirichlet(rs->sys, dofs.data(), vals.data(), cnt);
+  if (rc != HDG_OK) throw HdgError{rc, c->err};
+  g_alloc_stream = c->stream;
+  HDG_CUDA(cudaMallocHost(&rs->h_x, sizeof(double) * rs->sys->ndofs));
+  HDG_CUDA(cudaMallocHost(&rs->h_qu, sizeof(double) * (size_t)rs->sys->nc * rs->sys->n));
+  rs->cg = make_cg_solver(rs->sys);
+  rs->cg->prepare(e->solver);
+  rs->reqs = std::move(reqs);
+  rs->rep = 0;
+}
+
+// Starts a request on an idle, built resident system (engine thread): new coefficients,
+// reassembly, apply! of the recorded Dirichlet set and the CG preparation (the multigrid's numeric
+// set-up) are queued on the system's stream; the engine step gives it its chunks.
+void start_resident(hdg_engine* e, ResidentSys* rs, Request&& r) {
+  hdg_system* s = rs->sys;
+  const cudaStream_t st = rs->ctx.stream;
+  hdg_field f{r.f.kind, (int)r.f.prm.size(), r.f.prm.data()};
+  double tau = r.tau;
+  int rc = hdg_system_set_coefficients_batch(s, &tau, &f, nullptr, r.kappa.empty() ? nullptr : r.kappa.data());
+  if (rc != HDG_OK) throw HdgError{rc, rs->ctx.err};
+  g_alloc_stream = st;
+  assemble_async(s, st);
+  launch_dirichlet_apply(s, st);
+  s->applied = true;
+  rs->cg->prepare(e->solver);
+  rs->reqs.clear();
+  rs->reqs.push_back(std::move(r));
+  rs->rep = 0;
+}
+
 // Worker thread: builds flights from the job queue until the engine stops.
 void builder_main(hdg_engine* e) {
   cudaSetDevice(e->ctx->device);
@@ -218,10 +327,14 @@ void builder_main(hdg_engine* e) {
       job = std::move(e->jobs.front());
       e->jobs.pop_front();
     }
-    hdg_engine::Done d{nullptr, job.slot, job.bytes, HDG_OK, std::string(), (int)job.reqs.size()};
+    hdg_engine::Done d{nullptr, job.slot, job.bytes, HDG_OK, std::string(), (int)job.reqs.size(), job.rs};
     try {
-      d.fl = launch_flight(e, std::move(job.reqs), job.slot);
-      d.fl->bytes = job.bytes;
+      if (job.rs) {
+        build_resident(e, job.rs, std::move(job.reqs));
+      } else {
+        d.fl = launch_flight(e, std::move(job.reqs), job.slot);
+        d.fl->bytes = job.bytes;
+      }
     } catch (const HdgError& err) {
       d.rc = err.code;
       d.msg = err.msg;
@@ -242,40 +355,53 @@ void builder_main(hdg_engine* e) {
   }
 }
 
-void complete_flight(hdg_engine* e, Flight* fl) {
+void file_results(hdg_engine* e, const hdg_system* s, const hdg_mesh* m, const std::vector<Request>& reqs,
+                  const std::vector<hdg_stats>& st, const double* x, const double* qu);
+
+// Finishes the CG of a flight or resident system, recovers q and u, and files one result per request.
+void complete_solves(hdg_engine* e, hdg_ctx* ctx, CgSolver* cg, hdg_system* s, const hdg_mesh* m,
+                     const std::vector<Request>& reqs) {
   std::vector<hdg_stats> st;
-  g_alloc_stream = fl->ctx.stream;
-  fl->cg->finish(e->solver, &st);
-  fl->sys->have_solution = true;
-  launch_recover(fl->sys, fl->ctx.stream);
-  fl->sys->have_recovery = true;
-  hdg_system* s = fl->sys;
+  g_alloc_stream = ctx->stream;
+  cg->finish(e->solver, &st);
+  s->have_solution = true;
+  launch_recover(s, ctx->stream);
+  s->have_recovery = true;
   std::vector<double> x, qu;
   if (e->keep_results) {
     x.resize(s->ndofs);
     qu.resize((size_t)s->nc * s->n);
-    s->d_x.download(x.data(), x.size(), fl->ctx.stream);
-    s->d_qu.download(qu.data(), qu.size(), fl->ctx.stream);
+    s->d_x.download(x.data(), x.size(), ctx->stream);
+    s->d_qu.download(qu.data(), qu.size(), ctx->stream);
   }
-  HDG_CUDA(cudaStreamSynchronize(fl->ctx.stream));
+  HDG_CUDA(cudaStreamSynchronize(ctx->stream));
+  file_results(e, s, m, reqs, st, x.data(), qu.data());
+}
+
+// One result per request of a finished system (x, qu: its downloaded solution, if kept).
+void file_results(hdg_engine* e, const hdg_system* s, const hdg_mesh* m, const std::vector<Request>& reqs,
+                  const std::vector<hdg_stats>& st, const double* x, const double* qu) {
   const double t = now_s();
-  const hdg_mesh* m = fl->mesh;
   const int nv = 2 * s->nw;
-  for (size_t P = 0; P < fl->reqs.size(); ++P) {
+  for (size_t P = 0; P < reqs.size(); ++P) {
     Result r;
-    r.id = fl->reqs[P].id;
-    r.t_submit = fl->reqs[P].t_submit;
+    r.id = reqs[P].id;
+    r.t_submit = reqs[P].t_submit;
     r.t_done = t;
     r.stats = st[P];
     if (e->keep_results) {
-      r.uhat.assign(x.begin() + (size_t)m->prob_face0[P] * s->nt, x.begin() + (size_t)m->prob_face0[P + 1] * s->nt);
+      r.uhat.assign(x + (size_t)m->prob_face0[P] * s->nt, x + (size_t)m->prob_face0[P + 1] * s->nt);
       for (int c = m->prob_cell0[P]; c < m->prob_cell0[P + 1]; ++c) {
-        r.q.insert(r.q.end(), qu.begin() + (size_t)c * s->n, qu.begin() + (size_t)c * s->n + nv);
-        r.u.insert(r.u.end(), qu.begin() + (size_t)c * s->n + nv, qu.begin() + (size_t)(c + 1) * s->n);
+        r.q.insert(r.q.end(), qu + (size_t)c * s->n, qu + (size_t)c * s->n + nv);
+        r.u.insert(r.u.end(), qu + (size_t)c * s->n + nv, qu + (size_t)(c + 1) * s->n);
       }
     }
     e->done.push_back(std::move(r));
   }
+}
+
+void complete_flight(hdg_engine* e, Flight* fl) {
+  complete_solves(e, &fl->ctx, fl->cg, fl->sys, fl->mesh, fl->reqs);
 }
 
 }  // namespace
@@ -301,12 +427,13 @@ int hdg_engine_create(hdg_ctx* ctx, double hbm_budget_gb, int max_batch, int max
     e->streams.resize(max_flights);
     e->stream_busy.assign(max_flights, 0);
     for (auto& s : e->streams) HDG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-    // HDG_ENGINE_BUILDERS worker threads build flights (default 4, at most the flight slots;
-    // on the 2000 req/s stream 2 builders served 331 requests/s, 4 served 339)
-    int nb = 4;
+    // HDG_ENGINE_BUILDERS worker threads build flights (default 8, at most the flight slots;
+    // on the 2000 req/s stream 4 / 8 / 12 builders served 392 / 458 / 429 requests/s)
+    int nb = 8;
     if (const char* env = std::getenv("HDG_ENGINE_BUILDERS")) nb = std::atoi(env);
     nb = std::max(1, std::min(nb, std::max(1, max_flights)));
     for (int i = 0; i < nb; ++i) e->builders.emplace_back(builder_main, e);
+    if (const char* env = std::getenv("HDG_ENGINE_RESIDENT_COPIES")) e->resident_copies = std::max(0, std::atoi(env));
     *out = e;
     return HDG_OK;
   } catch (const HdgError& err) {
@@ -319,6 +446,7 @@ int hdg_engine_add_resident_mesh(hdg_engine* e, const hdg_mesh* host_mesh, int p
   if (!e || !host_mesh || !mesh_id) return HDG_ERR_ARG;
   e->resident.push_back(copy_host_mesh(host_mesh));
   e->resident_p.push_back(p);
+  e->rpool.emplace_back();
   *mesh_id = (int)e->resident.size() - 1;
   return HDG_OK;
 }
@@ -372,7 +500,21 @@ int hdg_engine_step(hdg_engine* e, int* n_inflight, int* n_pending) {
     }
     int fail_rc = HDG_OK;
     for (auto& d : done) {
-      if (d.fl) {
+      if (d.rs) {
+        if (d.rc == HDG_OK) {
+          e->ractive.push_back(d.rs);
+        } else {  // the resident system could not be built: drop it, report after the step
+          auto& pool = e->rpool[d.rs->mesh_id];
+          for (size_t k = 0; k < pool.size(); ++k)
+            if (pool[k].get() == d.rs) {
+              pool.erase(pool.begin() + k);
+              break;
+            }
+          e->in_use -= d.bytes;
+          fail_rc = d.rc;
+          e->ctx->err = d.msg;
+        }
+      } else if (d.fl) {
         e->flights.emplace_back(d.fl);
       } else {  // the admission failed: free its slot and memory, report after the step
         e->stream_busy[d.slot] = 0;
@@ -381,14 +523,72 @@ int hdg_engine_step(hdg_engine* e, int* n_inflight, int* n_pending) {
         e->ctx->err = d.msg;
       }
     }
+    // 1a. requests on resident meshes of their registered degree go to an idle resident system of
+    //     that mesh (started here, nothing built), or to a new one while the mesh has fewer than
+    //     resident_copies (built by a builder), or wait for one to become idle
+    auto resident_eligible = [&](const Request& r) {
+      return e->resident_copies > 0 && r.mesh_id >= 0 && r.p == e->resident_p[r.mesh_id];
+    };
+    for (auto it = e->pending.begin(); it != e->pending.end();) {
+      if (!resident_eligible(*it)) {
+        ++it;
+        continue;
+      }
+      auto& pool = e->rpool[it->mesh_id];
+      ResidentSys* idle = nullptr;
+      for (auto& r : pool)
+        if (!r->busy && r->qd == it->qd) {
+          idle = r.get();
+          break;
+        }
+      if (idle) {
+        idle->busy = true;
+        const double t0 = now_s();
+        start_resident(e, idle, std::move(*it));
+        e->t_resident_start += now_s() - t0;
+        e->ractive.push_back(idle);
+        it = e->pending.erase(it);
+        continue;
+      }
+      const size_t b = bytes_per_cell(it->p) * (size_t)e->resident[it->mesh_id]->nc;
+      if ((int)pool.size() < e->resident_copies && e->in_use + b <= e->budget) {
+        pool.emplace_back(new ResidentSys(e->ctx->device));
+        ResidentSys* rs = pool.back().get();
+        rs->mesh_id = it->mesh_id;
+        rs->p = it->p;
+        rs->qd = it->qd;
+        rs->busy = true;
+        rs->bytes = b;
+        e->in_use += b;
+        std::vector<Request> one;
+        one.push_back(std::move(*it));
+        it = e->pending.erase(it);
+        {
+          std::lock_guard<std::mutex> lk(e->mu);
+          e->building_reqs += 1;
+          ++e->building;
+          e->jobs.push_back(hdg_engine::Job{std::move(one), -1, b, rs});
+        }
+        e->cv.notify_one();
+        continue;
+      }
+      ++it;
+    }
+    {
+      std::lock_guard<std::mutex> lk(e->mu);
+      building = e->building;
+    }
     // 1. admission: one flight per (degree, quadrature) group of the pending queue, FIFO order,
     //    handed to the builders
-    while (!e->pending.empty() && (int)e->flights.size() + building < e->max_flights) {
-      const int p = e->pending.front().p, qd = e->pending.front().qd;
+    while ((int)e->flights.size() + building < e->max_flights) {
+      auto first = e->pending.begin();
+      while (first != e->pending.end() && resident_eligible(*first)) ++first;
+      if (first == e->pending.end()) break;
+      const int p = first->p, qd = first->qd;
       std::vector<Request> take;
       size_t bytes = 0;
-      for (auto it = e->pending.begin(); it != e->pending.end() && (int)take.size() < e->max_batch;) {
-        if (it->p != p || it->qd != qd) { ++it; continue; }
+      for (auto it = first; it != e->pending.end() && (int)take.size() < e->max_batch;) {
+        if (it->p != p || it->qd != qd || resident_eligible(*it)) { ++it; continue; }
         const size_t b = bytes_per_cell(p) * (size_t)request_mesh(e, *it)->nc;
         if (e->in_use + bytes + b > e->budget && !take.empty()) break;
         if (e->in_use + bytes + b > e->budget && !e->flights.empty()) break;  // wait for memory
@@ -405,7 +605,7 @@ int hdg_engine_step(hdg_engine* e, int* n_inflight, int* n_pending) {
         std::lock_guard<std::mutex> lk(e->mu);
         e->building_reqs += (int)take.size();
         ++e->building;
-        e->jobs.push_back(hdg_engine::Job{std::move(take), slot, bytes});
+        e->jobs.push_back(hdg_engine::Job{std::move(take), slot, bytes, nullptr});
       }
       ++building;
       e->cv.notify_one();
@@ -446,12 +646,60 @@ int hdg_engine_step(hdg_engine* e, int* n_inflight, int* n_pending) {
         HDG_CUDA(cudaEventRecord(fl->ready, fl->ctx.stream));
         ++i;
       }
+      for (size_t i = 0; i < e->ractive.size();) {
+        ResidentSys* rs = e->ractive[i];
+        g_alloc_stream = rs->ctx.stream;
+        if (rs->rep > 0 || rs->completing) {
+          const cudaError_t q = cudaEventQuery(rs->ready);
+          if (q == cudaErrorNotReady) {
+            ++i;
+            continue;
+          }
+          HDG_CUDA(q);
+          progressed = true;
+          const double tc = now_s();
+          if (rs->completing) {  // the final residual, recovery and downloads have landed
+            std::vector<hdg_stats> st;
+            rs->cg->finish_collect(&st);
+            file_results(e, rs->sys, rs->mesh, rs->reqs, st, rs->h_x, rs->h_qu);
+            e->t_complete += now_s() - tc;
+            e->ctx->launches += rs->ctx.launches;
+            rs->ctx.launches = 0;
+            ++e->n_resident_solves;
+            rs->completing = false;
+            rs->busy = false;
+            e->ractive.erase(e->ractive.begin() + i);
+            continue;
+          }
+          if (rs->cg->process(e->solver)) {  // converged: queue the completion, poll it later
+            hdg_system* s = rs->sys;
+            rs->cg->finish_enqueue();
+            s->have_solution = true;
+            launch_recover(s, rs->ctx.stream);
+            s->have_recovery = true;
+            if (e->keep_results) {
+              s->d_x.download(rs->h_x, (size_t)s->ndofs, rs->ctx.stream);
+              s->d_qu.download(rs->h_qu, (size_t)s->nc * s->n, rs->ctx.stream);
+            }
+            HDG_CUDA(cudaEventRecord(rs->ready, rs->ctx.stream));
+            rs->completing = true;
+            e->t_complete += now_s() - tc;
+            ++i;
+            continue;
+          }
+        }
+        progressed = true;
+        rs->cg->launch_chunk(rs->rep++);
+        rs->cg->enqueue_status_copy();
+        HDG_CUDA(cudaEventRecord(rs->ready, rs->ctx.stream));
+        ++i;
+      }
       if (progressed || now_s() - tw > 2e-4) break;
       std::this_thread::yield();
     }
     if (!progressed) e->t_wait += now_s() - tw;
     if (n_inflight) {  // requests being built count as in flight
-      int n = 0;
+      int n = (int)e->ractive.size();
       for (auto& fl : e->flights) n += (int)fl->reqs.size();
       std::lock_guard<std::mutex> lk(e->mu);
       *n_inflight = n + e->building_reqs;
@@ -527,12 +775,15 @@ int hdg_engine_destroy(hdg_engine* e) {
   if (std::getenv("HDG_ENGINE_VERBOSE"))
     std::fprintf(stderr,
                  "engine: %lld steps %.3f s, %lld flights; host s: concat %.3f space %.3f assemble %.3f apply %.3f "
-                 "prepare %.3f complete %.3f wait %.3f\n",
+                 "prepare %.3f complete %.3f wait %.3f; resident solves %lld, start %.3f\n",
                  (long long)e->n_steps, e->t_steps, (long long)e->n_flights, e->t_concat, e->t_space, e->t_assemble,
-                 e->t_apply, e->t_prepare, e->t_complete, e->t_wait);
+                 e->t_apply, e->t_prepare, e->t_complete, e->t_wait, (long long)e->n_resident_solves,
+                 e->t_resident_start);
   cudaSetDevice(e->ctx->device);
   for (auto& fl : e->flights) cudaStreamSynchronize(fl->ctx.stream);
   e->flights.clear();
+  e->ractive.clear();
+  e->rpool.clear();
   for (auto s : e->streams) {
     cudaStreamSynchronize(s);
     cudaStreamDestroy(s);

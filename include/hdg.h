@@ -247,6 +247,12 @@ typedef struct {
 } hdg_timings;
 /* Per-phase device times recorded while profiling was on (0 where nothing was recorded). */
 int hdg_system_timings(hdg_system* sys, hdg_timings* out);
+/* No reference counterpart.  One kernel family timed launch by launch in the sampled chunks of
+ * the last solve (profiling on): the summed CUDA-event durations, the summed algorithmic bytes
+ * (rows of the problems that iterated times the bytes per row) and the number of launches.
+ * HDG_SAMPLE_CHEB0: the level-0 Chebyshev smoother sweeps of the multigrid cycle. */
+#define HDG_SAMPLE_CHEB0 1
+int hdg_system_kernel_sample(hdg_system* sys, int which, double* total_ms, double* total_bytes, int* launches);
 
 /* ---- batches of independent problems ------------------------------------------------ */
 /* No reference counterpart: the reference solves one problem per script run.  A batch is a
@@ -336,7 +342,10 @@ typedef struct hdg_engine hdg_engine;
 int hdg_engine_create(hdg_ctx* ctx, double hbm_budget_gb, int max_batch, int max_flights, const hdg_solver* opts,
                       hdg_engine** out);
 /* Registers a host mesh (built with ctx == NULL) of degree p as resident: requests on it need no
- * mesh construction. */
+ * mesh construction.  With HDG_ENGINE_RESIDENT_COPIES=k (default 0) the engine also keeps up to k
+ * device-resident single-problem systems per resident mesh (device mesh, space, trace system, CG
+ * state, multigrid hierarchy fitted to the first request's matrix); a request on an idle one only
+ * uploads its coefficients, reassembles and solves. */
 int hdg_engine_add_resident_mesh(hdg_engine* e, const hdg_mesh* host_mesh, int p, int* mesh_id);
 /* Queues a request on resident mesh `mesh_id`, or (mesh_id < 0) on its own host mesh `mesh`. */
 int hdg_engine_submit(hdg_engine* e, int mesh_id, const hdg_mesh* mesh, int p, int quad_degree, const hdg_field* f,
