@@ -108,21 +108,27 @@ __global__ void k_lag_gather(int64_t n, const int32_t* __restrict__ ptr, const i
 }
 
 // ---- apply! -------------------------------------------------------------------------------------
-// mean |diag K| in one block, a fixed summation order
-__global__ void k_lag_meandiag(int n, const int32_t* __restrict__ colptr, const int32_t* __restrict__ rowval,
-                               const double* __restrict__ val, double* __restrict__ sc) {
-  __shared__ double part[1024];
+// mean |diag K| in two deterministic levels: every block sums a grid-strided share of the
+// columns with a fixed tree (part[block]), then one block sums the partials in block order
+constexpr int MD_BLOCK = 256, MD_MAX_BLOCKS = 1024;
+__global__ void __launch_bounds__(MD_BLOCK) k_lag_meandiag_part(int n, const int32_t* __restrict__ colptr,
+                                                                const int32_t* __restrict__ rowval,
+                                                                const double* __restrict__ val,
+                                                                double* __restrict__ part) {
+  __shared__ double sh[32];
   double s = 0.0;
-  for (int j = threadIdx.x; j < n; j += blockDim.x)
+  for (int j = blockIdx.x * MD_BLOCK + threadIdx.x; j < n; j += gridDim.x * MD_BLOCK)
     for (int e = colptr[j]; e < colptr[j + 1]; ++e)
       if (rowval[e] == j) s += fabs(val[e]);
-  part[threadIdx.x] = s;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int k = 0; k < (int)blockDim.x; ++k) t += part[k];
-    sc[0] = t / n;
-  }
+  s = block_sum<MD_BLOCK>(s, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+__global__ void __launch_bounds__(MD_MAX_BLOCKS) k_lag_meandiag_final(int n, int nparts, const double* __restrict__ part,
+                                                                      double* __restrict__ sc) {
+  __shared__ double sh[32];
+  double s = (int)threadIdx.x < nparts ? part[threadIdx.x] : 0.0;
+  s = block_sum<MD_MAX_BLOCKS>(s, sh);
+  if (threadIdx.x == 0) sc[0] = s / n;
 }
 
 // b[r] -= sum over prescribed d (increasing) of v_d K[r, d]; K is symmetric, so row r's entries
@@ -522,7 +528,15 @@ int hdg_lagrange_apply_dirichlet(hdg_lagrange* L, const int32_t* dofs, const dou
       dv.upload(vals, n, st);
       k_lag_scatter<<<nblk(n), 256, 0, st>>>(n, dd.p, dv.p, L->d_pres.p, L->d_gv.p);
     }
-    k_lag_meandiag<<<1, 1024, 0, st>>>(nd, L->d_colptr.p, L->d_rowval.p, L->d_val.p, L->d_sc.p);
+    {
+      const int nparts = (int)std::min<int64_t>(std::max<int64_t>(((int64_t)nd + MD_BLOCK - 1) / MD_BLOCK, 1),
+                                                 MD_MAX_BLOCKS);
+      DevBuf<double> part;
+      part.alloc((size_t)nparts);
+      k_lag_meandiag_part<<<nparts, MD_BLOCK, 0, st>>>(nd, L->d_colptr.p, L->d_rowval.p, L->d_val.p, part.p);
+      k_lag_meandiag_final<<<1, MD_MAX_BLOCKS, 0, st>>>(nd, nparts, part.p, L->d_sc.p);
+      L->ctx->launches++;
+    }
     k_lag_lift<<<nblk(nd), 256, 0, st>>>(nd, L->d_colptr.p, L->d_rowval.p, L->d_val.p, L->d_pres.p, L->d_gv.p,
                                          L->d_b.p);
     k_lag_zero<<<nblk(nd), 256, 0, st>>>(nd, L->d_colptr.p, L->d_rowval.p, L->d_val.p, L->d_pres.p, L->d_gv.p,

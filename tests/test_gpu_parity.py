@@ -362,9 +362,15 @@ def test_batch_matches_single_problems(H, oracle):
             assert rel(u, r["u"]) < rtol * 10
 
 
-def test_serving_same_alone_and_in_mix(H):
+@pytest.mark.parametrize("copies", [0, 1])
+def test_serving_same_alone_and_in_mix(H, monkeypatch, copies):
     """Continuous batching: every request's result is the same when served alone and when served
-    in a mix of requests of several sizes and degrees (resident and new meshes), within 1e-8."""
+    in a mix of requests of several sizes and degrees (resident and new meshes), within 1e-8.  With
+    copies = 1 the requests on resident meshes run on the engine's device-resident systems
+    (HDG_ENGINE_RESIDENT_COPIES): two resident meshes get a second request with another source
+    and coefficient, which waits for the first and then reuses its system (reassembly, the
+    multigrid hierarchy built for the first request's matrix)."""
+    monkeypatch.setenv("HDG_ENGINE_RESIDENT_COPIES", str(copies))
     rng = np.random.default_rng(11)
     ctx = H.default_context()
     specs = []
@@ -372,28 +378,32 @@ def test_serving_same_alone_and_in_mix(H):
         f = H.Field.bumps(rng.random((8, 2)), 0.05 + 0.1 * rng.random(8), 10 * rng.standard_normal(8))
         kc = np.exp(rng.uniform(np.log(1e-2), np.log(1e2), 2 * n * n))
         specs.append((H.Problem(n=n, p=p, f=f, kappa_cell=kc, jitter=0.2, seed=500 + k)))
+    resident = list(range(len(specs)))[::2]
+    extra = []  # (mesh index, source, kappa) of the second requests on two resident meshes
+    for i in resident[:2]:
+        pr = specs[i]
+        f2 = H.Field.bumps(rng.random((8, 2)), 0.05 + 0.1 * rng.random(8), 10 * rng.standard_normal(8))
+        extra.append((i, f2, pr.kappa_cell[::-1].copy()))
 
-    def serve(subset, resident):
+    def serve(reqs, resident_ids):
         eng = H.Engine(ctx, hbm_budget_gb=8, max_batch=8, max_flights=4, tol=1e-11)
-        mids = {}
-        if resident:
-            for i in subset[::2]:
-                mids[i] = eng.add_resident(H.batch.host_mesh(specs[i]), specs[i].p)
-        rid = {}
-        for i in subset:
+        mids = {i: eng.add_resident(H.batch.host_mesh(specs[i]), specs[i].p) for i in resident_ids}
+        rid = []
+        for i, f, kc in reqs:
             pr = specs[i]
             if i in mids:
-                rid[i] = eng.submit(pr.p, pr.f, pr.kappa_cell, mesh_id=mids[i])
+                rid.append(eng.submit(pr.p, f, kc, mesh_id=mids[i]))
             else:
-                rid[i] = eng.submit(pr.p, pr.f, pr.kappa_cell, mesh=H.batch.host_mesh(pr))
+                rid.append(eng.submit(pr.p, f, kc, mesh=H.batch.host_mesh(pr)))
         done = eng.run_until_idle()
-        assert len(done) == len(subset) and all(d["converged"] for d in done)
-        return {i: eng.result(rid[i]) for i in subset}
+        assert len(done) == len(reqs) and all(d["converged"] for d in done)
+        return [eng.result(r) for r in rid]
 
-    mix = serve(list(range(len(specs))), resident=True)
-    for i in range(len(specs)):
-        alone = serve([i], resident=False)[i]
-        for a, b in zip(mix[i], alone):
+    reqs = [(i, specs[i].f, specs[i].kappa_cell) for i in range(len(specs))] + extra
+    mix = serve(reqs, resident)
+    for (i, f, kc), got in zip(reqs, mix):
+        alone = serve([(i, f, kc)], [])[0]
+        for a, b in zip(got, alone):
             assert rel(a, b) < 1e-8, i
 
 
