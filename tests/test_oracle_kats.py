@@ -244,3 +244,14 @@ def test_trace_solution_sensitivity_to_ulp_changes(oracle):
     x1 = solve(K1)
     d = np.linalg.norm(x1 - x0) / np.linalg.norm(x0)
     assert 1e-14 < d < 1e-12, d
+
+
+def test_fp32_condensation_needs_an_fp64_refinement_sweep():
+    """The element condensation in FP32 alone is far from the FP64 trace solution on a mesh with
+    kappa over four decades per cell, while an FP32 factorisation of the Schur complement followed
+    by one FP64 refinement sweep (residual and products in FP64) is within 1e-8
+    (oracle/fp32_condensation_study.py; on 2*32^2 cells at p = 4: 6e-3 and 6e-10)."""
+    import fp32_condensation_study as study
+    r = study.study(n=12, p=3, seed=5, refine=(1,))
+    assert r["variants"]["fp32"]["uhat_rel_l2"] > 1e-5, r
+    assert r["variants"]["fp32+1"]["uhat_rel_l2"] < 1e-8, r
