@@ -19,6 +19,7 @@ host cores instead.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import math
 import os
@@ -402,6 +403,22 @@ def run_c4(args, ws, rank, local):
                 "d2h_bytes_per_step": int(d2h)},
         "clocks": clk,
     }
+    # ---- the same kind of problems as a request stream through the serving engine: 2000 req/s for
+    # the completed rate, 250 req/s (below saturation) for the service latency ----
+    if not args.no_serving:
+        del B
+        plain.clear()
+        gc.collect()
+        torch.cuda.synchronize()
+        kw = dict(tol=tol, precision=args.precision, preconditioner=args.preconditioner,
+                  hbm_budget_gb=args.hbm_budget_gb, max_batch=args.max_batch, max_flights=args.max_flights,
+                  seed=777 + rank, plain_sample=0)
+        line["serving"] = {
+            "workload": SERVE_DESC + f", {args.precision}, {args.preconditioner}-preconditioned CG tol {tol:g}; "
+                                     "requests enter as host arrays and results are read back to host memory",
+            "at_2000_req_per_s": serve_stream(H, ctx, local, 2000.0, 1000, **kw),
+            "at_250_req_per_s": serve_stream(H, ctx, local, 250.0, 500, accuracy_sample=6, **kw)}
+
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         specs = c4_specs()
         idx = c4_cpu_sample_indices(specs)
@@ -559,25 +576,20 @@ def draw_coefficients(H, rng, n):
     return f, kc
 
 
-def run_c5(args, ws, rank, local):
-    """Serving workload: a Poisson stream of solve requests (2000 req/s by default, seeded); each request is
-    drawn like the batching workload; 70 % reuse one of 32 resident meshes with a new source and
-    coefficient, 30 % come with a new mesh.  The engine admits by HBM budget, runs flights on
-    separate streams and completes requests as their flights converge."""
+def serve_stream(H, ctx, local, rate, nreq, *, tol, precision, preconditioner, hbm_budget_gb, max_batch,
+                 max_flights, warmup=3, seed=777, plain_sample=48, accuracy_sample=12):
+    """A Poisson stream of `nreq` solve requests at `rate` req/s (seeded) through the serving engine.
+    Each request is drawn like the batching workload; 70 % reuse one of 32 resident meshes with a new
+    source and coefficient, 30 % come with a new mesh.  Requests enter as host arrays and every result
+    is read back to host memory, so the completed rate is an end-to-end figure.  Returns the measured
+    figures; `plain_sample` requests are also solved one at a time by the plain FP64 path for the
+    speed-up, and `accuracy_sample` completed requests are checked against FP64 solves at 1e-12."""
     import numpy as np
     import torch
 
-    import __graft_entry__ as g
-    g.build()
-    H = g.import_package()
-    torch.cuda.set_device(local)
-    ctx = H.Context(local)
-    tol = args.tol if args.tol != 1e-12 else 1e-9
-    nreq = args.requests
-    rate = args.rate
     if not rate > 0:
         raise SystemExit("--rate must be positive")
-    rng = np.random.default_rng(777 + rank)
+    rng = np.random.default_rng(seed)
     resident = []
     for k in range(32):
         n, p = draw_shape(rng)
@@ -597,10 +609,16 @@ def run_c5(args, ws, rank, local):
             sd = 50000 + k
             reqs.append(dict(t=t, mid=-1, n=n, p=p, f=f, kc=kc, seed=sd,
                              mesh=H.batch.host_mesh(H.Problem(n=n, p=p, f=f, jitter=0.2, seed=sd))))
+    for r in reqs:
+        # bytes a request carries to the device: kappa per cell, the source's parameters and, for a new
+        # mesh, its coordinates and connectivity
+        r["h2d"] = np.asarray(r["kc"]).nbytes + 8 * (len(r["f"].params) + 1) + (
+            sum(a.nbytes for a in r["mesh"]._topology()) if r["mesh"] is not None else 0)
 
-    eng = H.Engine(ctx, hbm_budget_gb=args.hbm_budget_gb, max_batch=args.max_batch, max_flights=args.max_flights,
-                   tol=tol, precision=H.PREC_MIXED if args.precision == "mixed" else H.PREC_FP64, keep_results=True,
-                   preconditioner=H.PRECOND_AMG if args.preconditioner == "amg" else H.PRECOND_JACOBI)
+    pc = H.PRECOND_AMG if preconditioner == "amg" else H.PRECOND_JACOBI
+    eng = H.Engine(ctx, hbm_budget_gb=hbm_budget_gb, max_batch=max_batch, max_flights=max_flights,
+                   tol=tol, precision=H.PREC_MIXED if precision == "mixed" else H.PREC_FP64, keep_results=True,
+                   preconditioner=pc)
     host_res = [H.batch.host_mesh(pr) for pr in resident]
     mids = [eng.add_resident(hm, pr.p) for hm, pr in zip(host_res, resident)]
 
@@ -610,16 +628,17 @@ def run_c5(args, ws, rank, local):
         return eng.submit(r["p"], r["f"], r["kc"], mesh=r["mesh"])
 
     # warm-up: a short burst through the engine (compiles graphs, fills the memory pool)
-    for w in range(max(args.warmup, 3)):
+    for w in range(max(warmup, 3)):
         for r in reqs[w * 16:(w + 1) * 16]:
             submit(r)
         for d in eng.run_until_idle():
             eng.result(d["id"])
     torch.cuda.synchronize()
 
-    sample = set(range(0, nreq, max(1, nreq // 12)))
+    sample = set(range(0, nreq, max(1, nreq // max(1, accuracy_sample)))) if accuracy_sample else set()
     id2k, kept = {}, {}
     lat, its, res, conv = [], [], [], []
+    h2d = d2h = 0
     clocks = ClockSampler(local)
     clocks.start()
     launches0 = ctx.launches()
@@ -638,6 +657,9 @@ def run_c5(args, ws, rank, local):
         for d in eng.poll():
             k = id2k[d["id"]]
             uh, q, u = eng.result(d["id"])
+            r = reqs[k]
+            h2d += r["h2d"]
+            d2h += uh.nbytes + q.nbytes + u.nbytes
             if k in sample:
                 kept[k] = (uh, q, u)
             lat.append(d["latency"])
@@ -669,8 +691,7 @@ def run_c5(args, ws, rank, local):
         t1 = time.perf_counter()
         K, b, _, _ = H.doassemble(Vh, Wh, Mh, 1.0, pr.f, kappa_cell=pr.kappa_cell)
         H.apply_(K, b, H.Dirichlet(H.TrialFunction(Mh), dm, "boundary"))
-        uh = H.solve(K, b, tol=tol_, precision=H.PREC_FP64,
-                     preconditioner=H.PRECOND_AMG if args.preconditioner == "amg" else H.PRECOND_JACOBI)
+        uh = H.solve(K, b, tol=tol_, precision=H.PREC_FP64, preconditioner=pc)
         q, u, _ = K.recover()
         t2 = time.perf_counter()
         return t2 - t1, (uh, q, u)
@@ -680,26 +701,59 @@ def run_c5(args, ws, rank, local):
         _, ref = plain_solve(reqs[k], 1e-12)
         errs.append(max(rel_l2(got[0], ref[0]), rel_l2(got[1].ravel(), ref[1].ravel()),
                         rel_l2(got[2].ravel(), ref[2].ravel())))
-    plain_t = [plain_solve(reqs[k], tol)[0] for k in range(0, min(nreq, 48))]
-    plain_rate = len(plain_t) / sum(plain_t)
+    out = {
+        "rate_req_per_s": rate, "requests": nreq, "completed_per_s": served,
+        "ms_per_request": 1e3 * (t_last - first) / nreq,
+        "p50_ms": lat_ms[len(lat_ms) // 2], "p99_ms": lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))],
+        "h2d_bytes_per_request": h2d / nreq, "d2h_bytes_per_request": d2h / nreq,
+        "max_rel_l2_err_vs_fp64": max(errs) if errs else None, "accuracy_sample": len(errs),
+        "all_converged": bool(all(conv)), "max_rel_residual": float(max(res)),
+        "cg_iterations_mean": float(np.mean(its)), "wall_s": wall, "gpu_launches": launches, "clocks": clk,
+    }
+    if plain_sample:
+        plain_t = [plain_solve(reqs[k], tol)[0] for k in range(0, min(nreq, plain_sample))]
+        out["plain_fp64_solves_per_s"] = len(plain_t) / sum(plain_t)
+        out["plain_fp64_p50_ms"] = 1e3 * statistics.median(plain_t)
+    return out
+
+
+SERVE_DESC = ("c5: Poisson request stream (seeded), each request drawn like the batching workload; 70% on one of "
+              "32 resident meshes with a new source and kappa, 30% new meshes; continuous batching")
+
+
+def run_c5(args, ws, rank, local):
+    """Serving workload: the request stream of serve_stream at --rate (2000 req/s by default)."""
+    import torch
+
+    import __graft_entry__ as g
+    g.build()
+    H = g.import_package()
+    torch.cuda.set_device(local)
+    ctx = H.Context(local)
+    tol = args.tol if args.tol != 1e-12 else 1e-9
+    s = serve_stream(H, ctx, local, args.rate, args.requests, tol=tol, precision=args.precision,
+                     preconditioner=args.preconditioner, hbm_budget_gb=args.hbm_budget_gb, max_batch=args.max_batch,
+                     max_flights=args.max_flights, warmup=args.warmup, seed=777 + rank)
     line = {
-        "metric": METRIC, "value": served, "unit": "solves/s", "n_gpus": ws, "steps": nreq,
-        "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * (t_last - first) / nreq, "higher_is_better": True,
+        "metric": METRIC, "value": s["completed_per_s"], "unit": "solves/s", "n_gpus": ws, "steps": s["requests"],
+        "warmup": max(args.warmup, 3), "ms_per_step": s["ms_per_request"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if args.precision == "mixed" else "f64",
         "data": "synthetic",
-        "config": {"workload": f"c5: Poisson request stream at {rate:g} req/s (seeded), each drawn like the batching "
-                               "workload; 70% on one of 32 resident meshes with a new source and kappa, 30% new meshes;"
-                               f" continuous batching, {args.precision}, {args.preconditioner}-preconditioned CG "
-                               f"tol {tol:g}",
-                   "requests": nreq, "hbm_budget_gb": args.hbm_budget_gb, "max_batch": args.max_batch,
+        "config": {"workload": SERVE_DESC + f" at {args.rate:g} req/s, {args.precision}, {args.preconditioner}-"
+                               f"preconditioned CG tol {tol:g}",
+                   "requests": s["requests"], "hbm_budget_gb": args.hbm_budget_gb, "max_batch": args.max_batch,
                    "max_flights": args.max_flights, "step": "one request solved"},
-        "p50_ms": lat_ms[len(lat_ms) // 2], "p99_ms": lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))],
-        "plain_fp64_solves_per_s": plain_rate,
-        "plain_fp64_p50_ms": 1e3 * statistics.median(plain_t),
-        "speedup_vs_plain": served / plain_rate,
-        "max_rel_l2_err_vs_fp64": max(errs) if errs else None, "accuracy_sample": len(errs),
-        "all_converged": bool(all(conv)), "cg_iterations_mean": float(np.mean(its)), "wall_s": wall,
-        "gpu_launches": launches, "clocks": clk,
+        "p50_ms": s["p50_ms"], "p99_ms": s["p99_ms"],
+        "plain_fp64_solves_per_s": s["plain_fp64_solves_per_s"],
+        "plain_fp64_p50_ms": s["plain_fp64_p50_ms"],
+        "speedup_vs_plain": s["completed_per_s"] / s["plain_fp64_solves_per_s"],
+        "max_rel_l2_err_vs_fp64": s["max_rel_l2_err_vs_fp64"], "accuracy_sample": s["accuracy_sample"],
+        "all_converged": s["all_converged"], "cg_iterations_mean": s["cg_iterations_mean"], "wall_s": s["wall_s"],
+        "e2e": {"value": s["completed_per_s"], "unit": "solves/s",
+                "h2d_bytes_per_step": int(s["h2d_bytes_per_request"]),
+                "d2h_bytes_per_step": int(s["d2h_bytes_per_request"]),
+                "note": "requests enter as host arrays and results are read back to host memory"},
+        "gpu_launches": s["gpu_launches"], "clocks": s["clocks"],
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -837,6 +891,8 @@ def parse():
                     help="trace CG preconditioner (default: amg for the batch c4 and the stream c5, jacobi "
                          "otherwise); the plain FP64 paths of c4 and c5 use the same one")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true",
+                    help="c4 only: leave out the request-stream figures (the serving key)")
     ap.add_argument("--n", type=int, default=None, help="c1/c2 only: cells per side (a profiling case, not a bench line)")
     ap.add_argument("--p", type=int, default=None, help="c1/c2 only: polynomial degree (a profiling case)")
     args = ap.parse_args()
