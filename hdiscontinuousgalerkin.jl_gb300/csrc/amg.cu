@@ -578,18 +578,18 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
 // Numeric setup kernels
 namespace {
 
-__device__ __forceinline__ void atomic_max_pos(float* a, float v) {  // v >= 0: int order = float order
-  atomicMax(reinterpret_cast<int*>(a), __float_as_int(v));
-}
-
 // Inverse of each face's diagonal block (Gauss-Jordan, partial pivoting) and the per-problem
 // Gershgorin bound of D^-1 A0: max over rows of sum_j |(D^-1 A0)_ij|.
 template <int NT>
 __global__ void k_amg_block_inv(int nf, const int32_t* __restrict__ bcol5, const int8_t* __restrict__ kdiag,
                                 const float* __restrict__ val, const int32_t* __restrict__ face_prob,
                                 float* __restrict__ dinv, float* __restrict__ lam) {
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= nf) return;
+  // Threads past the end repeat the last face (whole warps stay for the reduction at the end) and
+  // write nothing.
+  const int fg = blockIdx.x * blockDim.x + threadIdx.x;
+  if (fg - (int)(threadIdx.x & 31) >= nf) return;  // whole warps past the end
+  const bool own = fg < nf;
+  const int f = own ? fg : nf - 1;
   const int64_t nd = (int64_t)nf * NT;
   float a[NT][2 * NT];
   const int kd = kdiag[f];
@@ -616,8 +616,9 @@ __global__ void k_amg_block_inv(int nf, const int32_t* __restrict__ bcol5, const
       for (int j = 0; j < 2 * NT; ++j) a[i][j] -= m * a[c][j];
     }
   }
-  for (int i = 0; i < NT; ++i)
-    for (int j = 0; j < NT; ++j) dinv[((int64_t)f * NT + i) * NT + j] = a[i][NT + j];
+  if (own)
+    for (int i = 0; i < NT; ++i)
+      for (int j = 0; j < NT; ++j) dinv[((int64_t)f * NT + i) * NT + j] = a[i][NT + j];
   // row sums of |D^-1 A0| over the face's rows
   float rs[NT];
   for (int i = 0; i < NT; ++i) rs[i] = 0.f;
@@ -636,7 +637,12 @@ __global__ void k_amg_block_inv(int nf, const int32_t* __restrict__ bcol5, const
   }
   float mx = 0.f;
   for (int i = 0; i < NT; ++i) mx = fmaxf(mx, rs[i]);
-  atomic_max_pos(lam + face_prob[f], mx);
+  // one atomic per problem present in the warp (consecutive faces mostly share one): the lanes of
+  // a problem take their maximum first (non-negative floats order like their bit patterns)
+  const int P = own ? face_prob[f] : -1;
+  const unsigned grp = __match_any_sync(0xffffffffu, P);
+  const int mxi = __reduce_max_sync(grp, __float_as_int(mx));
+  if (own && (int)(threadIdx.x & 31) == __ffs(grp) - 1) atomicMax(reinterpret_cast<int*>(lam + P), mxi);
 }
 
 // P0 = (I - w D^-1 A0) P_tent, w = 4/(3 lambda); one thread per face (all its nt rows).
@@ -742,27 +748,32 @@ __device__ __forceinline__ void add_at(const int32_t* __restrict__ col, float* _
   if (e < b && col[e] == key) val[e] += v;
 }
 
-// A1 = P0' (A0 P0), one thread per coarse row.
+// A1 = P0' (A0 P0), one warp per coarse row.  For each of the row's P0' entries (face f, mode c)
+// and each of the face's rows i in turn, the lanes take the entries of the A0 P0 row: their
+// columns are distinct, so no two lanes add to the same coarse entry at once, and every entry
+// receives its terms in the order (t, i) whatever the launch.
 template <int NT>
 __global__ void k_amg_rap0(int na, int wap, const int32_t* __restrict__ rptr0, const int32_t* __restrict__ rent0,
                            const float* __restrict__ pval0, const int32_t* __restrict__ apcol0,
                            const float* __restrict__ apval0, const int32_t* __restrict__ ptr1,
                            const int32_t* __restrict__ col1, float* __restrict__ val1) {
-  const int J = blockIdx.x * blockDim.x + threadIdx.x;
-  if (J >= na) return;
+  const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int J = (int)(gt >> 5), lane = threadIdx.x & 31;
+  if (J >= na) return;  // whole warps
   const int a0 = ptr1[J], a1 = ptr1[J + 1];
-  for (int e = a0; e < a1; ++e) val1[e] = 0.f;
+  for (int e = a0 + lane; e < a1; e += 32) val1[e] = 0.f;
+  __syncwarp();
   for (int t = rptr0[J]; t < rptr0[J + 1]; ++t) {
     const int f = rent0[t] / PW, c = rent0[t] - f * PW;
     for (int i = 0; i < NT; ++i) {
       const float p = pval0[((int64_t)f * NT + i) * PW + c];
       if (p == 0.f) continue;
       const float* apr = apval0 + ((int64_t)f * NT + i) * wap;
-      for (int q = 0; q < wap; ++q) {
+      for (int q = lane; q < wap; q += 32) {
         const int K = apcol0[(int64_t)f * wap + q];
-        if (K < 0) break;
-        add_at(col1, val1, a0, a1, K, p * apr[q]);
+        if (K >= 0) add_at(col1, val1, a0, a1, K, p * apr[q]);
       }
+      __syncwarp();
     }
   }
 }
@@ -794,37 +805,46 @@ __global__ void k_amg_p(int n, const int32_t* __restrict__ ptr, const int32_t* _
   add_at(pcol, pval, p0, p1, agg[i], tent[i]);
 }
 
-// A P on a CSR level, one thread per row
+// A P on a CSR level, one warp per row: for each entry (i, k) of A's row in turn, the lanes take
+// the entries of P's row k, whose columns are distinct (so no two lanes add to the same entry at
+// once, and each entry receives its terms in the order of A's row).
 __global__ void k_amg_ap(int n, const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
                          const float* __restrict__ val, const int32_t* __restrict__ pptr,
                          const int32_t* __restrict__ pcol, const float* __restrict__ pval,
                          const int32_t* __restrict__ apptr, const int32_t* __restrict__ apcol,
                          float* __restrict__ apval) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int i = (int)(gt >> 5), lane = threadIdx.x & 31;
+  if (i >= n) return;  // whole warps
   const int a0 = apptr[i], a1 = apptr[i + 1];
-  for (int e = a0; e < a1; ++e) apval[e] = 0.f;
+  for (int e = a0 + lane; e < a1; e += 32) apval[e] = 0.f;
+  __syncwarp();
   for (int e = ptr[i]; e < ptr[i + 1]; ++e) {
     const int k = col[e];
     const float a = val[e];
-    for (int t = pptr[k]; t < pptr[k + 1]; ++t) add_at(apcol, apval, a0, a1, pcol[t], a * pval[t]);
+    for (int t = pptr[k] + lane; t < pptr[k + 1]; t += 32) add_at(apcol, apval, a0, a1, pcol[t], a * pval[t]);
+    __syncwarp();
   }
 }
 
-// A_{l+1} = P' (A P), one thread per coarse row
+// A_{l+1} = P' (A P), one warp per coarse row: for each of the row's P' entries (fine row i) in
+// turn, the lanes take the entries of the A P row i (distinct columns), as in k_amg_rap0.
 __global__ void k_amg_rap(int nc, const int32_t* __restrict__ rptr, const int32_t* __restrict__ rent,
                           const int32_t* __restrict__ rrow, const float* __restrict__ pval,
                           const int32_t* __restrict__ apptr, const int32_t* __restrict__ apcol,
                           const float* __restrict__ apval, const int32_t* __restrict__ cptr,
                           const int32_t* __restrict__ ccol, float* __restrict__ cval) {
-  const int J = blockIdx.x * blockDim.x + threadIdx.x;
-  if (J >= nc) return;
+  const int64_t gt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int J = (int)(gt >> 5), lane = threadIdx.x & 31;
+  if (J >= nc) return;  // whole warps
   const int a0 = cptr[J], a1 = cptr[J + 1];
-  for (int e = a0; e < a1; ++e) cval[e] = 0.f;
+  for (int e = a0 + lane; e < a1; e += 32) cval[e] = 0.f;
+  __syncwarp();
   for (int t = rptr[J]; t < rptr[J + 1]; ++t) {
     const float p = pval[rent[t]];
     const int i = rrow[t];
-    for (int q = apptr[i]; q < apptr[i + 1]; ++q) add_at(ccol, cval, a0, a1, apcol[q], p * apval[q]);
+    for (int q = apptr[i] + lane; q < apptr[i + 1]; q += 32) add_at(ccol, cval, a0, a1, apcol[q], p * apval[q]);
+    __syncwarp();
   }
 }
 
@@ -1283,7 +1303,7 @@ template <int NT> void numeric_nt(hdg_system* s, const float* val0, cudaStream_t
   k_amg_ap0<NT><<<nblk((int64_t)nf * NT), 256, 0, st>>>(nf, H->wap, s->d_bcol5.p, val0, H->pcol0.p, H->pval0.p,
                                                         H->apmap0.p, H->apval0.p);
   AmgLevel& L1 = H->lev[0];
-  k_amg_rap0<NT><<<nblk(L1.n), 256, 0, st>>>(L1.n, H->wap, H->rptr0.p, H->rent0.p, H->pval0.p, H->apcol0.p,
+  k_amg_rap0<NT><<<nblk((int64_t)L1.n * 32), 256, 0, st>>>(L1.n, H->wap, H->rptr0.p, H->rent0.p, H->pval0.p, H->apcol0.p,
                                              H->apval0.p, L1.ptr.p, L1.col.p, L1.val.p);
   k_amg_dp0<NT><<<nblk(nf), 256, 0, st>>>(nf, s->d_kdiag.p, val0, H->pval0.p, H->dpval0.p);
   if (amg_level0_fp32()) {
@@ -1301,9 +1321,9 @@ template <int NT> void numeric_nt(hdg_system* s, const float* val0, cudaStream_t
     AmgLevel& C = H->lev[l + 1];
     k_amg_p<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.agg.p, L.tent.p, L.pptr.p,
                                        L.pcol.p, L.pval.p);
-    k_amg_ap<<<nblk(L.n), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.pptr.p, L.pcol.p, L.pval.p, L.apptr.p,
+    k_amg_ap<<<nblk((int64_t)L.n * 32), 256, 0, st>>>(L.n, L.ptr.p, L.col.p, L.val.p, L.pptr.p, L.pcol.p, L.pval.p, L.apptr.p,
                                         L.apcol.p, L.apval.p);
-    k_amg_rap<<<nblk(C.n), 256, 0, st>>>(C.n, L.rptr.p, L.rent.p, L.rrow.p, L.pval.p, L.apptr.p, L.apcol.p,
+    k_amg_rap<<<nblk((int64_t)C.n * 32), 256, 0, st>>>(C.n, L.rptr.p, L.rent.p, L.rrow.p, L.pval.p, L.apptr.p, L.apcol.p,
                                          L.apval.p, C.ptr.p, C.col.p, C.val.p);
     s->ctx->launches += 3;
   }

@@ -138,45 +138,62 @@ void build_segments(hdg_system* s) {
 namespace {
 constexpr int S5 = hdg_system::SLOTS;
 
-// val[(k nt + j) ndofs + r] = sum over sources of Ate_c[lf nt + i, lg nt + j], r = f nt + i
-template <int NT>
-__global__ void k_gather(const int nf, const int32_t* __restrict__ src5, const double* __restrict__ AB,
-                         double* __restrict__ val) {
-  constexpr int M = 3 * NT, MS = M + 1;
-  const int64_t ndofs = (int64_t)nf * NT, nval = ndofs * S5 * NT;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nval; t += (int64_t)gridDim.x * blockDim.x) {
-    const int s = (int)(t / ndofs);
-    const int r = (int)(t - (int64_t)s * ndofs);
-    const int f = r / NT, i = r - f * NT, k = s / NT, j = s - k * NT;
-    const int* sp = src5 + ((int64_t)k * nf + f) * 2;
-    double v = 0.0;
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      const int sr = sp[q];
-      if (sr >= 0) {
-        const int c = sr / 9, lf = (sr / 3) % 3, lg = sr % 3;
-        v += AB[(int64_t)c * M * MS + (lf * NT + i) * MS + lg * NT + j];
-      }
-    }
-    val[t] = v;
-  }
-}
+// Assembly of the trace system from the condensed blocks, GF faces per CTA:
+//   val[(k nt + j) ndofs + r] = sum over sources of Ate_c[lf nt + i, lg nt + j],  r = f nt + i
+//   b[r] = sum over the face's cells of bte_c[lf nt + i]        (assemble!(K, gdof, Ate) and (b, gdof, bte))
+// The CTA first copies, for each of its faces and each of the face's two cells, the cell's nt rows of
+// [Ate | bte] that belong to the face (one contiguous run of nt (m+1) doubles) into shared memory,
+// then writes the faces' 5 nt x nt slot blocks slot-major, so that both the reads and the writes
+// are contiguous.  The sources of a slot are added in the order src5 lists them (first the face's
+// first cell), the right-hand side's in the face's cell order.  Shared rows are padded to an odd
+// number of doubles so that the threads of a half-warp (consecutive rows of consecutive faces)
+// fall on different banks.
+template <int NT> struct GatherTile {
+  static constexpr int M = 3 * NT, MS = M + 1;
+  static constexpr int MSP = MS | 1;                             // padded row
+  static constexpr int RBP = (NT * MSP) | 1;                     // padded row block (one face, one cell)
+  static constexpr int GF = 32;                                  // faces per CTA
+  static constexpr size_t SMEM = sizeof(double) * (size_t)GF * 2 * RBP;
+};
 
-// b[f nt + i] = sum over the face's cells of bte_c[lf nt + i] (assemble!(rhs, gdof, bte))
 template <int NT>
-__global__ void k_gather_rhs(const int nf, const int32_t* __restrict__ fcell, const int8_t* __restrict__ flf,
-                             const double* __restrict__ AB, double* __restrict__ b) {
-  constexpr int M = 3 * NT, MS = M + 1;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nf * NT) return;
-  const int f = t / NT, i = t - f * NT;
-  double v = 0.0;
-#pragma unroll
-  for (int k = 0; k < 2; ++k) {
-    const int c = fcell[2 * f + k];
-    if (c >= 0) v += AB[(int64_t)c * M * MS + (flf[2 * f + k] * NT + i) * MS + M];
+__global__ void __launch_bounds__(256) k_gather_faces(const int nf, const int32_t* __restrict__ fcell,
+                                                      const int8_t* __restrict__ flf,
+                                                      const int32_t* __restrict__ src5,
+                                                      const double* __restrict__ AB, double* __restrict__ val,
+                                                      double* __restrict__ b) {
+  using T = GatherTile<NT>;
+  constexpr int M = T::M, MS = T::MS, MSP = T::MSP, RBP = T::RBP, GF = T::GF, RB = NT * MS;
+  extern __shared__ double sm[];
+  const int f0 = blockIdx.x * GF;
+  const int nfb = min(GF, nf - f0);
+  for (int t = threadIdx.x; t < nfb * 2 * RB; t += blockDim.x) {
+    const int fq = t / RB, e = t - fq * RB;                  // fq = 2 (face in tile) + side
+    const int c = fcell[2 * f0 + fq];
+    const int i = e / MS, col = e - i * MS;
+    sm[fq * RBP + i * MSP + col] = c >= 0 ? AB[(int64_t)c * M * MS + (int64_t)flf[2 * f0 + fq] * RB + e] : 0.0;
   }
-  b[t] = v;
+  __syncthreads();
+  const int64_t ndofs = (int64_t)nf * NT;
+  const int nr = nfb * NT;                                       // rows of the tile
+  for (int t = threadIdx.x; t < S5 * NT * nr; t += blockDim.x) {
+    const int sl = t / nr, r = t - sl * nr;
+    const int fl = r / NT, i = r - fl * NT, k = sl / NT, j = sl - k * NT;
+    const int f = f0 + fl;
+    const int2 sp = *reinterpret_cast<const int2*>(src5 + ((int64_t)k * nf + f) * 2);
+    const int c1 = fcell[2 * f];
+    double v = 0.0;
+    if (sp.x >= 0) v += sm[(2 * fl + (sp.x / 9 == c1 ? 0 : 1)) * RBP + i * MSP + (sp.x % 3) * NT + j];
+    if (sp.y >= 0) v += sm[(2 * fl + (sp.y / 9 == c1 ? 0 : 1)) * RBP + i * MSP + (sp.y % 3) * NT + j];
+    val[(int64_t)sl * ndofs + (int64_t)f0 * NT + r] = v;
+  }
+  for (int r = threadIdx.x; r < nr; r += blockDim.x) {
+    const int fl = r / NT, i = r - fl * NT;
+    double v = 0.0;
+    v += sm[(2 * fl) * RBP + i * MSP + M];
+    if (fcell[2 * (f0 + fl) + 1] >= 0) v += sm[(2 * fl + 1) * RBP + i * MSP + M];
+    b[(int64_t)f0 * NT + r] = v;
+  }
 }
 
 // meandiag(K) = mean |K_ii| of each problem (src/boundary.jl:169-175), a deterministic
@@ -252,15 +269,14 @@ __global__ void k_scatter_dirichlet(const int n, const int32_t* __restrict__ dof
 }
 
 template <int NT> void gather_t(hdg_system* s, cudaStream_t st) {
+  using T = GatherTile<NT>;
   hdg_mesh* m = s->space->mesh;
-  const int64_t nval = (int64_t)s->ndofs * S5 * NT;
-  int blocks = (int)std::min<int64_t>((nval + 255) / 256, 152 * 32);
-  k_gather<NT><<<blocks, 256, 0, st>>>(m->nf, s->d_src5.p, s->d_AB.p, s->d_val.p);
+  if (m->nf <= 0) return;
+  const unsigned blocks = (unsigned)((m->nf + T::GF - 1) / T::GF);
+  k_gather_faces<NT><<<blocks, 256, T::SMEM, st>>>(m->nf, m->d_fcell.p, m->d_flf.p, s->d_src5.p, s->d_AB.p,
+                                                    s->d_val.p, s->d_b.p);
   HDG_CUDA(cudaGetLastError());
-  const int nrow = m->nf * NT;
-  k_gather_rhs<NT><<<(nrow + 255) / 256, 256, 0, st>>>(m->nf, m->d_fcell.p, m->d_flf.p, s->d_AB.p, s->d_b.p);
-  HDG_CUDA(cudaGetLastError());
-  s->ctx->launches += 2;
+  s->ctx->launches += 1;
 }
 
 // Scatter of the prescribed dofs and values into per-row flags and values (d_pres, d_gv): the
