@@ -38,6 +38,10 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <numeric>
 
 #include <cuda_fp16.h>
@@ -50,6 +54,40 @@ constexpr int AMG_MAX_COARSE = 96;  // per problem, dense inverse on the coarses
 constexpr int AMG_MAX_LEVELS = 12;
 constexpr int AMG_CINV_MAX = 150;   // largest dense coarsest block: (2 m^2 + m) floats of shared memory
 constexpr int PW = 5;               // level-0 prolongator row width (a face and its 4 neighbours)
+constexpr int AMG_TAIL_THREADS = 512;  // threads of a k_amg_tail CTA (one CTA per problem)
+
+// Lanes per row of a coarse level with n rows (see the coarse-level kernels).
+inline int amg_group(int n) { return n >= 16384 ? 4 : (n >= 2048 ? 8 : 32); }
+
+constexpr int AMG_TAIL_MAXROWS = 4096;  // largest problem level the tail kernel may take
+constexpr int AMG_ROW_SWEEP_FACES = 100000;  // untuned default: a thread per row below this many faces
+
+// The coarse levels below some level T can be cycled by one k_amg_tail launch (one CTA per
+// problem) instead of a launch per kernel per level; both give the same bits, and the V-cycle
+// autotuner (amg_tune) picks T by timing.  HDG_AMG_TAIL_ROWS=k forces T = the first level whose
+// largest problem has at most k rows (0: no tail) and leaves T out of the tuning; -1 (unset):
+// tuned.
+int amg_tail_rows() {
+  static const int v = [] {
+    const char* e = std::getenv("HDG_AMG_TAIL_ROWS");
+    const int k = e ? std::atoi(e) : -1;
+    return (k >= -1 && k <= 65536) ? k : -1;
+  }();
+  return v;
+}
+
+// Level-0 smoother variant: -1 tuned (default), 0 a thread per face, 1 a thread per row
+// (HDG_AMG_SWEEP=face|row).  Both give the same bits.
+int amg_sweep_forced() {
+  static const int v = [] {
+    const char* e = std::getenv("HDG_AMG_SWEEP");
+    if (!e) return -1;
+    if (std::strcmp(e, "face") == 0) return 0;
+    if (std::strcmp(e, "row") == 0) return 1;
+    return -1;
+  }();
+  return v;
+}
 
 // Greedy aggregation on an adjacency graph (CSR, symmetric, no self loops needed):
 // 1. a node whose active neighbours are all free becomes a root with all of them;
@@ -183,6 +221,18 @@ struct AmgLevel {  // a scalar level l >= 1 (rows = aggregates of level l-1)
   DevBuf<int32_t> apptr, apcol;       // A P pattern
   DevBuf<float> apval;
   DevBuf<int32_t> rptr, rent, rrow;   // P': per coarse row the P entries (index, fine row)
+  DevBuf<int32_t> prow0;              // [nprob+1] first row of each problem (rows are grouped by problem)
+  int maxrows = 0;                    // rows of the largest problem
+};
+
+// One level as the tail kernel (k_amg_tail) reads it.
+struct TailLevel {
+  int g;                                      // lanes per row (amg_group of the level's rows)
+  const int32_t *ptr, *col, *prow0;
+  const float *val, *dl1inv;
+  float *b, *x, *t, *r;
+  const int32_t *pptr, *pcol, *rptr, *rent, *rrow;  // transfer to the next level
+  const float* pval;
 };
 
 struct AmgHierarchy {
@@ -211,6 +261,11 @@ struct AmgHierarchy {
   DevBuf<int32_t> crow0, coff;   // coff: offset of each problem's dense block
   DevBuf<float> cinv;
   int cmax = 0;
+  int tail_from = -1;        // first level (index into lev) cycled by k_amg_tail; -1: none
+  std::vector<int> tail_cands; // levels the tail may start at (problems' rows <= AMG_TAIL_MAXROWS)
+  DevBuf<TailLevel> tail_tab;  // every level's arrays for k_amg_tail
+  bool row_sweep = false;    // level-0 smoother: a thread per row (else per face)
+  bool tuned = false;        // the V-cycle autotuner has run (or its choice was taken from its cache)
   bool built = false;
 };
 
@@ -540,6 +595,33 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
     L.t.alloc(std::max(L.n, 1));
     L.r.alloc(std::max(L.n, 1));
   }
+  // per-problem row ranges of every level (aggregates are numbered by their smallest member, so a
+  // problem's rows are contiguous on every level) and the first level the tail kernel takes
+  bool grouped = true;
+  for (auto& L : H->lev) {
+    std::vector<int32_t> r0(s->nprob + 1, 0);
+    for (int i = 0; i < L.n; ++i) {
+      if (i > 0 && L.h_prob[i] < L.h_prob[i - 1]) grouped = false;
+      ++r0[L.h_prob[i] + 1];
+    }
+    L.maxrows = 0;
+    for (int P = 0; P < s->nprob; ++P) {
+      L.maxrows = std::max(L.maxrows, r0[P + 1]);
+      r0[P + 1] += r0[P];
+    }
+    L.prow0.upload(r0.data(), r0.size(), st);
+  }
+  H->tail_from = -1;
+  H->tail_cands.clear();
+  H->tuned = false;
+  H->row_sweep = nf < AMG_ROW_SWEEP_FACES;
+  const int tail_rows = amg_tail_rows();
+  if (grouped)
+    for (int l = 1; l + 1 < (int)H->lev.size(); ++l) {
+      if (tail_rows < 0 && H->lev[l].maxrows <= AMG_TAIL_MAXROWS) H->tail_cands.push_back(l);
+      if (tail_rows > 0 && H->tail_from < 0 && H->lev[l].maxrows <= tail_rows) H->tail_from = l;
+    }
+  if (H->tail_from >= 0) H->tail_cands.assign(1, H->tail_from);
   // coarsest: per-problem dense blocks
   const AmgLevel& C = H->lev.back();
   H->h_crow0.assign(s->nprob + 1, 0);
@@ -557,6 +639,15 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
   H->crow0.upload(H->h_crow0.data(), H->h_crow0.size(), st);
   H->coff.upload(coff.data(), coff.size(), st);
   H->cinv.alloc(std::max(coff[s->nprob], 1));
+  if (!H->tail_cands.empty()) {
+    std::vector<TailLevel> tab(H->lev.size());
+    for (size_t l = 0; l < H->lev.size(); ++l) {
+      const AmgLevel& L = H->lev[l];
+      tab[l] = TailLevel{amg_group(L.n), L.ptr.p, L.col.p, L.prow0.p, L.val.p, L.dl1inv.p, L.b.p, L.x.p, L.t.p,
+                         L.r.p, L.pptr.p, L.pcol.p, L.rptr.p, L.rent.p, L.rrow.p, L.pval.p};
+    }
+    H->tail_tab.upload(tab.data(), tab.size(), st);
+  }
   H->built = true;
   if (verbose) {  // level sizes: rows (largest problem's rows); host time of the set-up phases (ms)
     tph[7] = clk();
@@ -569,7 +660,7 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
       for (int i = 0; i < L.n; ++i) ++cnt[L.h_prob[i]];
       std::fprintf(stderr, ", %d (%d)", L.n, *std::max_element(cnt.begin(), cnt.end()));
     }
-    std::fprintf(stderr, "\n");
+    std::fprintf(stderr, "; tail from level %d\n", H->tail_from + 1);
   }
   HDG_CUDA(cudaStreamSynchronize(st));
 }
@@ -1218,6 +1309,143 @@ __global__ void k_amg_coarse_solve(const int32_t* __restrict__ crow0, const int3
   }
 }
 
+// ---- the coarse levels below a row limit, one CTA per problem ----------------------------
+// k_amg_tail runs the part of the V-cycle from level T down to the coarsest and back up to level
+// T for one problem per CTA, with a CTA barrier between the phases instead of a kernel boundary:
+// (nu - 1) sweeps, residual and restriction (with the next level's first sweep) on each level
+// going down, the dense coarsest solve, then prolongation and nu sweeps on each level going up.
+// Each row is computed exactly as the per-level kernels compute it (the same G lanes per row,
+// taken from the level's size, the same per-lane order and shuffle tree), and the iterates move
+// through the same buffers, so the cycle's result is bit-identical to theirs.
+struct TailArgs {
+  int T, nl, nu;
+  const TailLevel* L;  // device copy of the level table (nl entries), built with the hierarchy
+  const int32_t *crow0, *coff;
+  const float* cinv;
+  const int32_t* st;
+};
+
+__device__ __forceinline__ float group_sum_rt(float v, int G) {
+  for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Rows [r0, r1) in groups of G lanes: FN(row, lane, active) returns the lane's partial sum (0 when
+// inactive); every lane of a warp runs the same number of rounds, so the shuffles name all lanes.
+template <typename FN, typename OUT>
+__device__ __forceinline__ void tail_rows(int r0, int r1, int G, FN part, OUT out) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, rpw = 32 / G;
+  const int nw = AMG_TAIL_THREADS / 32;
+  for (int base = r0 + warp * rpw; base < r1; base += nw * rpw) {
+    const int i = base + lane / G, gl = lane % G;
+    const bool on = i < r1;
+    float v = on ? part(i, gl) : 0.f;
+    v = group_sum_rt(v, G);
+    if (on && gl == 0) out(i, v);
+  }
+}
+
+__global__ void __launch_bounds__(AMG_TAIL_THREADS) k_amg_tail(TailArgs a) {
+  const int P = blockIdx.x;
+  if (!amg_live(a.st, P)) return;
+  float* iter[AMG_MAX_LEVELS];
+  const int nu = a.nu, last = a.nl - 1;
+  // down
+  for (int l = a.T; l < last; ++l) {
+    const TailLevel L = a.L[l];
+    const TailLevel C = a.L[l + 1];
+    const int r0 = L.prow0[P], r1 = L.prow0[P + 1];
+    float* cur = L.x;
+    float* oth = L.t;
+    for (int sw = 1; sw < nu; ++sw) {
+      const float* xin = cur;
+      float* xout = oth;
+      tail_rows(r0, r1, L.g,
+                [&](int i, int gl) {
+                  float s = 0.f;
+                  for (int e = L.ptr[i] + gl; e < L.ptr[i + 1]; e += L.g) s += L.val[e] * xin[L.col[e]];
+                  return s;
+                },
+                [&](int i, float s) { xout[i] = xin[i] + (L.b[i] - s) * L.dl1inv[i]; });
+      __syncthreads();
+      float* tmp = cur;
+      cur = oth;
+      oth = tmp;
+    }
+    iter[l] = cur;
+    {
+      const float* x = cur;
+      tail_rows(r0, r1, L.g,
+                [&](int i, int gl) {
+                  float s = 0.f;
+                  for (int e = L.ptr[i] + gl; e < L.ptr[i + 1]; e += L.g) s += L.val[e] * x[L.col[e]];
+                  return s;
+                },
+                [&](int i, float s) { L.r[i] = L.b[i] - s; });
+    }
+    __syncthreads();
+    const bool coarsest = (l + 1 == last);
+    tail_rows(C.prow0[P], C.prow0[P + 1], C.g,
+              [&](int J, int gl) {
+                float s = 0.f;
+                for (int k = L.rptr[J] + gl; k < L.rptr[J + 1]; k += C.g) s += L.pval[L.rent[k]] * L.r[L.rrow[k]];
+                return s;
+              },
+              [&](int J, float s) {
+                C.b[J] = s;
+                if (!coarsest) C.x[J] = s * C.dl1inv[J];
+              });
+    __syncthreads();
+  }
+  // coarsest: x = A^-1 b
+  {
+    const TailLevel C = a.L[last];
+    const int r0 = a.crow0[P], m = a.crow0[P + 1] - r0;
+    const float* A = a.cinv + a.coff[P];
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+      float s = 0.f;
+      for (int j = 0; j < m; ++j) s += A[i * m + j] * C.b[r0 + j];
+      C.x[r0 + i] = s;
+    }
+  }
+  __syncthreads();
+  // up
+  const float* fin = a.L[last].x;
+  for (int l = last - 1; l >= a.T; --l) {
+    const TailLevel L = a.L[l];
+    const int r0 = L.prow0[P], r1 = L.prow0[P + 1];
+    float* x = iter[l];
+    float* y = L.r;
+    {
+      const float* xc = fin;
+      tail_rows(r0, r1, L.g,
+                [&](int i, int gl) {
+                  float s = 0.f;
+                  for (int e = L.pptr[i] + gl; e < L.pptr[i + 1]; e += L.g) s += L.pval[e] * xc[L.pcol[e]];
+                  return s;
+                },
+                [&](int i, float s) { x[i] += s; });
+    }
+    __syncthreads();
+    for (int sw = 0; sw < nu; ++sw) {
+      const float* xin = x;
+      float* xout = y;
+      tail_rows(r0, r1, L.g,
+                [&](int i, int gl) {
+                  float s = 0.f;
+                  for (int e = L.ptr[i] + gl; e < L.ptr[i + 1]; e += L.g) s += L.val[e] * xin[L.col[e]];
+                  return s;
+                },
+                [&](int i, float s) { xout[i] = xin[i] + (L.b[i] - s) * L.dl1inv[i]; });
+      __syncthreads();
+      float* tmp = x;
+      x = y;
+      y = tmp;
+    }
+    fin = x;
+  }
+}
+
 inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)std::max<int64_t>(1, (n + t - 1) / t); }
 
 // Degree of the level-0 Chebyshev smoother (HDG_AMG_CHEB_DEGREE, 1..4, default 4): each degree
@@ -1280,8 +1508,6 @@ int amg_cheb_degree() {
   return k;
 }
 
-// Lanes per row of a coarse level with n rows (see the coarse-level kernels).
-inline int amg_group(int n) { return n >= 16384 ? 4 : (n >= 2048 ? 8 : 32); }
 #define AMG_LAUNCH_G(KERNEL, ROWS, ST, ...)                                                        \
   do {                                                                                             \
     const int rows_ = (ROWS);                                                                      \
@@ -1340,10 +1566,9 @@ template <int NT> void numeric_nt(hdg_system* s, const float* val0, cudaStream_t
   HDG_CUDA(cudaGetLastError());
 }
 
-// One level-0 Chebyshev step: a thread per row below AMG_ROW_SWEEP_FACES faces (latency-bound
-// sizes), a thread per face above.  Measured: 49 k faces (p = 4): rows 15 -> 10 us per sweep;
-// 197 k faces (p = 2) and the batch's bins (0.4-0.7 M faces): faces faster.
-constexpr int AMG_ROW_SWEEP_FACES = 100000;
+// One level-0 Chebyshev step, a thread per row or a thread per face (H->row_sweep, tuned; both
+// give the same bits).  Measured before the tuner: 49 k faces (p = 4): rows 15 -> 10 us per
+// sweep; 197 k faces (p = 2) and the batch's bins (0.4-0.7 M faces): faces faster.
 template <int NT, typename VT>
 void cheb_sweep(hdg_system* s, const VT* val0, const float* b0, const float* in, float* out, int step,
                 const int32_t* cst, cudaStream_t st) {
@@ -1354,7 +1579,7 @@ void cheb_sweep(hdg_system* s, const VT* val0, const float* b0, const float* in,
     ep = new EventPair();
     ep->start(st);
   }
-  if (nf < AMG_ROW_SWEEP_FACES)
+  if (H->row_sweep)
     k_amg_row_cheb<NT, VT><<<nblk((int64_t)nf * NT), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->dinv0.p, H->lam0.p,
                                                               H->face_prob.p, b0, H->bt0.p, in, out, H->d0.p, step,
                                                               amg_cheb_ratio(s), cst);
@@ -1391,7 +1616,9 @@ void apply_nt(hdg_system* s, const VT* val0, const float* b0, float* z0, const i
   const int nu = amg_coarse_sweeps();
   float* iter[AMG_MAX_LEVELS];
   float* fin[AMG_MAX_LEVELS];
-  for (int l = 0; l + 1 < nl; ++l) {
+  // levels from T on (the coarsest included) are cycled by one k_amg_tail launch
+  const int T = H->tail_from >= 0 ? H->tail_from : nl;
+  for (int l = 0; l + 1 < std::min(T + 1, nl); ++l) {
     AmgLevel& L = H->lev[l];
     AmgLevel& C = H->lev[l + 1];
     float* cur = L.x.p;
@@ -1407,12 +1634,24 @@ void apply_nt(hdg_system* s, const VT* val0, const float* b0, float* z0, const i
     AMG_LAUNCH_G(k_amg_restrict, C.n, st, C.n, L.rptr.p, L.rent.p, L.rrow.p, L.pval.p, L.r.p,
                  coarsest ? nullptr : C.dl1inv.p, C.b.p, C.x.p, C.prob.p, cst);
   }
-  AmgLevel& C = H->lev.back();
-  if (H->cmax > 0) k_amg_coarse_solve<<<s->nprob, 128, 0, st>>>(H->crow0.p, H->coff.p, H->cinv.p, C.b.p, C.x.p, cst);
-  fin[nl - 1] = C.x.p;
+  int up_from = nl - 2;
+  if (T < nl) {
+    const TailArgs ta{T, nl, nu, H->tail_tab.p, H->crow0.p, H->coff.p, H->cinv.p, cst};
+    k_amg_tail<<<s->nprob, AMG_TAIL_THREADS, 0, st>>>(ta);
+    // where the tail leaves level T's result: the iterate after nu - 1 sweeps from x (alternating
+    // with t), then nu sweeps from it alternating with r
+    AmgLevel& L = H->lev[T];
+    float* it = ((nu - 1) % 2 == 0) ? L.x.p : L.t.p;
+    fin[T] = (nu % 2 == 0) ? it : L.r.p;
+    up_from = T - 1;
+  } else {
+    AmgLevel& C = H->lev.back();
+    if (H->cmax > 0) k_amg_coarse_solve<<<s->nprob, 128, 0, st>>>(H->crow0.p, H->coff.p, H->cinv.p, C.b.p, C.x.p, cst);
+    fin[nl - 1] = C.x.p;
+  }
   // coarse levels up: prolongate the coarser level's result into this level's iterate, then nu
   // sweeps alternating with r (free again); the last one holds the level's result
-  for (int l = nl - 2; l >= 0; --l) {
+  for (int l = up_from; l >= 0; --l) {
     AmgLevel& L = H->lev[l];
     float* a = iter[l];
     float* b = L.r.p;
@@ -1439,6 +1678,8 @@ void apply_nt(hdg_system* s, const VT* val0, const float* b0, float* z0, const i
 // The FP32 level-0 matrix: the system's FP32 copy when it has one, else a copy made here.
 const float* amg_level0_values(hdg_system* s, cudaStream_t st);
 
+void amg_tune(hdg_system* s, cudaStream_t st);
+
 void amg_setup_numeric(hdg_system* s, cudaStream_t st) {
   const float* v0 = amg_level0_values(s, st);
   switch (s->nt) {
@@ -1447,6 +1688,7 @@ void amg_setup_numeric(hdg_system* s, cudaStream_t st) {
     case 4: numeric_nt<4>(s, v0, st); break;
     case 5: numeric_nt<5>(s, v0, st); break;
   }
+  if (!s->amg->tuned) amg_tune(s, st);
 }
 
 // Algorithmic bytes of one V-cycle: every array a cycle kernel reads or writes, once (gathered
@@ -1496,8 +1738,9 @@ double amg_cheb0_bytes_per_row(const hdg_system* s) {
 int amg_cycle_launches(const hdg_system* s) {
   const int nl = (int)s->amg->lev.size(), k = amg_cheb_degree(), nu = amg_coarse_sweeps();
   // level 0 down, coarse levels down, coarsest, coarse levels up, level 0 up (the D2D copy of an
-  // odd degree is no kernel)
-  return (k + 2) + (nu + 1) * (nl - 1) + 1 + (nu + 1) * (nl - 1) + (1 + k);
+  // odd degree is no kernel); levels from the tail's first on are one launch
+  const int T = s->amg->tail_from >= 0 ? s->amg->tail_from : nl - 1;
+  return (k + 2) + (nu + 1) * T + 1 + (nu + 1) * T + (1 + k);
 }
 
 template <typename VT> void apply_dispatch(hdg_system* s, const VT* v0, const float* r, float* z,
@@ -1516,6 +1759,114 @@ void amg_apply(hdg_system* s, const float* r, float* z, const int32_t* cg_state,
   else
     apply_dispatch<float>(s, s->amg->val0f.p, r, z, cg_state, st);
   HDG_CUDA(cudaGetLastError());
+}
+
+// ---- V-cycle autotuner ---------------------------------------------------------------------
+// The launch shapes of the cycle that do not change its result are picked by timing, once per
+// hierarchy: the level-0 smoother with a thread per face or per row, and the level T from which
+// one k_amg_tail launch (a CTA per problem) replaces the per-level launches (or none).  Every
+// candidate computes the same bits, so the choice changes only the time.  Each candidate runs
+// the cycle once untimed and three times timed (CUDA events on the system's stream, on a zero
+// right-hand side: the cycle's work does not depend on the values); the fastest minimum wins.
+// Choices are cached by (nt, log2 faces, log2 problems, levels), so systems of similar shape
+// reuse them; a system marked one-shot (amg_tune_time false: the serving engine's flights) takes
+// a cached choice when there is one and the defaults otherwise, without timing.
+namespace {
+struct TuneKey {
+  int nt, lnf, lnp, nl;
+  bool operator<(const TuneKey& o) const { return std::tie(nt, lnf, lnp, nl) < std::tie(o.nt, o.lnf, o.lnp, o.nl); }
+};
+struct TuneVal {
+  bool row;
+  int tail;
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneVal> g_tune;
+int ilog2(int64_t v) {
+  int k = 0;
+  while (v > 1) {
+    v >>= 1;
+    ++k;
+  }
+  return k;
+}
+}  // namespace
+
+void amg_tune(hdg_system* s, cudaStream_t st) {
+  AmgHierarchy* H = s->amg;
+  H->tuned = true;
+  const int fs = amg_sweep_forced();
+  if (fs >= 0) H->row_sweep = (fs == 1);
+  const bool tune_sweep = fs < 0;
+  const bool tune_tail = amg_tail_rows() < 0 && !H->tail_cands.empty();
+  if (!tune_sweep && !tune_tail) return;
+  const bool verbose = std::getenv("HDG_AMG_VERBOSE") != nullptr;
+  const TuneKey key{s->nt, ilog2(H->nf), ilog2(std::max(s->nprob, 1)), (int)H->lev.size()};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      if (tune_sweep) H->row_sweep = it->second.row;
+      if (tune_tail) {
+        const int t = it->second.tail;
+        const bool ok = t < 0 || std::find(H->tail_cands.begin(), H->tail_cands.end(), t) != H->tail_cands.end();
+        H->tail_from = ok ? t : -1;
+      }
+      return;
+    }
+  }
+  if (!s->amg_tune_time) return;  // the defaults: sweep by face count, no tail
+  const int64_t n0 = (int64_t)H->nf * s->nt;
+  DevBuf<float> rin, zout;
+  rin.alloc((size_t)n0);
+  zout.alloc((size_t)n0);
+  HDG_CUDA(cudaMemsetAsync(rin.p, 0, sizeof(float) * n0, st));
+  std::vector<int> rows = tune_sweep ? std::vector<int>{0, 1} : std::vector<int>{(int)H->row_sweep};
+  std::vector<int> tails{H->tail_from};
+  if (tune_tail) {
+    tails.assign(1, -1);
+    tails.insert(tails.end(), H->tail_cands.begin(), H->tail_cands.end());
+  }
+  const bool prof = s->prof_cheb0;
+  s->prof_cheb0 = false;
+  cudaEvent_t e0, e1;
+  HDG_CUDA(cudaEventCreate(&e0));
+  HDG_CUDA(cudaEventCreate(&e1));
+  float best = 3.4e38f;
+  bool brow = H->row_sweep;
+  int btail = H->tail_from;
+  for (int rw : rows)
+    for (int tl : tails) {
+      H->row_sweep = (rw == 1);
+      H->tail_from = tl;
+      amg_apply(s, rin.p, zout.p, nullptr, st);
+      float tmin = 3.4e38f;
+      for (int rep = 0; rep < 3; ++rep) {
+        HDG_CUDA(cudaEventRecord(e0, st));
+        amg_apply(s, rin.p, zout.p, nullptr, st);
+        HDG_CUDA(cudaEventRecord(e1, st));
+        HDG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        HDG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        tmin = std::min(tmin, ms);
+      }
+      s->ctx->launches += 4 * amg_cycle_launches(s);
+      if (verbose)
+        std::fprintf(stderr, "amg tune: nt %d, %d faces, %d problems: %s sweep, tail from level %d: %.1f us\n", s->nt,
+                     H->nf, s->nprob, rw ? "row" : "face", tl + 1, 1e3 * tmin);
+      if (tmin < best) {
+        best = tmin;
+        brow = (rw == 1);
+        btail = tl;
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  H->row_sweep = brow;
+  H->tail_from = btail;
+  s->prof_cheb0 = prof;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = TuneVal{brow, btail};
 }
 
 namespace {

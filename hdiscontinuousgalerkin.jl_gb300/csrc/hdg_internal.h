@@ -303,6 +303,10 @@ struct hdg_system {
   std::vector<EventPair*> ev_cg_a, ev_cg_b;
   // level-0 multigrid smoother sweeps of the sampled chunks, each timed on its own
   bool prof_cheb0 = false;
+  // The multigrid V-cycle autotuner may time candidates when it has no cached choice for this
+  // system's shape; one-shot systems (the serving engine's flights) take a cached choice or the
+  // defaults instead.
+  bool amg_tune_time = true;
   std::vector<EventPair*> ev_cheb0;
   double prof_cheb0_bytes = 0.0;  // their algorithmic bytes (rows of the problems that iterated)
   // algorithmic bytes moved by the sampled CG launches (rows of the problems that iterated)

@@ -254,6 +254,7 @@ Flight* launch_flight(hdg_engine* e, std::vector<Request>&& reqs, int slot) {
   t0 = now_s();
   fl->t[3] += t0 - t1;
   g_alloc_stream = c->stream;
+  fl->sys->amg_tune_time = false;  // a flight is solved once: no timing of V-cycle variants
   fl->cg = make_cg_solver(fl->sys);
   fl->cg->prepare(e->solver);
   HDG_CUDA(cudaEventCreateWithFlags(&fl->ready, cudaEventDisableTiming));

@@ -683,3 +683,56 @@ def test_unstructured_at_scale_parity(H, oracle, tmp_path, p):
     q, u, _ = K.recover()
     oq, ou, _ = S.recover(ref)
     assert rel_l2(u, ou) <= 1e-10
+
+
+_TAIL_SCRIPT = r"""
+import os, sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+import __graft_entry__ as g
+H = g.import_package()
+rng = np.random.default_rng(11)
+probs = []
+for k, (n, p) in enumerate([(64, 2), (24, 2), (48, 2), (16, 3), (40, 3)]):
+    f = H.Field.bumps(rng.random((8, 2)), 0.05 + 0.1 * rng.random(8), 10 * rng.standard_normal(8))
+    kc = np.exp(rng.uniform(np.log(1e-2), np.log(1e2), 2 * n * n))
+    probs.append(H.Problem(n=n, p=p, f=f, kappa_cell=kc, jitter=0.2, seed=300 + k))
+B = H.Batch(H.default_context(), probs, precision=H.PREC_MIXED)
+stats = B.solve(tol=1e-9, preconditioner=H.PRECOND_AMG)
+assert all(s.converged for s in stats)
+np.savez(sys.argv[2], its=np.array([s.iterations for s in stats]),
+         **{f"u{k}": np.concatenate([np.ravel(a) for a in sol]) for k, sol in enumerate(B.solutions())})
+"""
+
+
+def test_multigrid_cycle_variants_are_bit_identical(tmp_path):
+    """The V-cycle's launch shapes that the autotuner chooses between give the same bits: the
+    coarse levels cycled by one k_amg_tail launch per V-cycle (one CTA per problem) or by one launch
+    per kernel per level (HDG_AMG_TAIL_ROWS), and the level-0 smoother with a thread per face or per
+    row (HDG_AMG_SWEEP); the tuned default too."""
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    script = tmp_path / "cycle.py"
+    script.write_text(_TAIL_SCRIPT)
+    out = {}
+    for name, env_add in (("plain", {"HDG_AMG_TAIL_ROWS": "0", "HDG_AMG_SWEEP": "face"}),
+                          ("tail", {"HDG_AMG_TAIL_ROWS": "1024", "HDG_AMG_SWEEP": "row"}),
+                          ("tuned", {})):
+        env = dict(os.environ, HDG_AMG_VERBOSE="1", **env_add)
+        for k in ("HDG_AMG_TAIL_ROWS", "HDG_AMG_SWEEP"):
+            if k not in env_add:
+                env.pop(k, None)
+        r = subprocess.run([sys.executable, str(script), root, str(tmp_path / f"{name}.npz")], env=env,
+                           capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr[-2000:]
+        out[name] = (np.load(tmp_path / f"{name}.npz"), r.stderr)
+    assert "tail from level 0" in out["plain"][1]
+    assert "tail from level 2" in out["tail"][1] or "tail from level 3" in out["tail"][1], out["tail"][1][-1000:]
+    assert "amg tune:" in out["tuned"][1]
+    a = out["plain"][0]
+    for name in ("tail", "tuned"):
+        b = out[name][0]
+        np.testing.assert_array_equal(a["its"], b["its"])
+        for k in a.files:
+            assert a[k].tobytes() == b[k].tobytes(), (name, k)
