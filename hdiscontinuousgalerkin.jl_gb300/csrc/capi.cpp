@@ -44,6 +44,7 @@ void set_device(hdg_ctx* ctx) {
 
 thread_local cudaStream_t g_alloc_stream = nullptr;
 thread_local cudaStream_t g_use_stream = nullptr;
+thread_local bool g_tuning_allowed = true;
 
 void order_streams(cudaStream_t before, cudaStream_t after) {
   cudaEvent_t e;
@@ -430,6 +431,7 @@ static int assemble_condense_impl(hdg_space* space, double tau, const hdg_field*
       s->ctx = ctx;
       s->precision = precision;
       s->he_tau = space->he_tau;
+      s->amg_tune_time = g_tuning_allowed;
       const RefTables& t = space->t;
       s->nw = t.nw;
       s->nt = t.nt;

@@ -548,10 +548,14 @@ template <int P> bool launch_cfg(hdg_system* s, cudaStream_t st, const ElemArgs&
 }
 
 // Autotuner: the first launch for a (device, degree, quadrature size, log2 of the cell count, path)
-// times every (warps per CTA, grid oversubscription) pair on the real inputs (the kernel only
-// writes its outputs from its inputs, and every configuration computes each cell with the same
-// instruction sequence, so the results are bit-identical) and keeps the fastest.  The choice is
-// cached for the process.  HDG_ELEMENT_WARPS=<1|2|4|8|16> fixes the warps per CTA instead.
+// times every (warps per CTA, grid oversubscription) pair on the real inputs, on at most the first
+// 65536 cells (the kernel only writes its outputs from its inputs, and every configuration
+// computes each cell with the same instruction sequence, so the results are bit-identical; the
+// real launch that follows writes every cell), and keeps the fastest.  The choice is cached for
+// the process.  On a thread that builds one-shot systems (g_tuning_allowed false) a key without a
+// cached choice takes the cached choice of the nearest cell count for the same degree, quadrature
+// and path, and is timed only when there is none.  HDG_ELEMENT_WARPS=<1|2|4|8|16> fixes the warps
+// per CTA instead.
 template <int P> void launch_p(hdg_system* s, cudaStream_t st, const ElemArgs& a) {
   static std::mutex mu;
   static std::map<std::tuple<int, int, int, int>, std::pair<int, int>> best;
@@ -565,6 +569,18 @@ template <int P> void launch_p(hdg_system* s, cudaStream_t st, const ElemArgs& a
   {
     std::lock_guard<std::mutex> lk(mu);
     auto it = best.find(key);
+    if (it == best.end() && !g_tuning_allowed) {  // nearest cached cell count, same degree and path
+      int dist = 1 << 30;
+      for (auto jt = best.begin(); jt != best.end(); ++jt) {
+        const auto& k = jt->first;
+        if (std::get<0>(k) != std::get<0>(key) || std::get<1>(k) != a.nq || std::get<3>(k) != a.schur) continue;
+        const int d = std::abs(std::get<2>(k) - lg);
+        if (d < dist) {
+          dist = d;
+          it = jt;
+        }
+      }
+    }
     if (it != best.end()) {
       launch_cfg<P>(s, st, a, it->second.first, it->second.second);
       return;
@@ -575,11 +591,13 @@ template <int P> void launch_p(hdg_system* s, cudaStream_t st, const ElemArgs& a
   cudaEvent_t e0, e1;
   HDG_CUDA(cudaEventCreate(&e0));
   HDG_CUDA(cudaEventCreate(&e1));
+  ElemArgs t = a;  // the trials run on a prefix of the cells
+  t.nc = std::min(a.nc, 65536);
   for (int w : {1, 2, 4, 8, 16})
     for (int g : {1, 4}) {
-      if (!launch_cfg<P>(s, st, a, w, g)) continue;  // warm-up launch of this configuration
+      if (!launch_cfg<P>(s, st, t, w, g)) continue;  // warm-up launch of this configuration
       HDG_CUDA(cudaEventRecord(e0, st));
-      launch_cfg<P>(s, st, a, w, g);
+      launch_cfg<P>(s, st, t, w, g);
       HDG_CUDA(cudaEventRecord(e1, st));
       HDG_CUDA(cudaEventSynchronize(e1));
       float ms = 0.f;

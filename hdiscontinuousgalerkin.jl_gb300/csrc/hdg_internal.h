@@ -34,6 +34,10 @@ extern thread_local cudaStream_t g_alloc_stream;
 // Stream that will use buffers allocated now, when it is not the allocation stream (a forked
 // stream of a pipelined batch step): a new allocation is ordered before that stream's later work.
 extern thread_local cudaStream_t g_use_stream;
+// The launch autotuners (element kernel, V-cycle) may time candidate configurations on this
+// thread.  Threads that build one-shot systems (the serving engine's flight builders) clear it:
+// they then take the nearest cached choice, and time candidates only when nothing is cached.
+extern thread_local bool g_tuning_allowed;
 void order_streams(cudaStream_t before, cudaStream_t after);  // `after` waits for `before`'s work so far
 template <class T> struct DevBuf {
   T* p = nullptr;

@@ -254,7 +254,6 @@ Flight* launch_flight(hdg_engine* e, std::vector<Request>&& reqs, int slot) {
   t0 = now_s();
   fl->t[3] += t0 - t1;
   g_alloc_stream = c->stream;
-  fl->sys->amg_tune_time = false;  // a flight is solved once: no timing of V-cycle variants
   fl->cg = make_cg_solver(fl->sys);
   fl->cg->prepare(e->solver);
   HDG_CUDA(cudaEventCreateWithFlags(&fl->ready, cudaEventDisableTiming));
@@ -319,6 +318,7 @@ void start_resident(hdg_engine* e, ResidentSys* rs, Request&& r) {
 // Worker thread: builds flights from the job queue until the engine stops.
 void builder_main(hdg_engine* e) {
   cudaSetDevice(e->ctx->device);
+  g_tuning_allowed = false;  // flights are solved once: autotuners take cached choices here
   for (;;) {
     hdg_engine::Job job;
     {
