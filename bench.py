@@ -886,8 +886,10 @@ def parse():
                     help="c5 only: mean arrival rate in requests/s (2000 is the workload; lower rates show latency "
                          "without queueing)")
     ap.add_argument("--hbm-budget-gb", type=float, default=64.0)
-    ap.add_argument("--max-batch", type=int, default=64)
-    ap.add_argument("--max-flights", type=int, default=8)
+    ap.add_argument("--max-batch", type=int, default=32,
+                    help="serving: requests per flight (measured on the 2000 req/s stream: flights x batch 8x64 831, "
+                         "12x64 901, 16x64 904, 16x32 964, 16x24 947, 24x32 915, 32x16 879 completed/s)")
+    ap.add_argument("--max-flights", type=int, default=16, help="serving: flights in progress at once")
     ap.add_argument("--precision", default=None, choices=["fp64", "mixed"],
                     help="default: mixed for the batched and served workloads (c3, c4, c5), fp64 for c1, c2")
     ap.add_argument("--tol", type=float, default=1e-12)

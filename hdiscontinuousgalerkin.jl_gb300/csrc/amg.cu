@@ -43,6 +43,7 @@
 #include <mutex>
 #include <tuple>
 #include <numeric>
+#include <thread>
 
 #include <cuda_fp16.h>
 
@@ -87,6 +88,56 @@ int amg_sweep_forced() {
     return -1;
   }();
   return v;
+}
+
+// ---- host parallelism of the symbolic set-up ------------------------------------------------
+// Rows of the set-up's per-row loops are independent; they run on up to 4 threads in contiguous
+// ranges (the calling thread takes the first), and every range's output is concatenated in row
+// order, so the hierarchy is the same as one built on one thread.
+int set_up_ranges(int64_t n, int64_t grain = 16384) {
+  static const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+  return (int)std::max<int64_t>(1, std::min<int64_t>(std::min(hw, 4), n / grain));
+}
+template <class F> void run_ranges(int64_t n, int k, F fn) {  // fn(range, begin, end)
+  if (k <= 1) {
+    fn(0, (int64_t)0, n);
+    return;
+  }
+  std::vector<std::thread> ts;
+  for (int t = 1; t < k; ++t) ts.emplace_back(fn, t, n * t / k, n * (t + 1) / k);
+  fn(0, (int64_t)0, n / k);
+  for (auto& t : ts) t.join();
+}
+// CSR rows [0, nr): rowfn(r, mark, out) appends the candidate columns of row r, using mark (one
+// int per column, private to the range) to skip repeats within the row; each row's columns are
+// then sorted.
+template <class RowFn>
+void build_csr(int nr, int ncol, RowFn rowfn, std::vector<int32_t>* ptr, std::vector<int32_t>* col) {
+  const int k = set_up_ranges(nr);
+  std::vector<std::vector<int32_t>> lc(k), lp(k);
+  run_ranges(nr, k, [&](int t, int64_t a, int64_t b) {
+    std::vector<int32_t> mark((size_t)std::max(ncol, 1), -1);
+    std::vector<int32_t>& c = lc[t];
+    std::vector<int32_t>& p = lp[t];
+    p.reserve((size_t)(b - a));
+    for (int64_t r = a; r < b; ++r) {
+      const size_t start = c.size();
+      rowfn((int)r, mark, c);
+      std::sort(c.begin() + start, c.end());
+      p.push_back((int32_t)c.size());
+    }
+  });
+  ptr->assign((size_t)nr + 1, 0);
+  size_t tot = 0;
+  for (int t = 0; t < k; ++t) tot += lc[t].size();
+  col->clear();
+  col->reserve(tot);
+  int64_t r = 0;
+  for (int t = 0; t < k; ++t) {
+    const int32_t off = (int32_t)col->size();
+    for (int32_t e : lp[t]) (*ptr)[(size_t)++r] = off + e;
+    col->insert(col->end(), lc[t].begin(), lc[t].end());
+  }
 }
 
 // Greedy aggregation on an adjacency graph (CSR, symmetric, no self loops needed):
@@ -345,31 +396,33 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
     d_m0.download(m0.data(), m0.size(), st);
     HDG_CUDA(cudaStreamSynchronize(st));
     std::vector<double> dg(nf, 0.0);
-    for (int f = 0; f < nf; ++f)
-      for (int k = 0; k < 5; ++k)
-        if (bcol5[(size_t)k * nf + f] == f) dg[f] = std::max(dg[f], std::fabs(m0[(size_t)k * nf + f]));
-    // strong neighbours in a fixed-width table (at most 4 slots each way), then compacted to CSR
-    constexpr int SW = 8;
-    std::vector<int32_t> tab((size_t)nf * SW);
-    std::vector<uint8_t> cnt(nf, 0);
-    for (int f = 0; f < nf; ++f)
-      for (int k = 0; k < 5; ++k) {
-        const int g = bcol5[(size_t)k * nf + f];
-        if (g == f) continue;
-        if (std::fabs(m0[(size_t)k * nf + f]) >= theta * std::sqrt(dg[f] * dg[g])) {
-          if (cnt[f] < SW) tab[(size_t)f * SW + cnt[f]++] = g;
-          if (cnt[g] < SW) tab[(size_t)g * SW + cnt[g]++] = f;  // symmetric closure
-        }
-      }
-    sadj.clear();
-    sadj.reserve((size_t)nf * 4);
-    for (int f = 0; f < nf; ++f) {
-      int32_t* v = &tab[(size_t)f * SW];
-      std::sort(v, v + cnt[f]);
-      const int n = (int)(std::unique(v, v + cnt[f]) - v);
-      sadj.insert(sadj.end(), v, v + n);
-      sptr[f + 1] = (int32_t)sadj.size();
-    }
+    run_ranges(nf, set_up_ranges(nf), [&](int, int64_t a, int64_t b) {
+      for (int64_t f = a; f < b; ++f)
+        for (int k = 0; k < 5; ++k)
+          if (bcol5[(size_t)k * nf + f] == f) dg[f] = std::max(dg[f], std::fabs(m0[(size_t)k * nf + f]));
+    });
+    // g is a strong neighbour of f when the coupling is strong in f's row or in g's (symmetric
+    // closure); each face's row is formed from the two rows alone
+    auto strong = [&](int f, int k) {
+      const int g = bcol5[(size_t)k * nf + f];
+      return std::fabs(m0[(size_t)k * nf + f]) >= theta * std::sqrt(dg[f] * dg[g]);
+    };
+    build_csr(
+        nf, nf,
+        [&](int f, std::vector<int32_t>& mark, std::vector<int32_t>& out) {
+          for (int k = 0; k < 5; ++k) {
+            const int g = bcol5[(size_t)k * nf + f];
+            if (g == f || mark[g] == f) continue;
+            bool st_ = strong(f, k);
+            for (int kk = 0; kk < 5 && !st_; ++kk)
+              if (bcol5[(size_t)kk * nf + g] == f) st_ = strong(g, kk);
+            if (st_) {
+              mark[g] = f;
+              out.push_back(g);
+            }
+          }
+        },
+        &sptr, &sadj);
   }
   tph[1] = clk();
   std::vector<int32_t> agg0;
@@ -383,51 +436,59 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
     if (agg0[f] >= 0) tent0[f] = (float)(1.0 / std::sqrt((double)size0[agg0[f]]));
   // P0 pattern per face: aggregates of the face and its neighbours (active only)
   std::vector<int32_t> pcol0((size_t)nf * PW, -1);
-  for (int f = 0; f < nf; ++f) {
-    if (!active[f]) continue;
-    int cols[8], nc = 0;
-    cols[nc++] = agg0[f];
-    for (int e = fptr[f]; e < fptr[f + 1]; ++e)
-      if (agg0[fadj[e]] >= 0) cols[nc++] = agg0[fadj[e]];
-    std::sort(cols, cols + nc);
-    nc = (int)(std::unique(cols, cols + nc) - cols);
-    for (int c = 0; c < nc && c < PW; ++c) pcol0[(size_t)f * PW + c] = cols[c];
-  }
+  const int kf = set_up_ranges(nf);
+  run_ranges(nf, kf, [&](int, int64_t a, int64_t b) {
+    for (int64_t f = a; f < b; ++f) {
+      if (!active[f]) continue;
+      int cols[8], nc = 0;
+      cols[nc++] = agg0[f];
+      for (int e = fptr[f]; e < fptr[f + 1]; ++e)
+        if (agg0[fadj[e]] >= 0) cols[nc++] = agg0[fadj[e]];
+      std::sort(cols, cols + nc);
+      nc = (int)(std::unique(cols, cols + nc) - cols);
+      for (int c = 0; c < nc && c < PW; ++c) pcol0[(size_t)f * PW + c] = cols[c];
+    }
+  });
   // A0 P0 pattern per face: union over the 5 slot faces of their P0 columns
   // (at most 5 slots x PW columns = 25 entries per face, kept in a fixed-width table)
   constexpr int APW = 5 * PW;
   std::vector<int32_t> apc((size_t)nf * APW);
   std::vector<uint8_t> apn(nf);
-  int wap = 1;
-  for (int f = 0; f < nf; ++f) {
-    int32_t* v = &apc[(size_t)f * APW];
-    int n = 0;
-    for (int k = 0; k < 5; ++k) {
-      const int g = bcol5[(size_t)k * nf + f];
-      for (int c = 0; c < PW; ++c)
-        if (pcol0[(size_t)g * PW + c] >= 0) v[n++] = pcol0[(size_t)g * PW + c];
+  std::vector<int> wapr(kf, 1);
+  run_ranges(nf, kf, [&](int t, int64_t a, int64_t b) {
+    for (int64_t f = a; f < b; ++f) {
+      int32_t* v = &apc[(size_t)f * APW];
+      int n = 0;
+      for (int k = 0; k < 5; ++k) {
+        const int g = bcol5[(size_t)k * nf + f];
+        for (int c = 0; c < PW; ++c)
+          if (pcol0[(size_t)g * PW + c] >= 0) v[n++] = pcol0[(size_t)g * PW + c];
+      }
+      std::sort(v, v + n);
+      n = (int)(std::unique(v, v + n) - v);
+      apn[f] = (uint8_t)n;
+      wapr[t] = std::max(wapr[t], n);
     }
-    std::sort(v, v + n);
-    n = (int)(std::unique(v, v + n) - v);
-    apn[f] = (uint8_t)n;
-    wap = std::max(wap, n);
-  }
+  });
+  const int wap = *std::max_element(wapr.begin(), wapr.end());
   if (wap > 32) throw HdgError{HDG_ERR_ARG, "AMG: prolongator pattern wider than 32 (invalid trace mesh)"};
   std::vector<int32_t> apcol0((size_t)nf * wap, -1);
   std::vector<int8_t> apmap0((size_t)nf * 5 * PW, -1);
-  for (int f = 0; f < nf; ++f) {
-    const int32_t* v = &apc[(size_t)f * APW];
-    const int n = apn[f];
-    std::copy(v, v + n, apcol0.begin() + (size_t)f * wap);
-    for (int k = 0; k < 5; ++k) {
-      const int g = bcol5[(size_t)k * nf + f];
-      for (int c = 0; c < PW; ++c) {
-        const int J = pcol0[(size_t)g * PW + c];
-        if (J < 0) continue;
-        apmap0[((size_t)f * 5 + k) * PW + c] = (int8_t)(std::lower_bound(v, v + n, J) - v);
+  run_ranges(nf, kf, [&](int, int64_t a, int64_t b) {
+    for (int64_t f = a; f < b; ++f) {
+      const int32_t* v = &apc[(size_t)f * APW];
+      const int n = apn[f];
+      std::copy(v, v + n, apcol0.begin() + (size_t)f * wap);
+      for (int k = 0; k < 5; ++k) {
+        const int g = bcol5[(size_t)k * nf + f];
+        for (int c = 0; c < PW; ++c) {
+          const int J = pcol0[(size_t)g * PW + c];
+          if (J < 0) continue;
+          apmap0[((size_t)f * 5 + k) * PW + c] = (int8_t)(std::lower_bound(v, v + n, J) - v);
+        }
       }
     }
-  }
+  });
   tph[3] = clk();
   // P0' lists and the level-1 pattern (rows = aggregates)
   std::vector<int32_t> rptr0, rent0;  // entries f * PW + c of P0 per column, in entry order
@@ -437,27 +498,24 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
   L1.h_ptr.assign(na0 + 1, 0);
   L1.h_prob.assign(na0, 0);
   L1.h_B.assign(na0, 0.0);
-  std::vector<int32_t> cols;
   // column unions below use a stamp per column (the row that last added it): each candidate is
   // looked at once, and only the distinct columns of a row are sorted
-  std::vector<int32_t> mark((size_t)na0, -1);
-  for (int J = 0; J < na0; ++J) {
-    cols.clear();
-    for (int t = rptr0[J]; t < rptr0[J + 1]; ++t) {
-      const int f = rent0[t] / PW;
-      for (int q = 0; q < apn[f]; ++q) {
-        const int32_t c = apc[(size_t)f * APW + q];
-        if (mark[c] != J) {
-          mark[c] = J;
-          cols.push_back(c);
+  build_csr(
+      na0, na0,
+      [&](int J, std::vector<int32_t>& mark, std::vector<int32_t>& out) {
+        for (int t = rptr0[J]; t < rptr0[J + 1]; ++t) {
+          const int f = rent0[t] / PW;
+          for (int q = 0; q < apn[f]; ++q) {
+            const int32_t c = apc[(size_t)f * APW + q];
+            if (mark[c] != J) {
+              mark[c] = J;
+              out.push_back(c);
+            }
+          }
         }
-      }
-    }
-    std::sort(cols.begin(), cols.end());
-    L1.h_col.insert(L1.h_col.end(), cols.begin(), cols.end());
-    L1.h_ptr[J + 1] = (int32_t)L1.h_col.size();
-    L1.h_B[J] = std::sqrt((double)size0[J]);
-  }
+      },
+      &L1.h_ptr, &L1.h_col);
+  for (int J = 0; J < na0; ++J) L1.h_B[J] = std::sqrt((double)size0[J]);
   for (int f = 0; f < nf; ++f)
     if (agg0[f] >= 0) L1.h_prob[agg0[f]] = fprob[f];
   tph[4] = clk();
@@ -504,35 +562,31 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
     for (int J = 0; J < na; ++J) nrm[J] = std::sqrt(nrm[J]);
     std::vector<float> tent(n);
     for (int i = 0; i < n; ++i) tent[i] = nrm[agg[i]] > 0 ? (float)(F.h_B[i] / nrm[agg[i]]) : 0.f;
-    // P pattern row i: aggregates of the columns of A row i
-    std::vector<int32_t> pptr(n + 1, 0), pcol, v;
-    std::vector<int32_t> cmark((size_t)na, -1);
-    auto add = [&](int32_t c, int32_t row) {
-      if (cmark[c] != row) {
-        cmark[c] = row;
-        v.push_back(c);
+    auto add = [](std::vector<int32_t>& mark, std::vector<int32_t>& out, int32_t c, int32_t row) {
+      if (mark[c] != row) {
+        mark[c] = row;
+        out.push_back(c);
       }
     };
-    for (int i = 0; i < n; ++i) {
-      v.clear();
-      for (int e = F.h_ptr[i]; e < F.h_ptr[i + 1]; ++e) add(agg[F.h_col[e]], i);
-      std::sort(v.begin(), v.end());
-      pcol.insert(pcol.end(), v.begin(), v.end());
-      pptr[i + 1] = (int32_t)pcol.size();
-    }
+    // P pattern row i: aggregates of the columns of A row i
+    std::vector<int32_t> pptr, pcol;
+    build_csr(
+        n, na,
+        [&](int i, std::vector<int32_t>& mark, std::vector<int32_t>& out) {
+          for (int e = F.h_ptr[i]; e < F.h_ptr[i + 1]; ++e) add(mark, out, agg[F.h_col[e]], i);
+        },
+        &pptr, &pcol);
     // A P pattern row i: union of the P rows of A row i's columns
-    std::vector<int32_t> apptr(n + 1, 0), apcol;
-    std::fill(cmark.begin(), cmark.end(), -1);
-    for (int i = 0; i < n; ++i) {
-      v.clear();
-      for (int e = F.h_ptr[i]; e < F.h_ptr[i + 1]; ++e) {
-        const int k = F.h_col[e];
-        for (int q = pptr[k]; q < pptr[k + 1]; ++q) add(pcol[q], i);
-      }
-      std::sort(v.begin(), v.end());
-      apcol.insert(apcol.end(), v.begin(), v.end());
-      apptr[i + 1] = (int32_t)apcol.size();
-    }
+    std::vector<int32_t> apptr, apcol;
+    build_csr(
+        n, na,
+        [&](int i, std::vector<int32_t>& mark, std::vector<int32_t>& out) {
+          for (int e = F.h_ptr[i]; e < F.h_ptr[i + 1]; ++e) {
+            const int k = F.h_col[e];
+            for (int q = pptr[k]; q < pptr[k + 1]; ++q) add(mark, out, pcol[q], i);
+          }
+        },
+        &apptr, &apcol);
     // P' lists and the next level's pattern
     std::vector<int32_t> prow_of(pcol.size());
     for (int i = 0; i < n; ++i)
@@ -543,26 +597,17 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
     for (size_t t = 0; t < rent.size(); ++t) rrow[t] = prow_of[rent[t]];
     AmgLevel C;
     C.n = na;
-    C.h_ptr.assign(na + 1, 0);
     C.h_prob.assign(na, 0);
     C.h_B = nrm;
-    std::fill(cmark.begin(), cmark.end(), -1);
-    for (int J = 0; J < na; ++J) {
-      cols.clear();
-      for (int t = rptr[J]; t < rptr[J + 1]; ++t) {
-        const int i = rrow[t];
-        for (int q = apptr[i]; q < apptr[i + 1]; ++q) {
-          const int32_t c = apcol[q];
-          if (cmark[c] != J) {
-            cmark[c] = J;
-            cols.push_back(c);
+    build_csr(
+        na, na,
+        [&](int J, std::vector<int32_t>& mark, std::vector<int32_t>& out) {
+          for (int t = rptr[J]; t < rptr[J + 1]; ++t) {
+            const int i = rrow[t];
+            for (int q = apptr[i]; q < apptr[i + 1]; ++q) add(mark, out, apcol[q], J);
           }
-        }
-      }
-      std::sort(cols.begin(), cols.end());
-      C.h_col.insert(C.h_col.end(), cols.begin(), cols.end());
-      C.h_ptr[J + 1] = (int32_t)C.h_col.size();
-    }
+        },
+        &C.h_ptr, &C.h_col);
     for (int i = 0; i < n; ++i) C.h_prob[agg[i]] = F.h_prob[i];
     F.nc = na;
     F.agg.upload(agg.data(), agg.size(), st);
