@@ -315,7 +315,7 @@ struct AmgHierarchy {
   int tail_from = -1;        // first level (index into lev) cycled by k_amg_tail; -1: none
   std::vector<int> tail_cands; // levels the tail may start at (problems' rows <= AMG_TAIL_MAXROWS)
   DevBuf<TailLevel> tail_tab;  // every level's arrays for k_amg_tail
-  bool row_sweep = false;    // level-0 smoother: a thread per row (else per face)
+  bool row_sweep = false;    // level-0 smoother, residual and prolongation: a thread per row (else per face)
   bool tuned = false;        // the V-cycle autotuner has run (or its choice was taken from its cache)
   bool built = false;
 };
@@ -1222,6 +1222,33 @@ __global__ void k_amg_face_residual(int nf, const int32_t* __restrict__ bcol5, c
   r[row] = s;
 }
 
+// The same residual with a thread per face (its nt rows): the face's block columns and neighbour
+// values are read once instead of nt times; each row's operations are those of the row kernel.
+template <int NT, typename VT>
+__global__ void k_amg_face_residual_f(int nf, const int32_t* __restrict__ bcol5, const VT* __restrict__ val,
+                                      const float* __restrict__ b, const float* __restrict__ x,
+                                      float* __restrict__ r, const int32_t* __restrict__ face_prob,
+                                      const int32_t* __restrict__ st) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf || !amg_live(st, face_prob[f])) return;
+  const int64_t nd = (int64_t)nf * NT;
+  float s[NT];
+#pragma unroll
+  for (int i = 0; i < NT; ++i) s[i] = b[(int64_t)f * NT + i];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const int g = bcol5[k * nf + f];
+#pragma unroll
+    for (int j = 0; j < NT; ++j) {
+      const float xv = x[(int64_t)g * NT + j];
+#pragma unroll
+      for (int i = 0; i < NT; ++i) s[i] -= ldv(&val[(k * NT + j) * nd + (int64_t)f * NT + i]) * xv;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < NT; ++i) r[(int64_t)f * NT + i] = s[i];
+}
+
 // b1 = P0' r0 = (D P0)' r~0 and the first l1-Jacobi sweep of level 1: x1 = b1 / dl1
 template <int NT>
 __global__ void k_amg_restrict0(int na, const int32_t* __restrict__ rptr0, const int32_t* __restrict__ rent0,
@@ -1255,6 +1282,34 @@ __global__ void k_amg_prolong0(int nf, const int32_t* __restrict__ pcol0, const 
     s += pval0[row * PW + c] * x1[J];
   }
   x0[row] += s;
+}
+
+// The same prolongation with a thread per face: the face's prolongator columns and coarse values
+// are read once for its nt rows; each row's operations are those of the row kernel.
+template <int NT>
+__global__ void k_amg_prolong0_f(int nf, const int32_t* __restrict__ pcol0, const float* __restrict__ pval0,
+                                 const float* __restrict__ x1, float* __restrict__ x0,
+                                 const int32_t* __restrict__ face_prob, const int32_t* __restrict__ st) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf || !amg_live(st, face_prob[f])) return;
+  float xv[PW];
+  int nc = 0;
+#pragma unroll
+  for (int c = 0; c < PW; ++c) {
+    const int J = pcol0[f * PW + c];
+    if (J < 0) break;
+    xv[c] = x1[J];
+    nc = c + 1;
+  }
+#pragma unroll
+  for (int i = 0; i < NT; ++i) {
+    const int64_t row = (int64_t)f * NT + i;
+    float s = 0.f;
+#pragma unroll
+    for (int c = 0; c < PW; ++c)
+      if (c < nc) s += pval0[row * PW + c] * xv[c];
+    x0[row] += s;
+  }
 }
 
 // Coarse-level kernels: G lanes per row (G a power of two <= 32).  The lanes of a group take a
@@ -1651,8 +1706,12 @@ void apply_nt(hdg_system* s, const VT* val0, const float* b0, float* z0, const i
     const float* in = (t == 0) ? nullptr : (out == z0 ? H->x0.p : z0);
     cheb_sweep<NT, VT>(s, val0, b0, in, out, t, cst, st);
   }
-  k_amg_face_residual<NT, VT><<<nblk(n0), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->bt0.p, z0, H->r0.p, H->face_prob.p,
-                                                    cst);
+  if (H->row_sweep)
+    k_amg_face_residual<NT, VT><<<nblk(n0), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->bt0.p, z0, H->r0.p,
+                                                          H->face_prob.p, cst);
+  else
+    k_amg_face_residual_f<NT, VT><<<nblk(nf), 256, 0, st>>>(nf, s->d_bcol5.p, val0, H->bt0.p, z0, H->r0.p,
+                                                            H->face_prob.p, cst);
   AmgLevel& L1 = H->lev[0];
   k_amg_restrict0<NT><<<nblk(L1.n), 256, 0, st>>>(L1.n, H->rptr0.p, H->rent0.p, H->dpval0.p, H->r0.p, L1.dl1inv.p,
                                                   L1.b.p, L1.x.p, L1.prob.p, cst);
@@ -1709,7 +1768,10 @@ void apply_nt(hdg_system* s, const VT* val0, const float* b0, float* z0, const i
   }
   // level 0 up: prolongate, then the same Chebyshev polynomial from the corrected iterate (z0,
   // x0, z0, ...); for odd k the result lands in x0 and is copied to z0
-  k_amg_prolong0<NT><<<nblk(n0), 256, 0, st>>>(nf, H->pcol0.p, H->pval0.p, fin[0], z0, H->face_prob.p, cst);
+  if (H->row_sweep)
+    k_amg_prolong0<NT><<<nblk(n0), 256, 0, st>>>(nf, H->pcol0.p, H->pval0.p, fin[0], z0, H->face_prob.p, cst);
+  else
+    k_amg_prolong0_f<NT><<<nblk(nf), 256, 0, st>>>(nf, H->pcol0.p, H->pval0.p, fin[0], z0, H->face_prob.p, cst);
   for (int t = 0; t < k; ++t) {
     const float* in = (t % 2 == 0) ? z0 : H->x0.p;
     float* out = (t % 2 == 0) ? H->x0.p : z0;
