@@ -18,7 +18,7 @@ from .fields import as_field
 
 
 class Engine:
-    def __init__(self, ctx, hbm_budget_gb=32.0, max_batch=64, max_flights=8, tol=1e-10,
+    def __init__(self, ctx, hbm_budget_gb=32.0, max_batch=32, max_flights=16, tol=1e-10,
                  precision=L.PREC_MIXED, chunk=32, maxit=100000, keep_results=True, preconditioner=L.PRECOND_JACOBI):
         self.ctx = ctx
         o = L.hdg_solver(float(tol), int(maxit), int(precision), int(chunk), 1e-5, int(preconditioner))

@@ -337,7 +337,11 @@ int hdg_lagrange_destroy(hdg_lagrange* sys);
  * requests into "flights" (one disjoint union system per degree, at most max_batch requests)
  * while the HBM budget and the flight slots allow, advances every flight by one chunk of CG
  * iterations on its own CUDA stream, and completes the flights whose problems are all done.
- * Requests arriving while others run join at the next step; flights overlap on the device. */
+ * Requests arriving while others run join at the next step; flights overlap on the device.
+ * Flights are built on HDG_ENGINE_BUILDERS worker threads (default 8); their launch autotuners
+ * take cached choices instead of timing.  Measured on a 2000 req/s stream of problems of 130 to
+ * 33000 cells: 16 flights of at most 32 requests served the most (965 requests/s), against 831
+ * for 8 flights of 64. */
 typedef struct hdg_engine hdg_engine;
 int hdg_engine_create(hdg_ctx* ctx, double hbm_budget_gb, int max_batch, int max_flights, const hdg_solver* opts,
                       hdg_engine** out);
