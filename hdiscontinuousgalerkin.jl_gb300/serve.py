@@ -1,6 +1,6 @@
 """Serving: continuous batching of HDG solve requests (hdg_engine_* in libhdg).
 
-    eng = Engine(ctx, hbm_budget_gb=32, max_batch=64, max_flights=8, tol=1e-10)
+    eng = Engine(ctx, hbm_budget_gb=32, max_batch=32, max_flights=16, tol=1e-10)
     mid = eng.add_resident(host_mesh, p)              # meshes kept on the engine
     rid = eng.submit(p, f, kappa_cell, mesh_id=mid)   # or mesh=<host mesh> for a new mesh
     while busy: eng.step(); done = eng.poll()          # admit / advance / complete
