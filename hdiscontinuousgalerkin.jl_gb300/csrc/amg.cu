@@ -1556,15 +1556,20 @@ inline unsigned nblk(int64_t n, int t = 256) { return (unsigned)std::max<int64_t
 // On the 131072-cell p=2 problem with kappa = 1, degree 2 was 5 % faster than 3 (103 vs 99
 // iterations).
 // l1-Jacobi sweeps before and after the coarse correction on each coarse level
-// (HDG_AMG_COARSE_SWEEPS, 1..4, default 2).  On the 256-problem batch 1/2/3 sweeps gave
-// 406/418/415 solves/s (396/359/349 iterations for the hardest problem).
-int amg_coarse_sweeps() {
-  static const int k = [] {
+// (HDG_AMG_COARSE_SWEEPS=1..8 sets one value for all).  With the strength-of-connection
+// aggregates, on the 256-problem batch (kappa per cell over four decades) 1/2/3/4 sweeps gave
+// 972/1068/1112-1121/1137 solves/s (mean CG iterations 98/80/72/67); on 2*256^2 cells, p = 2,
+// kappa = 1, 2/3/4 gave 43.6/43.0/41.6 solves/s (103/95/89 iterations); the request stream was
+// within 1.5 % for 2-4.  So 4 for systems with a variable kappa (per cell or a field), 2 for a
+// constant one.
+int amg_coarse_sweeps(const hdg_system* s) {
+  static const int env = [] {
     const char* e = std::getenv("HDG_AMG_COARSE_SWEEPS");
-    const int v = e ? std::atoi(e) : 2;
-    return (v >= 1 && v <= 4) ? v : 2;
+    const int v = e ? std::atoi(e) : 0;
+    return (v >= 1 && v <= 8) ? v : 0;
   }();
-  return k;
+  if (env > 0) return env;
+  return (s->kappa_cells || s->kappa_field) ? 4 : 2;
 }
 
 // Storage of the scaled level-0 matrix that the cycle reads: FP16 (default; half the bytes of
@@ -1717,7 +1722,7 @@ void apply_nt(hdg_system* s, const VT* val0, const float* b0, float* z0, const i
                                                   L1.b.p, L1.x.p, L1.prob.p, cst);
   // coarse levels down: x holds the first l1-Jacobi sweep (done by the restriction); the other
   // nu - 1 sweeps alternate between x and t; the iterate then stays where it is until the way up
-  const int nu = amg_coarse_sweeps();
+  const int nu = amg_coarse_sweeps(s);
   float* iter[AMG_MAX_LEVELS];
   float* fin[AMG_MAX_LEVELS];
   // levels from T on (the coarsest included) are cycled by one k_amg_tail launch
@@ -1825,7 +1830,7 @@ double amg_cycle_bytes(const hdg_system* s) {
       break;
     }
     const double npc = (double)H->lev[l].h_col.size();      // P and P' sizes are comparable to A's
-    b += (2 * amg_coarse_sweeps() - 1) * (spmv + 20.0 * n) + (spmv + 16.0 * n);  // sweeps, one residual
+    b += (2 * amg_coarse_sweeps(s) - 1) * (spmv + 20.0 * n) + (spmv + 16.0 * n);  // sweeps, one residual
     b += 2.0 * (8.0 * npc + 12.0 * n);                      // restriction and prolongation
   }
   return b;
@@ -1843,7 +1848,7 @@ double amg_cheb0_bytes_per_row(const hdg_system* s) {
 }
 
 int amg_cycle_launches(const hdg_system* s) {
-  const int nl = (int)s->amg->lev.size(), k = amg_cheb_degree(), nu = amg_coarse_sweeps();
+  const int nl = (int)s->amg->lev.size(), k = amg_cheb_degree(), nu = amg_coarse_sweeps(s);
   // level 0 down, coarse levels down, coarsest, coarse levels up, level 0 up (the D2D copy of an
   // odd degree is no kernel); levels from the tail's first on are one launch
   const int T = s->amg->tail_from >= 0 ? s->amg->tail_from : nl - 1;
