@@ -184,9 +184,9 @@ def element_cost(p, schur):
 
 def c4_rooflines(H, B, tims, pc, hbm, peak_kind):
     """The dominant kernel of the timed batch step and the element kernels.  The dominant kernel is
-    the instance of the largest kernel family of the step's launch list (the level-0 sweeps with the
-    multigrid) that moves the most algorithmic bytes per step (bytes per launch x launches): a
-    choice that does not depend on timing noise between the concurrent bins."""
+    the instance that moves the most algorithmic bytes per step (bytes per launch x launches) in the
+    kernel family with the most live time per step (mean event-timed launch x launches, summed over
+    the bins): level-0 sweeps, first-coarse-level sweeps or FP64 products."""
     k = 2  # Chebyshev degree of the level-0 smoother: 2k sweeps per V-cycle
     chunk = 8
     cand = []
@@ -198,18 +198,34 @@ def c4_rooflines(H, B, tims, pc, hbm, peak_kind):
             smp = bn.kernel_sample(1)
             if smp["launches"]:
                 cand.append(dict(kernel=f"k_amg_face_cheb<{nt}, __half> (level-0 Chebyshev sweep, p={bn.p} bin)",
-                                 key=f"c4:k_amg_face_cheb<{nt}>", mean_ms=smp["ms"] / smp["launches"],
+                                 key=f"c4:k_amg_face_cheb<{nt}>", family="level-0 sweeps",
+                                 mean_ms=smp["ms"] / smp["launches"],
                                  bytes_per_launch=smp["bytes"] / smp["launches"], launches=it_launched * 2 * k,
                                  full_launch_bytes=bn.ndofs * (5 * 2 * nt + 20 / nt + 20),
                                  sampled_launches=smp["launches"]))
+                # the first coarse level's l1-Jacobi sweeps, timed in the same sampled chunks
+                l1 = bn.kernel_sample(2)
+                if l1["launches"]:
+                    per_it = l1["launches"] / (smp["launches"] / (2 * k))  # sweeps per V-cycle
+                    cand.append(dict(kernel=f"k_amg_l1_sweep<4> (first coarse level, p={bn.p} bin)",
+                                     key="c4:k_amg_l1_sweep<4>", family="coarse sweeps",
+                                     mean_ms=l1["ms"] / l1["launches"],
+                                     bytes_per_launch=l1["bytes"] / l1["launches"], launches=it_launched * per_it,
+                                     full_launch_bytes=None, sampled_launches=l1["launches"]))
         if t["cg_samples"]:
             cand.append(dict(kernel=f"k_cg_a<{nt}, double> (FP64 q = A z + beta q, p={bn.p} bin)", key=f"c4:k_cg_a<{nt}>",
-                             mean_ms=t["cg_a_ms"], bytes_per_launch=t["cg_a_bytes"], launches=it_launched,
+                             family="FP64 products", mean_ms=t["cg_a_ms"], bytes_per_launch=t["cg_a_bytes"], launches=it_launched,
                              full_launch_bytes=bn.ndofs * (40 * nt + 20 / nt + 40), sampled_launches=t["cg_samples"]))
     for c in cand:
         c["est_ms_per_step"] = c["mean_ms"] * c["launches"]
         c["est_bytes_per_step"] = c["bytes_per_launch"] * c["launches"]
-    fam = [c for c in cand if c["key"].startswith("c4:k_amg_face_cheb")] or cand
+    # the family with the most live time per step (summed over the bins), then its instance that
+    # moves the most bytes
+    fam_ms = {}
+    for c in cand:
+        fam_ms[c["family"]] = fam_ms.get(c["family"], 0.0) + c["est_ms_per_step"]
+    top = max(fam_ms, key=fam_ms.get) if fam_ms else None
+    fam = [c for c in cand if c["family"] == top]
     dom = max(fam, key=lambda c: c["est_bytes_per_step"]) if fam else None
     rl = None
     if dom:
@@ -219,6 +235,7 @@ def c4_rooflines(H, B, tims, pc, hbm, peak_kind):
               "avg_launch_ms": dom["mean_ms"], "sampled_launches": dom["sampled_launches"],
               "algorithmic_bytes_per_full_launch": dom["full_launch_bytes"],
               "est_ms_per_step": dom["est_ms_per_step"],
+              "family": dom["family"], "family_ms_per_step": fam_ms,
               "how": "CUDA events around each launch of the sampled (un-graphed) CG chunks of the timed step, on "
                      "the bin's stream while the other bins run; bytes = rows of the problems that iterated x "
                      "bytes per row; traffic: ncu dram read+write per launch of the same kernel in the same bench "
@@ -227,6 +244,15 @@ def c4_rooflines(H, B, tims, pc, hbm, peak_kind):
               "fallback 6.8 TB/s",
               "others": [{kk: c[kk] for kk in ("kernel", "mean_ms", "bytes_per_launch", "launches", "est_ms_per_step")}
                          for c in sorted(cand, key=lambda c: -c["est_ms_per_step"])[:6]]}
+    # the level-0 sweep, the largest HBM stream of the cycle, beside it (its traffic is captured)
+    l0 = [c for c in cand if c["family"] == "level-0 sweeps"]
+    if rl is not None and l0 and dom["family"] != "level-0 sweeps":
+        c0 = max(l0, key=lambda c: c["est_bytes_per_step"])
+        a0 = c0["bytes_per_launch"] / (c0["mean_ms"] / 1e3) / 1e9
+        rl["level0_sweep"] = {"kernel": c0["kernel"], "achieved": a0, "frac": a0 / hbm,
+                              "traffic": profile_traffic(c0["key"]),
+                              "algorithmic_bytes_per_launch": c0["bytes_per_launch"], "avg_launch_ms": c0["mean_ms"],
+                              "algorithmic_bytes_per_full_launch": c0["full_launch_bytes"]}
     el = []
     tot_b = tot_f = tot_nom = tot_ms = 0.0
     for bn, t in zip(B.bins, tims):

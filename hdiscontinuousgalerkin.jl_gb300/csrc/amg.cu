@@ -694,7 +694,7 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
     H->tail_tab.upload(tab.data(), tab.size(), st);
   }
   H->built = true;
-  if (verbose) {  // level sizes: rows (largest problem's rows); host time of the set-up phases (ms)
+  if (verbose) {  // level sizes: rows (largest problem's rows; nonzeros); host time of the set-up phases (ms)
     tph[7] = clk();
     std::fprintf(stderr, "amg setup ms: strength %.1f agg0 %.1f p0 %.1f level1 %.1f upload0 %.1f coarse %.1f upload %.1f\n",
                  1e3 * (tph[1] - tph[0]), 1e3 * (tph[2] - tph[1]), 1e3 * (tph[3] - tph[2]), 1e3 * (tph[4] - tph[3]),
@@ -703,7 +703,7 @@ void amg_setup_symbolic(hdg_system* s, const std::vector<char>& dirichlet_face) 
     for (const AmgLevel& L : H->lev) {
       std::vector<int> cnt(s->nprob, 0);
       for (int i = 0; i < L.n; ++i) ++cnt[L.h_prob[i]];
-      std::fprintf(stderr, ", %d (%d)", L.n, *std::max_element(cnt.begin(), cnt.end()));
+      std::fprintf(stderr, ", %d (%d; %zu nnz)", L.n, *std::max_element(cnt.begin(), cnt.end()), L.h_col.size());
     }
     std::fprintf(stderr, "; tail from level %d\n", H->tail_from + 1);
   }
@@ -1733,8 +1733,14 @@ void apply_nt(hdg_system* s, const VT* val0, const float* b0, float* z0, const i
     float* cur = L.x.p;
     float* oth = L.t.p;
     for (int sw = 1; sw < nu; ++sw) {
+      EventPair* ep = (s->prof_cheb0 && l == 0) ? new EventPair() : nullptr;  // sampled chunk: time level 1
+      if (ep) ep->start(st);
       AMG_LAUNCH_G(k_amg_l1_sweep, L.n, st, L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, cur, oth, L.prob.p,
                    cst);
+      if (ep) {
+        ep->stop(st);
+        s->ev_l1.push_back(ep);
+      }
       std::swap(cur, oth);
     }
     iter[l] = cur;
@@ -1766,7 +1772,13 @@ void apply_nt(hdg_system* s, const VT* val0, const float* b0, float* z0, const i
     float* b = L.r.p;
     AMG_LAUNCH_G(k_amg_prolong, L.n, st, L.n, L.pptr.p, L.pcol.p, L.pval.p, fin[l + 1], a, L.prob.p, cst);
     for (int sw = 0; sw < nu; ++sw) {
+      EventPair* ep = (s->prof_cheb0 && l == 0) ? new EventPair() : nullptr;
+      if (ep) ep->start(st);
       AMG_LAUNCH_G(k_amg_l1_sweep, L.n, st, L.n, L.ptr.p, L.col.p, L.val.p, L.dl1inv.p, L.b.p, a, b, L.prob.p, cst);
+      if (ep) {
+        ep->stop(st);
+        s->ev_l1.push_back(ep);
+      }
       std::swap(a, b);
     }
     fin[l] = a;
@@ -1845,6 +1857,18 @@ double amg_cheb0_bytes_per_row(const hdg_system* s) {
   const double nt = H->nt, vb = H->val0h.p ? 2.0 : 4.0;
   const int k = amg_cheb_degree();
   return (16.0 + 4.0 * nt) + (2 * k - 1) * (5.0 * vb * nt + 20.0 / nt + 20.0);
+}
+
+// Algorithmic bytes per trace row of the first coarse level's l1-Jacobi sweeps in one V-cycle
+// (2 nu - 1 of them): each reads the level's CSR values and columns (8 per entry), row pointers,
+// b, dl1, the iterate (neighbour values counted once, at their own row) and writes the new
+// iterate: 8 nnz + 20 n bytes per sweep, spread over the trace rows.
+double amg_l1sweep_bytes_per_row(const hdg_system* s) {
+  const AmgHierarchy* H = s->amg;
+  if (!H || H->lev.size() < 2) return 0.0;
+  const AmgLevel& L = H->lev[0];
+  const double per_sweep = 8.0 * (double)L.h_col.size() + 20.0 * L.n;
+  return (2 * amg_coarse_sweeps(s) - 1) * per_sweep / ((double)H->nf * H->nt);
 }
 
 int amg_cycle_launches(const hdg_system* s) {

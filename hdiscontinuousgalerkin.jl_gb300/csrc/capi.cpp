@@ -60,6 +60,7 @@ hdg_system::~hdg_system() {
   for (auto* e : ev_cg_a) delete e;
   for (auto* e : ev_cg_b) delete e;
   for (auto* e : ev_cheb0) delete e;
+  for (auto* e : ev_l1) delete e;
 }
 
 extern "C" {
@@ -917,14 +918,16 @@ int hdg_system_timings(hdg_system* s, hdg_timings* out) {
 
 int hdg_system_kernel_sample(hdg_system* s, int which, double* total_ms, double* total_bytes, int* launches) {
   if (!s || !total_ms || !total_bytes || !launches) return HDG_ERR_ARG;
-  if (which != HDG_SAMPLE_CHEB0) return fail(s->ctx, HDG_ERR_ARG, "unknown kernel sample");
+  if (which != HDG_SAMPLE_CHEB0 && which != HDG_SAMPLE_L1SWEEP)
+    return fail(s->ctx, HDG_ERR_ARG, "unknown kernel sample");
   return guard(s->ctx, [&]() -> int {
     set_device(s->ctx);
+    const std::vector<EventPair*>& ev = which == HDG_SAMPLE_CHEB0 ? s->ev_cheb0 : s->ev_l1;
     double t = 0.0;
-    for (auto* e : s->ev_cheb0) t += e->ms();
+    for (auto* e : ev) t += e->ms();
     *total_ms = t;
-    *total_bytes = s->prof_cheb0_bytes;
-    *launches = (int)s->ev_cheb0.size();
+    *total_bytes = which == HDG_SAMPLE_CHEB0 ? s->prof_cheb0_bytes : s->prof_l1_bytes;
+    *launches = (int)ev.size();
     return HDG_OK;
   });
 }

@@ -594,6 +594,9 @@ template <int NT> struct SolverNT : CgSolver {
     for (auto* e : s->ev_cheb0) delete e;
     s->ev_cheb0.clear();
     s->prof_cheb0_bytes = 0.0;
+    for (auto* e : s->ev_l1) delete e;
+    s->ev_l1.clear();
+    s->prof_l1_bytes = 0.0;
     sample_pending = false;
     it_prev.assign(nprob, 0);
     if (s->ctx->profiling) s->ev_cg.start(st);
@@ -792,7 +795,10 @@ template <int NT> struct SolverNT : CgSolver {
     }
     s->prof_a_bytes += rows_it * bytes_per_row_a();
     s->prof_b_bytes += rows_it * bytes_per_row_b();
-    if (mg) s->prof_cheb0_bytes += rows_it * amg_cheb0_bytes_per_row(s);
+    if (mg) {
+      s->prof_cheb0_bytes += rows_it * amg_cheb0_bytes_per_row(s);
+      s->prof_l1_bytes += rows_it * amg_l1sweep_bytes_per_row(s);
+    }
   }
 
   bool process(const hdg_solver& o) override {

@@ -312,6 +312,8 @@ struct hdg_system {
   // defaults instead.
   bool amg_tune_time = true;
   std::vector<EventPair*> ev_cheb0;
+  std::vector<EventPair*> ev_l1;  // sampled chunks: each l1-Jacobi sweep of the first coarse level
+  double prof_l1_bytes = 0.0;     // their algorithmic bytes (rows of the problems that iterated)
   double prof_cheb0_bytes = 0.0;  // their algorithmic bytes (rows of the problems that iterated)
   // algorithmic bytes moved by the sampled CG launches (rows of the problems that iterated)
   double prof_a_bytes = 0.0, prof_b_bytes = 0.0;
@@ -396,6 +398,7 @@ void amg_setup_numeric(hdg_system* s, cudaStream_t st);
 void amg_apply(hdg_system* s, const float* r, float* z, const int32_t* cg_state, cudaStream_t st);
 int amg_cycle_launches(const hdg_system* s);                             // kernels per V-cycle
 double amg_cycle_bytes(const hdg_system* s);                             // algorithmic bytes per V-cycle
+double amg_l1sweep_bytes_per_row(const hdg_system* s);  // first-coarse-level sweeps per cycle, per trace row
 double amg_cheb0_bytes_per_row(const hdg_system* s);  // level-0 sweeps of one V-cycle, per trace row
 
 void mesh_build_rectangle(hdg_mesh* m, int nx, int ny, const double LL[2], const double UR[2]);

@@ -250,8 +250,10 @@ int hdg_system_timings(hdg_system* sys, hdg_timings* out);
 /* No reference counterpart.  One kernel family timed launch by launch in the sampled chunks of
  * the last solve (profiling on): the summed CUDA-event durations, the summed algorithmic bytes
  * (rows of the problems that iterated times the bytes per row) and the number of launches.
- * HDG_SAMPLE_CHEB0: the level-0 Chebyshev smoother sweeps of the multigrid cycle. */
+ * HDG_SAMPLE_CHEB0: the level-0 Chebyshev smoother sweeps of the multigrid cycle;
+ * HDG_SAMPLE_L1SWEEP: the l1-Jacobi sweeps of the first coarse level. */
 #define HDG_SAMPLE_CHEB0 1
+#define HDG_SAMPLE_L1SWEEP 2
 int hdg_system_kernel_sample(hdg_system* sys, int which, double* total_ms, double* total_bytes, int* launches);
 
 /* ---- batches of independent problems ------------------------------------------------ */

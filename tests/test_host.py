@@ -297,6 +297,37 @@ def test_bench_cpu_sample_is_stratified():
     assert sizes[0] <= alln[len(alln) // 40] and sizes[-1] >= alln[-len(alln) // 40 - 1]
 
 
+def test_bench_roofline_selection():
+    """The bench's roofline picks the kernel family with the most live time per step and, in it,
+    the instance moving the most bytes; the level-0 sweep is reported beside it with the traffic
+    of its committed ncu summary (stand-in bins: no GPU)."""
+    import types
+    import bench
+
+    class Bin:
+        def __init__(self, p, nd, l0, l1):
+            self.p, self.ndofs, self.idx = p, nd, [0]
+            self.mesh = types.SimpleNamespace(ncells=1000)
+            self._s = {1: l0, 2: l1}
+
+        def kernel_sample(self, which):
+            ms, by, n = self._s[which]
+            return {"ms": ms, "bytes": by, "launches": n}
+
+    H = types.SimpleNamespace(PRECOND_AMG=1)
+    bins = [Bin(1, 1000, (1.0, 1e9, 32), (2.0, 1e8, 56)), Bin(4, 5000, (1.5, 4e9, 32), (2.5, 3e8, 56))]
+    B = types.SimpleNamespace(bins=bins, stats=[types.SimpleNamespace(iterations=100)])
+    tims = [{"cg_samples": 8, "cg_a_ms": 0.1, "cg_a_bytes": 1e8, "element_ms": 5.0}] * 2
+    rl, rle = bench.c4_rooflines(H, B, tims, 1, 6769.1, "measured")
+    assert rl["family"] == "coarse sweeps" and "p=4 bin" in rl["kernel"]
+    assert rl["family_ms_per_step"]["coarse sweeps"] > rl["family_ms_per_step"]["level-0 sweeps"]
+    assert abs(rl["achieved"] - (3e8 / 56) / (2.5e-3 / 56) / 1e9) < 1e-9
+    l0 = rl["level0_sweep"]
+    assert "k_amg_face_cheb<5" in l0["kernel"] and l0["traffic"] == bench.profile_traffic("c4:k_amg_face_cheb<5>")
+    assert l0["traffic"] is not None
+    assert rle["bound"] == "fp64 pipe" and len(rle["bins"]) == 2
+
+
 @pytest.mark.parametrize("kind,prm,code,word", [
     (2, [3.0, 0.5, 0.5, 0.1, 1.0], -1, b"BUMPS"),        # K = 3 bumps, parameters for one
     (1, [1.0], -1, b"SINSIN"),                          # sin sin needs a, kx, ky
