@@ -2,8 +2,11 @@
 ``src/…jl:N-M``, ``examples/…jl:N``, ``test/…jl:N``) in this repository's sources and documents
 points inside the cited file, and that the cited file exists.
 
-The reference tree is read from the first argument, else from $HDG_REFERENCE_TREE, else from
-/root/reference.  Usage:  python tests/golden/check_citations.py [reference-tree]
+Scanned: the package, the oracle, the tests, the C header, the top-level Python files and the
+repository's own user-facing documents (DOCS below); files that review or survey the project
+are not part of it and are not scanned.  The reference tree is read from the first argument,
+else from $HDG_REFERENCE_TREE, else from the reference checkout of the build machine.
+Usage:  python tests/golden/check_citations.py [reference-tree]
 Prints one line per bad citation and exits 1 if there is any.
 """
 from __future__ import annotations
@@ -16,10 +19,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 CITE = re.compile(r"((?:src|examples|test)/[A-Za-z0-9_./]+?\.jl):(\d+)(?:\s*[-–]\s*(\d+))?((?:\s*,\s*:?\d+(?:\s*[-–]\s*\d+)?)*)")
 MORE = re.compile(r":?(\d+)(?:\s*[-–]\s*(\d+))?")
-SKIP_DIRS = {".git", "_work", "gpurun_out", "_build", "__pycache__", "baseline", ".pytest_cache"}
+SKIP_DIRS = {"_build", "__pycache__", ".pytest_cache"}
 EXTS = (".py", ".cpp", ".cu", ".cuh", ".h", ".md")
-# files whose citations are the judge's or the driver's, not the product's
-SKIP_FILES = {"VERDICT.md", "ADVICE.md", "SURVEY.md", "BASELINE.md", "BASELINE.json"}
+SOURCE_DIRS = ("hdiscontinuousgalerkin.jl_gb300", "oracle", "tests", "include", "profiles")
+DOCS = ("DESIGN.md", "INTEGRATION.md", "README.md")
 
 
 def reference_tree(argv=None):
@@ -30,13 +33,21 @@ def reference_tree(argv=None):
     return None
 
 
+def scanned_files():
+    for top in SOURCE_DIRS:
+        for d, dirs, files in os.walk(os.path.join(ROOT, top)):
+            dirs[:] = [x for x in dirs if x not in SKIP_DIRS]
+            for fn in files:
+                if fn.endswith(EXTS):
+                    yield os.path.join(d, fn)
+    for fn in sorted(os.listdir(ROOT)):
+        if fn.endswith(".py") or fn in DOCS:
+            yield os.path.join(ROOT, fn)
+
+
 def citations():
-    for d, dirs, files in os.walk(ROOT):
-        dirs[:] = [x for x in dirs if x not in SKIP_DIRS]
-        for fn in files:
-            if not fn.endswith(EXTS) or fn in SKIP_FILES:
-                continue
-            path = os.path.join(d, fn)
+    for path in scanned_files():
+        if os.path.isfile(path):
             with open(path, encoding="utf-8", errors="replace") as fh:
                 for ln, text in enumerate(fh, 1):
                     for m in CITE.finditer(text):
