@@ -163,8 +163,9 @@ def element_cost(p, schur):
     """Per-cell algorithmic bytes and FP64 FLOPs of the element kernel of degree p.  Bytes: read 3
     node ids, 6 coordinates, the orientation byte and kappa (69 B); write [Ate | bte] and the stored
     rows of [K_e | b_e] (all n rows on the full path, the nw u rows on the Cholesky-Schur path).
-    FLOPs: the operations the kernel performs (2 per FMA); the dense-LU count of the survey (2/3 n^3
-    + 2 n^2 (m+1) + 2 m^2 n + ...) is the nominal work and is reported beside it."""
+    FLOPs: the operations the kernel performs (2 per FMA); the count of a dense LU of the n x n local
+    system with m+1 right-hand sides and the Ate product (2/3 n^3 + 2 n^2 (m+1) + 2 m^2 n) is the
+    nominal work and is reported beside it."""
     nw, nt = (p + 1) * (p + 2) // 2, p + 1
     n, m = 3 * nw, 3 * nt
     rc = nw + m + 1

@@ -3,8 +3,8 @@
 points inside the cited file, and that the cited file exists.
 
 Scanned: the package, the oracle, the tests, the C header, the top-level Python files and the
-repository's own user-facing documents (DOCS below); files that review or survey the project
-are not part of it and are not scanned.  The reference tree is read from the first argument,
+repository's own user-facing documents (DOCS below); other documents at the top level are
+not part of the product and are not scanned.  The reference tree is read from the first argument,
 else from $HDG_REFERENCE_TREE, else from the reference checkout of the build machine.
 Usage:  python tests/golden/check_citations.py [reference-tree]
 Prints one line per bad citation and exits 1 if there is any.
