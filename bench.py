@@ -262,6 +262,7 @@ def c4_rooflines(H, B, tims, pc, hbm, peak_kind):
         cells = bn.mesh.ncells
         ms = t["element_ms"]
         el.append({"p": bn.p, "path": "cholesky-schur" if schur else "full LU", "cells": cells, "ms": ms,
+                   "elements_per_s": cells / (ms / 1e3) if ms else None,
                    "gbs": cells * nb / (ms / 1e3) / 1e9 if ms else None,
                    "fp64_tflops": cells * fl / (ms / 1e3) / 1e12 if ms else None})
         tot_b += cells * nb
@@ -276,6 +277,7 @@ def c4_rooflines(H, B, tims, pc, hbm, peak_kind):
              "fp64_frac": tot_f / (tot_ms / 1e3) / 1e12 / FP64_TFLOPS_MEASURED if tot_ms else None,
              "nominal_dense_lu_tflops": tot_nom / (tot_ms / 1e3) / 1e12 if tot_ms else None,
              "ms_sum_of_bins": tot_ms, "bins": el,
+             "elements_per_s": sum(b["cells"] for b in el) / (tot_ms / 1e3) if tot_ms else None,
              "how": "element kernel of each bin timed with CUDA events in the timed step (bins run concurrently, so "
                     "each kernel shares the GPU); HBM fraction of measured copy bandwidth and FP64 fraction of the "
                     "measured FMA rate"}

@@ -326,6 +326,7 @@ def test_bench_roofline_selection():
     assert "k_amg_face_cheb<5" in l0["kernel"] and l0["traffic"] == bench.profile_traffic("c4:k_amg_face_cheb<5>")
     assert l0["traffic"] is not None
     assert rle["bound"] == "fp64 pipe" and len(rle["bins"]) == 2
+    assert abs(rle["elements_per_s"] - 2000 / 10e-3) < 1e-6 and rle["bins"][0]["elements_per_s"] == 1000 / 5e-3
 
 
 @pytest.mark.parametrize("kind,prm,code,word", [
