@@ -171,7 +171,8 @@ int hdg_apply_dirichlet(hdg_system* sys, const int32_t* dofs, const double* vals
 /* Preconditioner of the trace CG. */
 enum {
   HDG_PRECOND_JACOBI = 0, /* diagonal (the default) */
-  HDG_PRECOND_AMG = 1     /* smoothed-aggregation multigrid V(2,2) cycle in FP32 (CG itself in FP64) */
+  HDG_PRECOND_AMG = 1     /* smoothed-aggregation multigrid V-cycle in FP32 (CG itself in FP64): Chebyshev
+                             smoothing on the trace level, l1-Jacobi on the coarse levels */
 };
 typedef struct {
   double tol;         /* relative residual |r|/|b| to reach (default 1e-12) */
