@@ -214,6 +214,37 @@ def test_unstructured_figure1_reader_matches_oracle(H, oracle):
         assert [H.face_orientation(m, c + 1, f + 1) for f in range(3)] == [om.orientation(c, f) for f in range(3)]
 
 
+def test_generated_unstructured_mesh_reader_matches_oracle(H, oracle, tmp_path):
+    """A Delaunay mesh written by tests/golden/make_unstructured_mesh.py (the generator of the
+    at-scale GPU test, here with 42 x 42 points): its cells are counter-clockwise, its boundary
+    edges are exactly the edges on the square's sides, and the library's reader gives the oracle's
+    topology, first-visit face numbering, boundary set and orientations bit for bit."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import make_unstructured_mesh as gen
+    xy, tri, edges, bnd = gen.unstructured_square(42, 7)
+    a, b, c = xy[tri[:, 0]], xy[tri[:, 1]], xy[tri[:, 2]]
+    assert np.all((b[:, 0] - a[:, 0]) * (c[:, 1] - a[:, 1]) - (b[:, 1] - a[:, 1]) * (c[:, 0] - a[:, 0]) > 0)
+    mid = 0.5 * (xy[edges[:, 0]] + xy[edges[:, 1]])
+    on_side = (np.isclose(mid[:, 0], 0) | np.isclose(mid[:, 0], 1) | np.isclose(mid[:, 1], 0)
+               | np.isclose(mid[:, 1], 1))
+    assert np.array_equal(on_side, bnd == 1)
+    root = str(tmp_path / "sq")
+    nc = gen.write_triangle_mesh(root, 42, 7)
+    assert nc == len(tri) > 3000
+    m = H.parse_mesh_triangle(root, ctx=None)
+    om = oracle.parse_mesh_triangle(root)
+    assert (m.nnodes, m.ncells, m.nfaces) == (om.nnodes, om.ncells, om.nfaces) == (42 * 42, nc, len(edges))
+    xyl, cn, cf, fc = m._topology()
+    assert np.array_equal(xyl, om.xy)
+    assert np.array_equal(cn, om.cells) and np.array_equal(cf, om.cell_faces)
+    assert np.array_equal(fc, om.faces)
+    assert sorted(H.getfaceset(m, "boundary")) == sorted(om.faceset("boundary").tolist())
+    assert len(H.getfaceset(m, "boundary")) == int(bnd.sum())
+    for cc in range(0, m.ncells, 97):
+        assert [H.face_orientation(m, cc + 1, f + 1) for f in range(3)] == [om.orientation(cc, f) for f in range(3)]
+
+
 def test_write_vtk_roundtrip(H, tmp_path):
     """The headless output that stands in for the reference's Makie plot: a legacy VTK file whose
     points, triangles and fields read back as written."""
